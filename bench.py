@@ -1,0 +1,298 @@
+#!/usr/bin/env python
+"""Benchmark of the FDTD step loop (one JSON line on stdout, rank 0).
+
+Workload: the heterogeneous-dielectric grid, 320×192×128 cells, 12-cell CPML
+(CUDA-path CPML semantics), Si strip + random 2×2×0.22 µm design region,
+y-polarised Gaussian current plane, two 21-frequency flux planes with
+Kahan-compensated FP32 DFT accumulation; FP32 bulk arithmetic.  A "step" is
+one full FDTD time step (H half-step + E half-step + DFT on decimation steps)
+over the whole grid; the metric is cell-updates per second.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Multi-GPU: replicas only (one independent simulation per GPU, no collective
+on the data path); value = all ranks' cell-updates / max-over-ranks time.
+The reference arm times the CPU restatement of the reference's CPU step loop
+(the reference is Julia and cannot run here) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import __graft_entry__  # noqa: E402
+
+METRIC = "Gcell-updates/s & %HBM roofline; serve p50/p99 latency at 1e-4 flux error"
+UNIT = "Gcell-updates/s"
+WORKLOAD = ("waveguide 320x192x128 FP32, 12-cell CPML (CUDA-path semantics), Si strip eps 12.25 in "
+            "eps 2.085 + random 2x2x0.22um design (seed 1234, 3-cell box filter), Ey Gaussian current "
+            "plane (waist 0.4um), Gaussian pulse fcen=1/1.55 fwidth=0.25fcen, 2 flux planes x 21 freqs, "
+            "Kahan FP32 DFT")
+
+
+def dist_env():
+    return int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), int(
+        os.environ.get("LOCAL_RANK", "0"))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int, period_ms: int = 100):
+        self.cmd = ["nvidia-smi", "-i", str(gpu_index), f"--query-gpu={self.FIELDS}",
+                    "--format=csv,noheader,nounits", f"-lms", str(period_ms)]
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(self.cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.thread.join(timeout=5)
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / "dram_traffic.json"
+    if not p.exists():
+        return None
+    d = json.loads(p.read_text())
+    v = d.get(kernel)
+    return None if v is None else float(v)
+
+
+def build_workload(dtype="f32", semantics="cpml"):
+    __graft_entry__.package()
+    from khronos_gb300 import configs
+
+    w = configs.waveguide(dtype=dtype)
+    w.sim.semantics = semantics
+    return w, w.sim.spec()
+
+
+def cpu_baseline(spec, budget_s=12.0):
+    """The CPU restatement on the host cores, on a bounded number of full-grid steps."""
+    orc = __graft_entry__._oracle()
+    o = orc.OracleSim(spec)
+    t0 = time.perf_counter()
+    o.step(2)
+    per = max((time.perf_counter() - t0) / 2, 1e-6)
+    n = int(max(3, min(200, budget_s / per)))
+    t0 = time.perf_counter()
+    o.step(n)
+    dt = time.perf_counter() - t0
+    o.close()
+    cells = spec.cells
+    return {"value": cells * n / dt / 1e9, "unit": UNIT, "cores": orc.num_threads(), "kind": "port",
+            "sample": f"{n} full-grid steps of the same workload after 2 warm-up steps "
+                      f"({cells} cells, FP32, C++ restatement of the reference CPU step loop, OpenMP)"}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return 0
+    w, spec = build_workload("f32", "reference_cpu")
+    orc = __graft_entry__._oracle()
+    o = orc.OracleSim(spec)
+    o.step(max(args.warmup, 1))
+    # each timed step is one full-grid step; bound the run to about a minute
+    t0 = time.perf_counter()
+    o.step(1)
+    per = max(time.perf_counter() - t0, 1e-6)
+    k = int(max(1, min(args.steps, 60.0 / per)))
+    t0 = time.perf_counter()
+    o.step(k)
+    dt = time.perf_counter() - t0
+    value = spec.cells * k / dt / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": k, "warmup": args.warmup, "ms_per_step": dt / k * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD.replace("CUDA-path semantics", "reference CPU-path semantics"),
+                   "grid": list(spec.n), "note": "reference is Julia (absent); timed: its CPU step loop "
+                                                 "restated in C++ (oracle/), all host threads"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": orc.num_threads(), "kind": "port",
+                         "sample": f"{k} full-grid steps (requested {args.steps}) after {args.warmup} warm-up"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, world, rank, local_rank):
+    import torch
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+
+        dist_mod.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+        dist = dist_mod
+    __graft_entry__.package()
+    from khronos_gb300.device import GpuSim
+
+    w, spec = build_workload("f32", "cpml")
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+
+    # ---- device-resident run: inputs already in HBM --------------------------
+    gpu = GpuSim(spec)
+    gpu.step(args.warmup, sh)
+    torch.cuda.synchronize()
+    h_bytes, e_bytes, dft_bytes = gpu.model_bytes_split()
+    launches0 = gpu.launches
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clk:
+        start.record(stream)
+        h_ms, e_ms, dft_ms = gpu.step_timed(args.steps, sh)
+        end.record(stream)
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms = start.elapsed_time(end)
+    launches = gpu.launches - launches0
+    t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    cells = spec.cells
+    value = world * cells * args.steps / (ms_max / 1e3) / 1e9
+    gpu.close()
+
+    # ---- end to end through the C ABI with host buffers ------------------------
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    g2 = GpuSim(spec)  # host arrays -> device (materials, σ, sources, monitors)
+    g2.step(args.steps, sh)
+    dft_host = [g2.dft(m) for m in range(len(spec.monitors))]
+    fluxes = [g2.flux(list(range(4 * i, 4 * i + 4)), fm.normal_axis, fm.dA)
+              for i, fm in enumerate(w.flux_monitors)]
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    g2.close()
+    h2d = sum(a.nbytes for _, _, a in spec.materials) // 2  # values cross as the run's FP32
+    h2d += sum(s.amp.size * 16 for s in spec.sources) + sum(x.size * 8 for x in spec.sigma_b + spec.sigma_d
+                                                            if x is not None)
+    d2h = sum(d.size * 16 for d in dft_host) + sum(f.size * 8 for f in fluxes)
+    t2 = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+    if dist:
+        dist.all_reduce(t2, op=dist.ReduceOp.MAX)
+    e2e_value = world * cells * args.steps / float(t2.item()) / 1e9
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+    peak, peak_kind = measured_peaks()
+    e_launch_ms = e_ms / args.steps
+    achieved = e_bytes / (e_launch_ms / 1e3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "grid": list(spec.n), "cells": cells,
+                   "l2": "inputs larger than L2 (fields+materials+CPML state ~0.9 GB per replica vs 129 MB L2); no flush",
+                   "parallelism": f"replicas{world}" if world > 1 else "single"},
+        "roofline": {"bound": "hbm", "kernel": "half_step_kernel<float,E>", "achieved": achieved, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "algorithmic_bytes_per_launch": e_bytes,
+                     "traffic": ncu_traffic("half_step_kernel<float,E>"),
+                     "h_kernel": {"achieved": h_bytes / (h_ms / args.steps / 1e3) / 1e9,
+                                  "algorithmic_bytes_per_launch": h_bytes, "ms_per_launch": h_ms / args.steps},
+                     "e_ms_per_launch": e_launch_ms, "dft_ms_per_step": dft_ms / args.steps,
+                     "step_model_bytes": h_bytes + e_bytes + dft_bytes,
+                     "step_achieved": (h_bytes + e_bytes + dft_bytes) / (ms_max / args.steps / 1e3) / 1e9},
+        "clocks": clk.summary(),
+        "gpu_launches": launches,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d / args.steps,
+                "d2h_bytes_per_step": d2h / args.steps,
+                "scope": "GpuSim(spec) from host arrays + K steps + DFT arrays and flux read back to host"},
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(spec)
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args(argv)
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local_rank = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, world, rank)
+    return run_ours(args, world, rank, local_rank)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,205 @@
+/*
+ * khronos_gb300.h — C ABI of the GB300-native FDTD step loop.
+ *
+ * One `kh_sim` handle owns the device state of one single-domain Yee grid
+ * (fields, CPML auxiliaries, materials, dispersive poles, sources, DFT
+ * monitors).  Every entry point returns a kh_status; nothing aborts or
+ * throws across the boundary.  A handle is single-threaded; distinct handles
+ * may run concurrently on distinct streams.  Device work is enqueued on the
+ * stream passed to kh_sim_step (a cudaStream_t passed as void*, NULL = the
+ * legacy default stream); the library uses the CUDA primary context of the
+ * current device, exactly like CUDA.jl does.
+ *
+ * Reference interface each group of calls replaces (Khronos.jl sources):
+ *   kh_sim_create / kh_sim_prepare   prepare_simulation!   src/Simulation.jl:92-283
+ *                                    (field allocation Chunking.jl:1069-1146,
+ *                                     PML σ Boundaries.jl:99-164)
+ *   kh_sim_set_material              GeometryData arrays   src/DataStructures.jl:214-242,
+ *                                    per-chunk slicing     src/Chunking.jl:1159-1213
+ *   kh_sim_add_pole                  init_polarization!    src/Geometry.jl:1136-1355
+ *   kh_sim_add_source                assemble_sources      src/Sources/Sources.jl:44-92
+ *                                    eval_time_source      src/Sources/TimeSources.jl:61-132,178-184
+ *   kh_sim_add_dft_monitor           init_monitors(::DFTMonitor) src/Monitors/Monitors.jl:202-272
+ *   kh_sim_step                      step!(sim)            src/Kernels/Kernels.jl:20-88
+ *                                    (one call = n iterations of the `run` loop,
+ *                                     src/Simulation.jl:356-362)
+ *   kh_sim_read_dft                  DFTMonitorData.fields download (Array(...))
+ *   kh_sim_flux                      get_flux              src/Monitors/FluxMonitor.jl:92-156
+ *   kh_sim_get_field                 _pull_fields_from_device src/Visualization.jl:294-331
+ *   kh_sim_reset                     reset_fields!         src/Simulation.jl:571-637
+ *   kh_sim_timestep / _sources_active  sim.timestep / sim.sources_active
+ *
+ * Index conventions.  Cells are 0-based: cell (i,j,k) of this ABI is the
+ * reference's Center index (i+1, j+1, k+1).  Per-voxel material arrays are
+ * given over the Center range, x fastest: value[(k*ny + j)*nx + i].  Field
+ * snapshots use the reference's component dimensions (src/utils.jl:26-37),
+ * e.g. Ex is nx × (ny+1) × (nz+1), x fastest; the extra staggered layer is the
+ * zero Dirichlet wall.  Complex host arrays are interleaved (re, im) doubles.
+ */
+#ifndef KHRONOS_GB300_H
+#define KHRONOS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t kh_status;
+#define KH_OK 0
+#define KH_ERR_INVALID 1     /* bad argument or call order */
+#define KH_ERR_OOM 2         /* device or host allocation failed */
+#define KH_ERR_CUDA 3        /* a CUDA runtime call failed */
+#define KH_ERR_TIMEOUT 4     /* a bounded device-side wait gave up */
+#define KH_ERR_NAN 5         /* non-finite field value detected */
+#define KH_ERR_UNSUPPORTED 6 /* configuration the reference itself rejects */
+
+#define KH_F32 0
+#define KH_F64 1
+
+/* Field components, in the reference's order Ex, Ey, Ez, Hx, Hy, Hz. */
+#define KH_EX 0
+#define KH_EY 1
+#define KH_EZ 2
+#define KH_HX 3
+#define KH_HY 4
+#define KH_HZ 5
+
+/* Material array kinds for kh_sim_set_material (comp = 0,1,2 for x,y,z). */
+#define KH_MAT_EPS_INV 0   /* ε⁻¹ per voxel, per component              */
+#define KH_MAT_MU_INV 1    /* μ⁻¹ per voxel, per component              */
+#define KH_MAT_SIGMA_D 2   /* electric conductivity σD (raw, not ×Δt/2) */
+#define KH_MAT_SIGMA_B 3   /* magnetic conductivity σB (raw)            */
+#define KH_MAT_CHI3 4      /* χ(3) on the Center grid (comp ignored)    */
+
+/* Time profiles of a source. */
+#define KH_TIME_GAUSSIAN 0 /* GaussianPulseData  TimeSources.jl:78-132  */
+#define KH_TIME_CW 1       /* ContinuousWaveData TimeSources.jl:53-72   */
+#define KH_TIME_TABLE 2    /* CustomSourceData   TimeSources.jl:157-190 (host-tabulated) */
+
+typedef struct kh_sim kh_sim;
+
+/* Grid and boundary description.  All floating values are the ones the
+ * reference's SimulationData stores (already rounded to the run's precision
+ * when dtype == KH_F32), passed as double. */
+typedef struct {
+  int32_t n[3];        /* Nx, Ny, Nz (cells)                                   */
+  int32_t dtype;       /* KH_F32 or KH_F64: precision of fields and arithmetic */
+  double delta[3];     /* Δx, Δy, Δz                                          */
+  double dt;           /* Δt                                                   */
+  /* PML region widths in cells per axis and side: ceil(L/Δ) as in
+   * Chunking.jl:121-122 and 642-643; 0 = no PML on that side.  A width equal
+   * to n[a] on the low side marks the whole axis as PML (single-chunk plan). */
+  int32_t pml_lo[3];
+  int32_t pml_hi[3];
+  /* PML conductivities sampled at cell centres, length n[a], i.e. the
+   * reference's σ[2i-1] samples of compute_sigma (Boundaries.jl:23-72), already
+   * scaled by Δt/2.  NULL = all zero. */
+  const double* sigma_b[3];
+  const double* sigma_d[3];
+  double eps_inv;      /* scalar ε⁻¹ used where no per-voxel array is set (1) */
+  double mu_inv;       /* scalar μ⁻¹ (1)                                       */
+  int32_t semantics;   /* KH_SEM_*: which of the reference's CPML paths to follow */
+} kh_sim_desc;
+
+/* CPML stage semantics.
+ * KH_SEM_REFERENCE_CPU: the reference's CPU (KernelAbstractions) path:
+ *   generic_curl!/update_field_generic dispatch on the auxiliaries each
+ *   PML-grid chunk allocates (Helpers.jl:39-366, Chunking.jl:1069-1146).  Where
+ *   a chunk has no U array the σ_prev stage is skipped (Helpers.jl:208-223);
+ *   with PML on any axis this makes the CPML grow without bound.
+ * KH_SEM_CPML: the stage logic of the reference's CUDA PML kernels
+ *   (_cuda_pml_BH_kernel!/_cuda_pml_DE_kernel!, CUDAKernels.jl:126-427): U
+ *   (σ_next), T (σ_prev) and W (σ_own) stages each applied whenever their axis
+ *   is PML in the cell's chunk; stable and absorbing. */
+#define KH_SEM_REFERENCE_CPU 0
+#define KH_SEM_CPML 1
+
+/* ADE coefficients of one Lorentz/Drude pole (Susceptibility.jl:60-85). */
+typedef struct {
+  double gamma1_inv;
+  double gamma1;
+  double omega0_dt_sq;
+  double sigma_omega0_dt_sq;
+  double drude_coeff;
+  int32_t is_drude;
+} kh_pole_coeffs;
+
+/* One source component (one SourceData entry, Sources.jl:44-92). */
+typedef struct {
+  int32_t component;   /* KH_EX..KH_HZ                                         */
+  int32_t start[3];    /* 0-based cell of amplitude element (0,0,0)
+                          (= GridVolume.start_idx - 1)                          */
+  int32_t dims[3];     /* amplitude array extent                              */
+  const double* amp;   /* complex amplitudes, interleaved, x fastest           */
+  int32_t time_kind;   /* KH_TIME_*                                            */
+  double fcen;         /* Gaussian / CW centre frequency                       */
+  double width;        /* Gaussian width (1/fwidth_in)                         */
+  double peak_time;    /* Gaussian peak time                                   */
+  double cutoff;       /* Gaussian cutoff, or the TABLE source's end_time      */
+  int64_t table_len;   /* KH_TIME_TABLE: number of steps tabulated             */
+  const double* table; /* KH_TIME_TABLE: 2 complex values per step n:
+                          f(nΔt) then f(nΔt+Δt/2), interleaved                  */
+} kh_source_desc;
+
+/* Library and device information. */
+const char* kh_version(void);
+kh_status kh_device_info(int32_t* sm_count, int32_t* cc_major, int32_t* cc_minor);
+
+/* Lifecycle. */
+kh_status kh_sim_create(const kh_sim_desc* desc, kh_sim** out);
+void kh_sim_destroy(kh_sim* sim);
+const char* kh_last_error(const kh_sim* sim);
+
+/* Set-up (before kh_sim_prepare). */
+kh_status kh_sim_set_material(kh_sim* sim, int32_t kind, int32_t comp, const double* values);
+kh_status kh_sim_add_pole(kh_sim* sim, const kh_pole_coeffs* coeffs, const double* sigma);
+kh_status kh_sim_add_source(kh_sim* sim, const kh_source_desc* src);
+kh_status kh_sim_add_dft_monitor(kh_sim* sim, int32_t component, const int32_t start[3],
+                                 const int32_t dims[3], int32_t nfreq, const double* freqs,
+                                 int32_t decimation, int32_t* out_id);
+kh_status kh_sim_prepare(kh_sim* sim);
+
+/* Time stepping: nsteps full steps of step!(sim) on `stream`. */
+kh_status kh_sim_step(kh_sim* sim, int64_t nsteps, void* stream);
+kh_status kh_sim_synchronize(kh_sim* sim);
+kh_status kh_sim_timestep(const kh_sim* sim, int64_t* out);
+kh_status kh_sim_sources_active(const kh_sim* sim, int32_t* out);
+/* Kernel launches issued since creation (fused half-step + DFT launches). */
+kh_status kh_sim_launch_count(const kh_sim* sim, int64_t* out);
+
+/* Results. */
+kh_status kh_sim_get_field(kh_sim* sim, int32_t component, double* out);
+kh_status kh_sim_read_dft(kh_sim* sim, int32_t monitor_id, double* out);
+kh_status kh_sim_monitor_info(const kh_sim* sim, int32_t monitor_id, int32_t dims[3], int32_t* nfreq);
+/* Poynting flux of four DFT monitors (E1, E2, H1, H2 tangential), FP64 on the
+ * device: S(f) = Σ Re(E1·H2* − E2·H1*)·dA after averaging the two normal layers. */
+kh_status kh_sim_flux(kh_sim* sim, const int32_t ids[4], int32_t normal_axis, double dA,
+                      double* out);
+
+/* State control. */
+kh_status kh_sim_reset(kh_sim* sim);
+kh_status kh_sim_state_bytes(const kh_sim* sim, int64_t* out);
+kh_status kh_sim_export_state(kh_sim* sim, void* host_dst, int64_t bytes);
+kh_status kh_sim_import_state(kh_sim* sim, const void* host_src, int64_t bytes);
+
+/* Compulsory-traffic model of one full step (bytes): the reference's 9 + 12
+ * words per cell (benchmark/benchmark_metrics.jl:236-241) plus CPML
+ * auxiliaries, dispersive and χ3 terms, plus DFT monitor traffic amortised
+ * over the decimation.  The split gives the H half-step kernel, the E
+ * half-step kernel and the DFT launches separately. */
+kh_status kh_sim_model_bytes_per_step(const kh_sim* sim, double* out);
+kh_status kh_sim_model_bytes_split(const kh_sim* sim, double* h_half, double* e_half,
+                                   double* dft);
+
+/* kh_sim_step with CUDA events recorded on `stream` around every launch
+ * group; returns the summed device time (ms) of the H half-step kernels, the
+ * E half-step kernels and the DFT launches of these nsteps. */
+kh_status kh_sim_step_timed(kh_sim* sim, int64_t nsteps, void* stream, double* h_ms,
+                            double* e_ms, double* dft_ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KHRONOS_GB300_H */

@@ -1,0 +1,184 @@
+"""Synthetic workloads with the shapes of the benchmark configurations.
+
+All inputs are synthetic and seeded (no dataset exists for these runs):
+
+* ``dipole``     — 64³ vacuum, 10-cell CPML, Ez point dipole, x-normal flux
+                   plane at 3 frequencies, 1000 steps (FP32 and FP64).
+* ``waveguide``  — 320×192×128, 12-cell CPML, Si strip (ε 12.25) in ε 2.085
+                   cladding through a 2×2×0.22 µm random design region
+                   (ρ ~ U(0,1), seed 1234, 3-cell box filter), Ey current plane
+                   with a 0.4 µm Gaussian profile, two 21-frequency flux planes,
+                   4000 steps.
+* ``dispersive`` — 256³, 12-cell CPML, ε 2.25 slab with χ3 = 1e-3, 4 Lorentz +
+                   4 Drude spheres (seed 42), Ez plane source, 6-face box flux at
+                   11 frequencies, 3000 steps.
+
+``scale`` shrinks the cell counts (same physical layout, coarser or smaller
+grid) so the CPU oracle can run the same layout in seconds.
+
+Shapes are rasterised by sampling each Yee component at its own position
+(first object wins), which is how the reference samples material points
+(src/Geometry.jl:241-248, 353-366), without subpixel smoothing.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from typing import List
+
+import numpy as np
+
+from . import grid as G
+from .monitors import FluxMonitor
+from .simulation import Simulation, apply_chi1_correction
+from .sources import GaussianPulseSource, ProfileSource, UniformSource
+from .spec import DrudeSusceptibility, LorentzianSusceptibility
+
+FCEN = 1 / 1.55
+
+
+@dataclass
+class Workload:
+    name: str
+    sim: Simulation
+    steps: int
+    flux_monitors: List[FluxMonitor] = field(default_factory=list)
+    description: str = ""
+
+
+def yee_coords(g: G.Grid, comp: int):
+    """Physical coordinates of component ``comp`` at cells 0..n-1 per axis."""
+    o = g.component_origin(comp)
+    return [o[a] + np.arange(g.n[a]) * float(g.delta[a]) for a in range(3)]
+
+
+def _box_mask(xs, ys, zs, center, size):
+    mx = np.abs(xs - center[0]) <= size[0] / 2
+    my = np.abs(ys - center[1]) <= size[1] / 2
+    mz = np.abs(zs - center[2]) <= size[2] / 2
+    return mx[:, None, None] & my[None, :, None] & mz[None, None, :]
+
+
+def _sphere_mask(xs, ys, zs, c, r):
+    d2 = (xs[:, None, None] - c[0]) ** 2 + (ys[None, :, None] - c[1]) ** 2 + (zs[None, None, :] - c[2]) ** 2
+    return d2 <= r * r
+
+
+def _freqs(n, lo, hi):
+    return list(np.linspace(lo, hi, n)) if n > 1 else [0.5 * (lo + hi)]
+
+
+def dipole(dtype="f32", steps=1000, resolution=20, size=3.2, pml=0.5) -> Workload:
+    src = UniformSource(time_profile=GaussianPulseSource(fcen=FCEN, fwidth=0.2 * FCEN),
+                        component=G.EZ, center=(0.0, 0.0, 0.0), size=(0.0, 0.0, 0.0))
+    inner = size - 2 * pml
+    fm = FluxMonitor(center=(0.8 * size / 3.2, 0.0, 0.0), size=(0.0, 0.9 * inner, 0.9 * inner),
+                     frequencies=[0.9 * FCEN, FCEN, 1.1 * FCEN])
+    sim = Simulation(cell_size=(size, size, size), resolution=resolution, sources=[src],
+                     boundaries=[[pml, pml]] * 3, monitors=[fm], dtype=dtype)
+    return Workload("dipole", sim, steps, [fm],
+                    f"{sim.n[0]}x{sim.n[1]}x{sim.n[2]} vacuum, PML {pml} um, Ez point dipole")
+
+
+def waveguide(dtype="f32", steps=4000, scale=1.0, seed=1234) -> Workload:
+    res = 25 * scale
+    size = (12.8, 7.68, 5.12)
+    pml = 12 / 25
+    sim_probe = G.Grid.build(size, (0, 0, 0), res, dtype)
+    g = sim_probe
+    # ε per component: cladding, Si strip along x, random design region
+    eps = []
+    rng = np.random.default_rng(seed)
+    design_c, design_s = (0.0, 0.0, 0.0), (2.0, 2.0, 0.22)
+    # design density on the cell grid, 3-cell box filter with clamped edges
+    xs_c, ys_c, zs_c = yee_coords(g, G.CENTER)
+    rho = rng.uniform(0.0, 1.0, size=g.n)
+    pad = np.pad(rho, 1, mode="edge")
+    filt = np.zeros_like(rho)
+    for dx in range(3):
+        for dy in range(3):
+            for dz in range(3):
+                filt += pad[dx:dx + g.n[0], dy:dy + g.n[1], dz:dz + g.n[2]]
+    filt /= 27.0
+    for comp in (G.EX, G.EY, G.EZ):
+        xs, ys, zs = yee_coords(g, comp)
+        e = np.full(g.n, 2.085)
+        strip = _box_mask(xs, ys, zs, (0.0, 0.0, 0.0), (1e9, 0.5, 0.22))
+        e[strip] = 12.25
+        dm = _box_mask(xs, ys, zs, design_c, design_s)
+        e[dm] = 2.085 + filt[dm] * (12.25 - 2.085)
+        eps.append(1.0 / e)
+    inner_y = size[1] - 2 * pml
+    inner_z = size[2] - 2 * pml
+    src = ProfileSource(time_profile=GaussianPulseSource(fcen=FCEN, fwidth=0.25 * FCEN),
+                        component=G.EY, center=(-5.0, 0.0, 0.0), size=(0.0, inner_y, inner_z),
+                        profile_func=lambda x, y, z: math.exp(-((y ** 2 + z ** 2) / 0.4 ** 2)))
+    fw = 0.25 * FCEN
+    freqs = _freqs(21, FCEN - 0.5 * fw, FCEN + 0.5 * fw)
+    fms = [FluxMonitor(center=(xp, 0.0, 0.0), size=(0.0, 0.9 * inner_y, 0.9 * inner_z), frequencies=freqs)
+           for xp in (-4.0, 4.0)]
+    sim = Simulation(cell_size=size, resolution=res, sources=[src], boundaries=[[pml, pml]] * 3,
+                     monitors=fms, dtype=dtype, eps_inv=eps)
+    return Workload("waveguide", sim, steps, fms,
+                    f"{sim.n[0]}x{sim.n[1]}x{sim.n[2]} Si strip + random design, PML 12 cells")
+
+
+def dispersive(dtype="f32", steps=3000, scale=1.0, seed=42) -> Workload:
+    res = 20 * scale
+    L = 12.8
+    pml = 12 / 20
+    g = G.Grid.build((L, L, L), (0, 0, 0), res, dtype)
+    rng = np.random.default_rng(seed)
+    lo_int = -L / 2 + pml + 0.2
+    spheres = []
+    for s in range(8):
+        r = rng.uniform(0.2, 0.6)
+        c = tuple(rng.uniform(lo_int + r, -lo_int - r) for _ in range(3))
+        spheres.append((c, r, "lorentz" if s < 4 else "drude"))
+    lor = LorentzianSusceptibility(1.0, 0.05, 1.0)
+    dru = DrudeSusceptibility(0.1, (2 * math.pi * 5.0) ** 2 / (2 * math.pi * 0.1))
+    eps_c, chi3 = [], None
+    sig_l = np.zeros(g.n)
+    sig_d = np.zeros(g.n)
+    xs, ys, zs = yee_coords(g, G.EX)  # pole σ on Ex positions, shared by x/y/z (Geometry.jl:1146-1177)
+    for (c, r, kind) in spheres:
+        m = _sphere_mask(xs, ys, zs, c, r)
+        if kind == "lorentz":
+            sig_l[m & (sig_d == 0)] = lor.sigma
+        else:
+            sig_d[m & (sig_l == 0)] = dru.sigma
+    for comp in (G.EX, G.EY, G.EZ):
+        cx, cy, cz = yee_coords(g, comp)
+        e = np.ones(g.n)
+        slab = (np.abs(cz) <= 1.0)[None, None, :] & np.ones(g.n, dtype=bool)
+        e[slab] = 2.25
+        for (c, r, kind) in reversed(spheres):  # first object wins
+            e[_sphere_mask(cx, cy, cz, c, r)] = 2.0 if kind == "lorentz" else 1.0
+        eps_c.append(1.0 / e)
+    xc, yc, zc = yee_coords(g, G.CENTER)
+    chi3 = np.zeros(g.n)
+    chi3[:, :, np.abs(zc) <= 1.0] = 1e-3
+    for (c, r, kind) in spheres:
+        chi3[_sphere_mask(xc, yc, zc, c, r)] = 0.0
+    poles = [(lor, sig_l), (dru, sig_d)]
+    eps_c = apply_chi1_correction(eps_c, poles, g.dt, T=np.float64)
+    inner = L - 2 * pml
+    src = UniformSource(time_profile=GaussianPulseSource(fcen=FCEN, fwidth=0.2 * FCEN), component=G.EZ,
+                        center=(-5.0 * L / 12.8, 0.0, 0.0), size=(0.0, inner, inner))
+    freqs = _freqs(11, 0.8 * FCEN, 1.2 * FCEN)
+    h = 4.5 * L / 12.8
+    fms = []
+    for a in range(3):
+        for sgn in (-1, 1):
+            c = [0.0, 0.0, 0.0]
+            c[a] = sgn * h
+            sz = [2 * h, 2 * h, 2 * h]
+            sz[a] = 0.0
+            fms.append(FluxMonitor(center=tuple(c), size=tuple(sz), frequencies=freqs))
+    sim = Simulation(cell_size=(L, L, L), resolution=res, sources=[src], boundaries=[[pml, pml]] * 3,
+                     monitors=fms, dtype=dtype, eps_inv=eps_c, chi3=chi3, poles=poles)
+    return Workload("dispersive", sim, steps, fms,
+                    f"{sim.n[0]}^3, chi3 slab, 4 Lorentz + 4 Drude spheres, PML 12 cells")
+
+
+BUILDERS = {"dipole": dipole, "waveguide": waveguide, "dispersive": dispersive}

@@ -1,0 +1,535 @@
+// sm_103a kernels of the FDTD step loop.
+//
+// One fused kernel per half-step replaces the reference's per-chunk dispatch
+// (step_H_fused!/step_E_fused!, src/Kernels/Kernels.jl:164-454): the curl,
+// the CPML cascade (Helpers.jl:30-270), the constitutive update
+// (Helpers.jl:323-409), source injection (Sources.jl:346-357) and, on the E
+// half, the χ3 correction (Dispersive.jl:127-147) and the ADE pole update
+// (Dispersive.jl:25-88) all happen in one pass over the grid.
+//
+// Work decomposition: a warp owns 32 × VEC consecutive x cells of one row
+// (VEC = 16 bytes of the run's type) and marches over kPlanesPerCta z planes;
+// the CTA holds kBlockY rows.  x neighbours come from warp shuffles, the z
+// neighbour plane is carried in registers from the previous plane (2.5D
+// register rotation), y neighbours are vector loads that hit L1 (the row
+// above belongs to the next warp of the same CTA).
+//
+// Which arrays a cell touches is a static property of the cell:
+//  * plain cells (no CPML region flag, no source/χ3/pole) keep no B/D state:
+//    O += m⁻¹·K.  This equals m⁻¹·(T + K) of the reference up to rounding and
+//    is exact when m⁻¹ = 1;
+//  * all other cells keep B/D and follow the reference's dispatch on which
+//    CPML auxiliaries its region allocates (Chunking.jl:1069-1146).
+#include <cuda_runtime.h>
+
+#include "kh_kernels.cuh"
+
+namespace kh {
+
+template <typename T>
+struct VT;
+template <>
+struct VT<float> {
+  using V = float4;
+};
+template <>
+struct VT<double> {
+  using V = double2;
+};
+
+template <typename T>
+__device__ __forceinline__ void vld(const T* ptr, T (&v)[Vec<T>::N]) {
+  using V = typename VT<T>::V;
+  V x = *reinterpret_cast<const V*>(ptr);
+  if constexpr (Vec<T>::N == 4) {
+    v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+  } else {
+    v[0] = x.x; v[1] = x.y;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void vst(T* ptr, const T (&v)[Vec<T>::N]) {
+  using V = typename VT<T>::V;
+  V x;
+  if constexpr (Vec<T>::N == 4) {
+    x.x = v[0]; x.y = v[1]; x.z = v[2]; x.w = v[3];
+  } else {
+    x.x = v[0]; x.y = v[1];
+  }
+  *reinterpret_cast<V*>(ptr) = x;
+}
+
+// update_field_from_curl (Helpers.jl:30-33)
+template <typename T>
+__device__ __forceinline__ T ufc_old(T A, T B, T Bold, T s) {
+  return (((T(1) - s) * A + B) - Bold) / (T(1) + s);
+}
+template <typename T>
+__device__ __forceinline__ T ufc(T A, T B, T s) {
+  return ((T(1) - s) * A + B) / (T(1) + s);
+}
+
+// Per-cell update of one cell that keeps B/D state, or sits in a CPML region,
+// or carries a source, χ3 or a pole.
+template <typename T, bool H>
+__device__ __forceinline__ void general_cell(const HalfStepParams<T>& p, long long q, int i, int j,
+                                             int k, bool fx, bool fy, bool fz, uint32_t cls,
+                                             bool special, const T (&K)[3], T (&O)[3]) {
+  const bool f[3] = {fx, fy, fz};
+  const int ix3[3] = {i, j, k};
+  const bool region = fx || fy || fz;
+  bool regC = false;
+  if (region) {
+    const int rx = i < p.pml_lo[0] ? 0 : (i >= p.nx - p.pml_hi[0] ? 2 : 1);
+    const int ry = j < p.pml_lo[1] ? 0 : (j >= p.ny - p.pml_hi[1] ? 2 : 1);
+    const int rz = k < p.pml_lo[2] ? 0 : (k >= p.nz - p.pml_hi[2] ? 2 : 1);
+    regC = (p.sigma_region_mask >> (rx + 3 * ry + 9 * rz)) & 1u;
+  }
+
+  // Source term S of this half-step (update_source!, Sources.jl:346-357).
+  T S[3] = {T(0), T(0), T(0)};
+  bool hasS[3] = {false, false, false};
+  if (p.sources_active && (cls & (H ? kHasSrcH : kHasSrcE))) {
+    const int slot = int(cls >> kSlotShift);
+    const int e1 = p.slot_off[slot + 1];
+    for (int e = p.slot_off[slot]; e < e1; ++e) {
+      const int c = p.ent_comp[e] - (H ? 3 : 0);  // entries carry components 0..5
+      if (c < 0 || c > 2) continue;
+      const Cplx<T> a = p.ent_amp[e];
+      const Cplx<T> fv = p.f_now[p.ent_src[e]];
+      S[c] += fv.re * a.re - fv.im * a.im;  // real(f(t) · amplitude)
+      hasS[c] = true;
+    }
+  }
+
+  // Total polarisation Σ_p P_p (accumulate_polarization_kernel!, Dispersive.jl:95-104).
+  T Ptot[3] = {T(0), T(0), T(0)};
+  if constexpr (!H) {
+    if (cls & kHasPole) {
+      for (int pp = 0; pp < p.npoles; ++pp)
+        for (int c = 0; c < 3; ++c) Ptot[c] += p.poles[pp].P[c][q];
+    }
+  }
+
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const int nx_ = (c + 1) % 3, pv = (c + 2) % 3;
+    const bool hasU = region && f[nx_];
+    const bool hasW = region && f[c];
+    const bool hasC = regC && (f[nx_] || f[pv]);
+    const bool hasSD = region && p.msig[c] != nullptr;
+    const T m = p.m_inv[c] ? p.m_inv[c][q] : p.m_scalar;
+    const bool keepT = special || (p.cpml ? region : (hasU || hasW || hasC || hasSD));
+    if (!keepT) {
+      O[c] = O[c] + m * K[c];
+      continue;
+    }
+    T t = p.Ts[c][q];
+    if (!region) {
+      t = t + K[c];  // step_curl_and_update! (ReferenceKernels.jl:340-345)
+    } else if (p.cpml) {
+      // _cuda_pml_BH_kernel!/_cuda_pml_DE_kernel! stages (CUDAKernels.jl:150-281)
+      const T sn = p.sig[nx_][ix3[nx_]];
+      const T sp = p.sig[pv][ix3[pv]];
+      T in_t = K[c];
+      if (f[nx_] && sn != T(0)) {
+        const T u = p.U[c][q];
+        const T un = ufc(u, K[c], sn);
+        p.U[c][q] = un;
+        in_t = un - u;
+      }
+      t = (f[pv] && sp != T(0)) ? ((T(1) - sp) * t + in_t) / (T(1) + sp) : t + in_t;
+    } else {
+      const T sn = p.sig[nx_][ix3[nx_]];
+      const T sp = p.sig[pv][ix3[pv]];
+      if (hasC && hasU) {
+        const T sD = hasSD ? T(0.5) * (p.dt * p.msig[c][q]) : T(0);
+        const T u = p.U[c][q];
+        if (hasSD && sD != T(0)) {  // three-stage cascade (Helpers.jl:60-67)
+          const T cc = p.C[c][q];
+          const T cn = ufc(cc, K[c], sD);
+          p.C[c][q] = cn;
+          const T un = ufc_old(u, cn, cc, sn);
+          p.U[c][q] = un;
+          t = ufc_old(t, un, u, sp);
+        } else {  // two-stage cascade (Helpers.jl:53-59, 72-78)
+          const T un = ufc(u, K[c], sn);
+          p.U[c][q] = un;
+          t = ufc_old(t, un, u, sp);
+        }
+      } else if (hasU) {  // C absent (Helpers.jl:113-139)
+        if (sn == T(0)) {
+          t = ufc(t, K[c], sp);
+        } else {
+          const T u = p.U[c][q];
+          const T un = ufc(u, K[c], sn);
+          p.U[c][q] = un;
+          t = ufc_old(t, un, u, sp);
+        }
+      } else if (hasSD) {  // C and U absent, conductivity present (Helpers.jl:225-240)
+        const T sD = T(0.5) * (p.dt * p.msig[c][q]);
+        t = ufc(t, K[c], sD);
+      } else {  // C and U absent: σ_prev dropped (Helpers.jl:208-223)
+        t = t + K[c];
+      }
+    }
+    p.Ts[c][q] = t;
+    T net = t;
+    if (hasS[c]) net += S[c];
+    if constexpr (!H) {
+      if (cls & kHasPole) net -= Ptot[c];
+    }
+    const T sc = region ? p.sig[c][ix3[c]] : T(0);
+    if (hasW && sc != T(0)) {  // update_field_generic W cascade (Helpers.jl:333-339)
+      const T w = p.W[c][q];
+      const T wn = m * net;
+      p.W[c][q] = wn;
+      O[c] = (O[c] + (T(1) + sc) * wn) - (T(1) - sc) * w;
+    } else {
+      O[c] = m * net;
+    }
+  }
+
+  if constexpr (!H) {
+    // χ3 Kerr correction (Dispersive.jl:127-147)
+    if (cls & kHasChi3) {
+      const T c3 = p.chi3[q];
+      if (c3 != T(0)) {
+        const T esq = (O[0] * O[0] + O[1] * O[1]) + O[2] * O[2];
+        const T corr = T(1) / (T(1) + c3 * esq);
+        O[0] = O[0] * corr;
+        O[1] = O[1] * corr;
+        O[2] = O[2] * corr;
+      }
+    }
+    // ADE poles with E^{n+1} (Dispersive.jl:25-88)
+    if (cls & kHasPole) {
+      for (int pp = 0; pp < p.npoles; ++pp) {
+        const PoleParams<T>& P = p.poles[pp];
+        const T s = P.sigma[q];
+        if (s == T(0)) continue;
+        for (int c = 0; c < 3; ++c) {
+          const T px = P.P[c][q];
+          const T pprev = P.Pprev[c][q];
+          T pn;
+          if (P.is_drude) pn = P.gamma1_inv * ((T(2) * px - P.gamma1 * pprev) + (P.drive * s) * O[c]);
+          else pn = P.gamma1_inv * ((P.coeff_p * px - P.gamma1 * pprev) + (P.drive * s) * O[c]);
+          P.P[c][q] = pn;
+          P.Pprev[c][q] = px;
+        }
+      }
+    }
+  }
+}
+
+// One fused half-step.  H = true: B/H from curl E; H = false: D/E from curl H.
+template <typename T, bool H>
+__global__ void __launch_bounds__(32 * kBlockY) half_step_kernel(const HalfStepParams<T> p) {
+  constexpr int VN = Vec<T>::N;
+  constexpr int s = H ? 1 : -1;
+  const int lane = threadIdx.x;
+  const int j = blockIdx.y * kBlockY + threadIdx.y;
+  if (j >= p.ny) return;  // warp-uniform: blockDim.x == 32
+  const int xb = blockIdx.x;
+  const int x0 = (xb * 32 + lane) * VN;
+  const bool lane_ok = x0 < p.nx;
+  const int k0 = blockIdx.z * kPlanesPerCta;
+  const int k1 = min(k0 + kPlanesPerCta, p.nz);
+  const long long row = p.origin + (long long)j * p.pitch + x0;
+  const long long ystep = (long long)s * p.pitch;
+  const long long zstep = (long long)s * p.plane;
+
+  const bool fy = j < p.pml_lo[1] || j >= p.ny - p.pml_hi[1];
+  // rotated z-neighbour planes of A0, A1
+  T r0[VN], r1[VN];
+#pragma unroll
+  for (int v = 0; v < VN; ++v) { r0[v] = T(0); r1[v] = T(0); }
+  if (lane_ok) {
+    const long long q0 = row + (long long)k0 * p.plane + (H ? 0 : -p.plane);
+    vld(p.A[0] + q0, r0);
+    vld(p.A[1] + q0, r1);
+  }
+
+  for (int k = k0; k < k1; ++k) {
+    const long long q = row + (long long)k * p.plane;
+    T l0[VN], l1[VN], a2[VN], y0[VN], y2[VN];
+#pragma unroll
+    for (int v = 0; v < VN; ++v) { l0[v] = l1[v] = a2[v] = y0[v] = y2[v] = T(0); }
+    if (lane_ok) {
+      if constexpr (H) {  // l = A(k+1)
+        vld(p.A[0] + q + zstep, l0);
+        vld(p.A[1] + q + zstep, l1);
+      } else {  // l = A(k)
+        vld(p.A[0] + q, l0);
+        vld(p.A[1] + q, l1);
+      }
+      vld(p.A[2] + q, a2);
+      vld(p.A[0] + q + ystep, y0);
+      vld(p.A[2] + q + ystep, y2);
+    }
+    // cur = A0/A1 at plane k, nb = at plane k+s
+    T* cur0 = H ? r0 : l0;
+    T* cur1 = H ? r1 : l1;
+    T* nb0 = H ? l0 : r0;
+    T* nb1 = H ? l1 : r1;
+
+    // x neighbours of A1 and A2 at plane k
+    T x1s[VN], x2s[VN];
+    if constexpr (H) {
+      T n1 = __shfl_down_sync(0xffffffffu, cur1[0], 1);
+      T n2 = __shfl_down_sync(0xffffffffu, a2[0], 1);
+      if (lane == 31 && lane_ok) {
+        n1 = p.A[1][q + VN];
+        n2 = p.A[2][q + VN];
+      }
+#pragma unroll
+      for (int v = 0; v < VN - 1; ++v) { x1s[v] = cur1[v + 1]; x2s[v] = a2[v + 1]; }
+      x1s[VN - 1] = n1;
+      x2s[VN - 1] = n2;
+    } else {
+      T n1 = __shfl_up_sync(0xffffffffu, cur1[VN - 1], 1);
+      T n2 = __shfl_up_sync(0xffffffffu, a2[VN - 1], 1);
+      if (lane == 0 && lane_ok) {
+        n1 = p.A[1][q - 1];
+        n2 = p.A[2][q - 1];
+      }
+#pragma unroll
+      for (int v = 1; v < VN; ++v) { x1s[v] = cur1[v - 1]; x2s[v] = a2[v - 1]; }
+      x1s[0] = n1;
+      x2s[0] = n2;
+    }
+
+    if (lane_ok) {
+      T O0[VN], O1[VN], O2[VN];
+      vld(p.O[0] + q, O0);
+      vld(p.O[1] + q, O1);
+      vld(p.O[2] + q, O2);
+      T m0[VN], m1[VN], m2[VN];
+      const bool pervox = p.m_inv[0] != nullptr;
+      if (pervox) {
+        vld(p.m_inv[0] + q, m0);
+        vld(p.m_inv[1] + q, m1);
+        vld(p.m_inv[2] + q, m2);
+      }
+      const bool fz = k < p.pml_lo[2] || k >= p.nz - p.pml_hi[2];
+      const bool yz = fy || fz;
+      uint32_t tf = 0;
+      if (p.tile_flag) tf = p.tile_flag[((long long)k * p.ny + j) * p.nxb + xb] & p.tile_bit;
+#pragma unroll
+      for (int v = 0; v < VN; ++v) {
+        const int i = x0 + v;
+        if (i >= p.nx) continue;
+        const T K0 = p.dt * (p.inv_d[2] * (nb1[v] - cur1[v]) - p.inv_d[1] * (y2[v] - a2[v]));
+        const T K1 = p.dt * (p.inv_d[0] * (x2s[v] - a2[v]) - p.inv_d[2] * (nb0[v] - cur0[v]));
+        const T K2 = p.dt * (p.inv_d[1] * (y0[v] - cur0[v]) - p.inv_d[0] * (x1s[v] - cur1[v]));
+        const bool fx = i < p.pml_lo[0] || i >= p.nx - p.pml_hi[0];
+        const uint32_t cls = tf ? p.cell_class[q + v] : 0u;
+        const bool special = cls & (H ? kSpecialH : kSpecialE);
+        if (!(fx || yz || special)) {
+          const T a = pervox ? m0[v] : p.m_scalar;
+          const T b = pervox ? m1[v] : p.m_scalar;
+          const T c = pervox ? m2[v] : p.m_scalar;
+          O0[v] = O0[v] + a * K0;
+          O1[v] = O1[v] + b * K1;
+          O2[v] = O2[v] + c * K2;
+        } else {
+          const T Kc[3] = {K0, K1, K2};
+          T Oc[3] = {O0[v], O1[v], O2[v]};
+          general_cell<T, H>(p, q + v, i, j, k, fx, fy, fz, cls, special, Kc, Oc);
+          O0[v] = Oc[0];
+          O1[v] = Oc[1];
+          O2[v] = Oc[2];
+        }
+      }
+      if (x0 + VN <= p.nx) {
+        vst(p.O[0] + q, O0);
+        vst(p.O[1] + q, O1);
+        vst(p.O[2] + q, O2);
+      } else {
+#pragma unroll
+        for (int v = 0; v < VN; ++v) {
+          if (x0 + v < p.nx) {
+            p.O[0][q + v] = O0[v];
+            p.O[1][q + v] = O1[v];
+            p.O[2][q + v] = O2[v];
+          }
+        }
+      }
+    }
+    // rotate: H half keeps A(k+1) as the next plane's A(k); E half keeps
+    // A(k) as the next plane's A(k-1)
+#pragma unroll
+    for (int v = 0; v < VN; ++v) { r0[v] = l0[v]; r1[v] = l1[v]; }
+  }
+}
+
+template <typename T>
+void launch_half_step(bool h_half, const HalfStepParams<T>& p, void* stream) {
+  dim3 block(32, kBlockY, 1);
+  dim3 grid(p.nxb, (p.ny + kBlockY - 1) / kBlockY, (p.nz + kPlanesPerCta - 1) / kPlanesPerCta);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (h_half) half_step_kernel<T, true><<<grid, block, 0, st>>>(p);
+  else half_step_kernel<T, false><<<grid, block, 0, st>>>(p);
+}
+
+// ---------------------------------------------------------------------------
+// DFT accumulation (update_dft_monitor!, Monitors.jl:361-379):
+//   F[cell, f] += Δt·exp(i2πf t)·field[cell]
+// FP32 accumulators carry a Kahan compensation term.
+template <typename T>
+__global__ void dft_kernel(const DftParams<T> p) {
+  const long long ncell = (long long)p.dims[0] * p.dims[1] * p.dims[2];
+  const long long total = ncell * p.nf;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int f = int(t / ncell);
+    const long long cell = t - (long long)f * ncell;
+    const int i = int(cell % p.dims[0]);
+    const long long r = cell / p.dims[0];
+    const int jj = int(r % p.dims[1]);
+    const int kk = int(r / p.dims[1]);
+    const long long q = p.origin + (long long)(p.start[2] + kk) * p.plane +
+                        (long long)(p.start[1] + jj) * p.pitch + (p.start[0] + i);
+    const T v = p.field[q];
+    const Cplx<T> ph = p.phase[f];
+    Cplx<T> acc = p.F[t];
+    if (p.comp) {
+      Cplx<T> c = p.comp[t];
+      const T yr = ph.re * v - c.re;
+      const T yi = ph.im * v - c.im;
+      const T tr = acc.re + yr;
+      const T ti = acc.im + yi;
+      c.re = (tr - acc.re) - yr;
+      c.im = (ti - acc.im) - yi;
+      acc.re = tr;
+      acc.im = ti;
+      p.comp[t] = c;
+    } else {
+      acc.re = acc.re + ph.re * v;
+      acc.im = acc.im + ph.im * v;
+    }
+    p.F[t] = acc;
+  }
+}
+
+template <typename T>
+void launch_dft(const DftParams<T>& p, void* stream) {
+  const long long total = (long long)p.dims[0] * p.dims[1] * p.dims[2] * p.nf;
+  int blocks = int((total + 255) / 256);
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  if (blocks < 1) blocks = 1;
+  dft_kernel<T><<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(p);
+}
+
+// ---------------------------------------------------------------------------
+// Flux (get_flux, FluxMonitor.jl:92-156) in FP64: one block per frequency,
+// fixed-order tree reduction so the result is reproducible.
+template <typename T>
+__device__ __forceinline__ void load_c(const Cplx<T>* F, const Cplx<T>* C, long long q, double& re,
+                                       double& im) {
+  re = double(F[q].re);
+  im = double(F[q].im);
+  if (C) {  // Kahan: sum - compensation
+    re -= double(C[q].re);
+    im -= double(C[q].im);
+  }
+}
+
+struct FluxArgs {
+  int d[4][3];
+  int normal;
+  int nf;
+  double dA;
+};
+
+template <typename T>
+__device__ __forceinline__ void avg_at(const Cplx<T>* F, const Cplx<T>* C, const int* d, int normal,
+                                       int a1, int a2, int i1, int i2, int f, double& re,
+                                       double& im) {
+  int idx[3];
+  idx[normal] = 0;
+  idx[a1] = i1;
+  idx[a2] = i2;
+  const long long ncell = (long long)d[0] * d[1] * d[2];
+  long long q = (long long)f * ncell + ((long long)idx[2] * d[1] + idx[1]) * d[0] + idx[0];
+  load_c(F, C, q, re, im);
+  if (d[normal] >= 2) {  // _avg_dim: (layer 1 + layer 2) / 2
+    idx[normal] = 1;
+    long long q2 = (long long)f * ncell + ((long long)idx[2] * d[1] + idx[1]) * d[0] + idx[0];
+    double r2, i2v;
+    load_c(F, C, q2, r2, i2v);
+    re = (re + r2) / 2;
+    im = (im + i2v) / 2;
+  }
+}
+
+template <typename T>
+__global__ void flux_kernel(const Cplx<T>* e1, const Cplx<T>* e2, const Cplx<T>* h1,
+                            const Cplx<T>* h2, const Cplx<T>* ce1, const Cplx<T>* ce2,
+                            const Cplx<T>* ch1, const Cplx<T>* ch2, const FluxArgs a,
+                            double* out) {
+  const int f = blockIdx.x;
+  const int n = a.normal;
+  const int a1 = n == 0 ? 1 : 0;
+  const int a2 = n == 2 ? 1 : 2;
+  int n1 = a.d[0][a1], n2 = a.d[0][a2];
+  for (int m = 1; m < 4; ++m) {
+    n1 = min(n1, a.d[m][a1]);
+    n2 = min(n2, a.d[m][a2]);
+  }
+  double acc = 0.0;
+  for (long long t = threadIdx.x; t < (long long)n1 * n2; t += blockDim.x) {
+    const int i1 = int(t % n1), i2 = int(t / n1);
+    double E1r, E1i, E2r, E2i, H1r, H1i, H2r, H2i;
+    avg_at(e1, ce1, a.d[0], n, a1, a2, i1, i2, f, E1r, E1i);
+    avg_at(e2, ce2, a.d[1], n, a1, a2, i1, i2, f, E2r, E2i);
+    avg_at(h1, ch1, a.d[2], n, a1, a2, i1, i2, f, H1r, H1i);
+    avg_at(h2, ch2, a.d[3], n, a1, a2, i1, i2, f, H2r, H2i);
+    // Re(E1·conj(H2) − E2·conj(H1))
+    acc += ((E1r * H2r + E1i * H2i) - (E2r * H1r + E2i * H1i)) * a.dA;
+  }
+  __shared__ double red[256];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[f] = red[0];
+}
+
+template <typename T>
+void launch_flux(const Cplx<T>* e1, const Cplx<T>* e2, const Cplx<T>* h1, const Cplx<T>* h2,
+                 const Cplx<T>* c_e1, const Cplx<T>* c_e2, const Cplx<T>* c_h1,
+                 const Cplx<T>* c_h2, const int dims_e1[3], const int dims_e2[3],
+                 const int dims_h1[3], const int dims_h2[3], int normal_axis, int nf, double dA,
+                 double* out, void* stream) {
+  FluxArgs a;
+  for (int q = 0; q < 3; ++q) {
+    a.d[0][q] = dims_e1[q];
+    a.d[1][q] = dims_e2[q];
+    a.d[2][q] = dims_h1[q];
+    a.d[3][q] = dims_h2[q];
+  }
+  a.normal = normal_axis;
+  a.nf = nf;
+  a.dA = dA;
+  flux_kernel<T><<<nf, 256, 0, static_cast<cudaStream_t>(stream)>>>(e1, e2, h1, h2, c_e1, c_e2,
+                                                                      c_h1, c_h2, a, out);
+}
+
+template void launch_half_step<float>(bool, const HalfStepParams<float>&, void*);
+template void launch_half_step<double>(bool, const HalfStepParams<double>&, void*);
+template void launch_dft<float>(const DftParams<float>&, void*);
+template void launch_dft<double>(const DftParams<double>&, void*);
+template void launch_flux<float>(const Cplx<float>*, const Cplx<float>*, const Cplx<float>*,
+                                 const Cplx<float>*, const Cplx<float>*, const Cplx<float>*,
+                                 const Cplx<float>*, const Cplx<float>*, const int*, const int*,
+                                 const int*, const int*, int, int, double, double*, void*);
+template void launch_flux<double>(const Cplx<double>*, const Cplx<double>*, const Cplx<double>*,
+                                  const Cplx<double>*, const Cplx<double>*, const Cplx<double>*,
+                                  const Cplx<double>*, const Cplx<double>*, const int*, const int*,
+                                  const int*, const int*, int, int, double, double*, void*);
+
+}  // namespace kh

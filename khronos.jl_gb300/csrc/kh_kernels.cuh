@@ -1,0 +1,120 @@
+// Shared declarations between the sm_103a kernels (kh_kernels.cu) and the
+// host-side C-ABI implementation (kh_sim.cu).
+//
+// Device layout of every full-domain array (fields, materials, auxiliaries):
+//   element (i, j, k), -1 <= i,j,k <= n, lives at
+//     origin + (k * (ny + 2) + j) * pitch + i
+//   with origin = ((ny + 2) + 1) * pitch + XOFF and XOFF = VEC elements
+//   (16 bytes), so x = 0 of every row is 16-byte aligned and the row pitch is
+//   a multiple of 128 bytes.  The ring i,j,k in {-1, n} (and the row padding)
+//   is never written: it is the reference's zero ghost layer / staggered wall.
+#pragma once
+
+#include <cstdint>
+
+namespace kh {
+
+constexpr int kMaxPoles = 4;
+constexpr int kBlockY = 4;      // rows per CTA
+constexpr int kPlanesPerCta = 16;
+
+// cell_class bits (full-domain uint32 array, read only inside flagged tiles)
+constexpr uint32_t kSpecialE = 1u << 0;  // D-state kept: E source, χ3 or pole
+constexpr uint32_t kSpecialH = 1u << 1;  // B-state kept: H source
+constexpr uint32_t kHasChi3 = 1u << 2;
+constexpr uint32_t kHasPole = 1u << 3;
+constexpr uint32_t kHasSrcE = 1u << 4;
+constexpr uint32_t kHasSrcH = 1u << 5;
+constexpr int kSlotShift = 8;            // source slot index in the upper 24 bits
+
+template <typename T>
+struct Vec;
+template <>
+struct Vec<float> {
+  static constexpr int N = 4;
+};
+template <>
+struct Vec<double> {
+  static constexpr int N = 2;
+};
+
+template <typename T>
+struct PoleParams {
+  T gamma1_inv, gamma1, coeff_p, drive;  // drive = sigma_omega0_dt_sq or drude_coeff
+  int is_drude;
+  const T* sigma;
+  T* P[3];
+  T* Pprev[3];
+};
+
+template <typename T>
+struct Cplx {
+  T re, im;
+};
+
+// Parameters of one fused half-step launch.
+template <typename T>
+struct HalfStepParams {
+  int nx, ny, nz;
+  long long pitch, plane, origin;
+  int nxb;  // x tiles of 32*VEC cells
+  T dt, inv_d[3];
+
+  const T* A[3];  // curl source field (E for the H half, H for the E half)
+  T* O[3];        // updated field (H or E)
+  T* Ts[3];       // B or D state where kept (nullptr if no cell keeps it)
+  T* U[3];        // CPML U auxiliaries (nullptr if none)
+  T* W[3];        // CPML W auxiliaries
+  T* C[3];        // conductivity cascade C
+  const T* m_inv[3];  // per-voxel μ⁻¹ / ε⁻¹ or nullptr
+  T m_scalar;
+  const T* msig[3];   // material conductivity σB / σD or nullptr
+  const T* sig[3];    // PML σ per axis at cell centres (length n_a, zeros outside PML)
+  int pml_lo[3], pml_hi[3];
+  int cpml;                    // 1: CUDA-path CPML stages, 0: CPU-path dispatch
+  uint32_t sigma_region_mask;  // bit r (r = rx + 3 ry + 9 rz) set: region has conductivity
+
+  const uint8_t* tile_flag;   // per (xb, j, k): special cells present
+  const uint32_t* cell_class; // per cell
+  uint8_t tile_bit;           // which tile_flag bit this half reads
+
+  // sources (folded into the half-step)
+  int sources_active;
+  const int* slot_off;        // slot -> [slot_off[s], slot_off[s+1]) entries
+  const int* ent_src;         // source index of entry
+  const int* ent_comp;        // component 0..2 within this half
+  const Cplx<T>* ent_amp;     // complex amplitude of entry
+  const Cplx<T>* f_now;       // per source: time factor f(t) of this half-step
+
+  // E half only
+  const T* chi3;
+  int npoles;
+  PoleParams<T> poles[kMaxPoles];
+};
+
+template <typename T>
+struct DftParams {
+  const T* field;
+  long long pitch, plane, origin;
+  int start[3], dims[3];
+  int nf;
+  const Cplx<T>* phase;  // nf entries: Δt·exp(i 2π f t)
+  Cplx<T>* F;            // (cells, nf) accumulators, cell-major per frequency
+  Cplx<T>* comp;         // Kahan compensation (FP32) or nullptr
+};
+
+template <typename T>
+void launch_half_step(bool h_half, const HalfStepParams<T>& p, void* stream);
+
+template <typename T>
+void launch_dft(const DftParams<T>& p, void* stream);
+
+// FP64 flux reduction: one block per frequency.
+template <typename T>
+void launch_flux(const Cplx<T>* e1, const Cplx<T>* e2, const Cplx<T>* h1, const Cplx<T>* h2,
+                 const Cplx<T>* c_e1, const Cplx<T>* c_e2, const Cplx<T>* c_h1,
+                 const Cplx<T>* c_h2, const int dims_e1[3], const int dims_e2[3],
+                 const int dims_h1[3], const int dims_h2[3], int normal_axis, int nf, double dA,
+                 double* out, void* stream);
+
+}  // namespace kh

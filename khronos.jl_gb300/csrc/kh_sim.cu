@@ -1,0 +1,1113 @@
+// Host side of the C ABI declared in include/khronos_gb300.h.
+//
+// A kh_sim owns one single-domain grid in device memory.  kh_sim_prepare
+// classifies every cell once (CPML region flags, sources, χ3, poles), builds
+// the sparse source table and allocates only the auxiliary arrays some cell
+// uses.  kh_sim_step then issues, per step, the fused H kernel, the H-side DFT
+// launches on decimation steps, the fused E kernel and the E-side DFT
+// launches, mirroring step!(sim) (src/Kernels/Kernels.jl:20-88).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/khronos_gb300.h"
+#include "kh_kernels.cuh"
+
+using kh::Cplx;
+
+namespace {
+
+const char* kVersion = "khronos_gb300 1.0 (sm_103a)";
+
+struct SimBase {
+  virtual ~SimBase() = default;
+  std::string err;
+  int64_t launches = 0;
+  virtual kh_status set_material(int kind, int comp, const double* v) = 0;
+  virtual kh_status add_pole(const kh_pole_coeffs& c, const double* s) = 0;
+  virtual kh_status add_source(const kh_source_desc& s) = 0;
+  virtual kh_status add_monitor(int comp, const int32_t* st, const int32_t* dm, int nf,
+                                const double* f, int dec, int32_t* id) = 0;
+  virtual kh_status prepare() = 0;
+  virtual kh_status step(int64_t n, cudaStream_t s) = 0;
+  virtual int64_t timestep() const = 0;
+  virtual int sources_active() const = 0;
+  virtual kh_status get_field(int comp, double* out) = 0;
+  virtual kh_status read_dft(int id, double* out) = 0;
+  virtual kh_status monitor_info(int id, int32_t* dims, int32_t* nf) const = 0;
+  virtual kh_status flux(const int32_t* ids, int normal, double dA, double* out) = 0;
+  virtual kh_status reset() = 0;
+  virtual int64_t state_bytes() const = 0;
+  virtual kh_status export_state(void* dst, int64_t bytes) = 0;
+  virtual kh_status import_state(const void* src, int64_t bytes) = 0;
+  virtual double model_bytes_per_step() const = 0;
+  virtual void model_split(double& h, double& e, double& dft) const = 0;
+  virtual kh_status step_timed(int64_t n, cudaStream_t s, double* h_ms, double* e_ms,
+                               double* dft_ms) = 0;
+};
+
+#define KH_CUDA(call)                                                          \
+  do {                                                                         \
+    cudaError_t e_ = (call);                                                   \
+    if (e_ != cudaSuccess) {                                                   \
+      err = std::string(#call) + ": " + cudaGetErrorString(e_);                \
+      return e_ == cudaErrorMemoryAllocation ? KH_ERR_OOM : KH_ERR_CUDA;       \
+    }                                                                          \
+  } while (0)
+
+template <typename T>
+class Sim : public SimBase {
+ public:
+  static constexpr int VN = kh::Vec<T>::N;
+
+  explicit Sim(const kh_sim_desc& desc) : d_(desc) {
+    for (int a = 0; a < 3; ++a) n_[a] = desc.n[a];
+    dt_ = T(desc.dt);
+    for (int a = 0; a < 3; ++a) delta_[a] = T(desc.delta[a]);
+    const long long nxp = (n_[0] + VN - 1) / VN * VN;
+    const long long align = 128 / sizeof(T);
+    pitch_ = (VN + nxp + VN + align - 1) / align * align;
+    plane_ = pitch_ * (n_[1] + 2);
+    origin_ = plane_ + pitch_ + VN;
+    total_ = plane_ * (n_[2] + 2);
+    nxb_ = int((n_[0] + 32 * VN - 1) / (32 * VN));
+    for (int a = 0; a < 3; ++a) {
+      sigb_h_[a].assign(n_[a], T(0));
+      sigd_h_[a].assign(n_[a], T(0));
+      if (desc.sigma_b[a]) for (int i = 0; i < n_[a]; ++i) sigb_h_[a][i] = T(desc.sigma_b[a][i]);
+      if (desc.sigma_d[a]) for (int i = 0; i < n_[a]; ++i) sigd_h_[a][i] = T(desc.sigma_d[a][i]);
+    }
+  }
+
+  ~Sim() override {
+    for (void* p : allocs_) cudaFree(p);
+    if (pinned_) cudaFreeHost(pinned_);
+    if (copy_done_) cudaEventDestroy(copy_done_);
+    if (batch_done_) cudaEventDestroy(batch_done_);
+    for (cudaEvent_t ev : events_) cudaEventDestroy(ev);
+  }
+
+  // ---------------- set-up ----------------
+  kh_status set_material(int kind, int comp, const double* v) override {
+    if (prepared_) return fail(KH_ERR_INVALID, "set_material after prepare");
+    if (!v) return fail(KH_ERR_INVALID, "null material array");
+    std::vector<T>* dst = nullptr;
+    if (kind == KH_MAT_CHI3) dst = &chi3_h_;
+    else if (comp < 0 || comp > 2) return fail(KH_ERR_INVALID, "material component must be 0..2");
+    else if (kind == KH_MAT_EPS_INV) dst = &eps_h_[comp];
+    else if (kind == KH_MAT_MU_INV) dst = &mu_h_[comp];
+    else if (kind == KH_MAT_SIGMA_D) dst = &msigd_h_[comp];
+    else if (kind == KH_MAT_SIGMA_B) dst = &msigb_h_[comp];
+    else return fail(KH_ERR_INVALID, "unknown material kind");
+    const size_t cnt = size_t(n_[0]) * n_[1] * n_[2];
+    dst->resize(cnt);
+    for (size_t q = 0; q < cnt; ++q) (*dst)[q] = T(v[q]);
+    return KH_OK;
+  }
+
+  kh_status add_pole(const kh_pole_coeffs& c, const double* s) override {
+    if (prepared_) return fail(KH_ERR_INVALID, "add_pole after prepare");
+    if (int(poles_.size()) >= kh::kMaxPoles) return fail(KH_ERR_UNSUPPORTED, "too many poles");
+    if (!s) return fail(KH_ERR_INVALID, "null pole sigma");
+    PoleH p;
+    p.c = c;
+    const size_t cnt = size_t(n_[0]) * n_[1] * n_[2];
+    p.sigma.resize(cnt);
+    for (size_t q = 0; q < cnt; ++q) p.sigma[q] = T(s[q]);
+    poles_.push_back(std::move(p));
+    return KH_OK;
+  }
+
+  kh_status add_source(const kh_source_desc& s) override {
+    if (prepared_) return fail(KH_ERR_INVALID, "add_source after prepare");
+    if (s.component < 0 || s.component > 5) return fail(KH_ERR_INVALID, "bad source component");
+    if (s.dims[0] < 0 || s.dims[1] < 0 || s.dims[2] < 0) return fail(KH_ERR_INVALID, "bad source dims");
+    if (s.time_kind < KH_TIME_GAUSSIAN || s.time_kind > KH_TIME_TABLE)
+      return fail(KH_ERR_INVALID, "bad time profile");
+    const size_t cnt = size_t(s.dims[0]) * s.dims[1] * s.dims[2];
+    if (cnt && !s.amp) return fail(KH_ERR_INVALID, "null amplitude");
+    SrcH h;
+    h.d = s;
+    h.d.amp = nullptr;
+    h.d.table = nullptr;
+    h.amp.resize(cnt);
+    for (size_t q = 0; q < cnt; ++q) h.amp[q] = std::complex<double>(s.amp[2 * q], s.amp[2 * q + 1]);
+    if (s.time_kind == KH_TIME_TABLE) {
+      if (s.table_len < 0 || (s.table_len > 0 && !s.table)) return fail(KH_ERR_INVALID, "bad table");
+      h.table.resize(size_t(2 * s.table_len));
+      for (int64_t q = 0; q < 2 * s.table_len; ++q)
+        h.table[q] = std::complex<T>(T(s.table[2 * q]), T(s.table[2 * q + 1]));
+    }
+    srcs_.push_back(std::move(h));
+    return KH_OK;
+  }
+
+  kh_status add_monitor(int comp, const int32_t* st, const int32_t* dm, int nf, const double* f,
+                        int dec, int32_t* id) override {
+    if (prepared_) return fail(KH_ERR_INVALID, "add_dft_monitor after prepare");
+    if (comp < 0 || comp > 5 || !st || !dm || nf <= 0 || !f || !id)
+      return fail(KH_ERR_INVALID, "bad monitor arguments");
+    Mon m;
+    m.comp = comp;
+    for (int a = 0; a < 3; ++a) {
+      m.start[a] = st[a];
+      m.dims[a] = dm[a];
+      // the read box may reach the staggered wall layer (index n) but no further
+      if (dm[a] <= 0 || st[a] < 0 || st[a] + dm[a] > n_[a] + 1)
+        return fail(KH_ERR_INVALID, "monitor box outside the grid");
+    }
+    m.nf = nf;
+    m.dec = dec < 1 ? 1 : dec;
+    m.freqs.assign(f, f + nf);
+    mons_.push_back(std::move(m));
+    *id = int32_t(mons_.size() - 1);
+    return KH_OK;
+  }
+
+  kh_status prepare() override {
+    if (prepared_) return KH_OK;
+    for (int a = 0; a < 3; ++a) {
+      if (d_.pml_lo[a] < 0 || d_.pml_hi[a] < 0 || d_.pml_lo[a] + d_.pml_hi[a] > n_[a])
+        if (!(d_.pml_lo[a] == n_[a] && d_.pml_hi[a] == 0))
+          return fail(KH_ERR_INVALID, "PML widths exceed the axis");
+      lo_[a] = d_.pml_lo[a];
+      hi_[a] = d_.pml_hi[a];
+      pml_axis_[a] = lo_[a] > 0 || hi_[a] > 0;
+    }
+    const bool any_pml = pml_axis_[0] || pml_axis_[1] || pml_axis_[2];
+
+    if (d_.semantics != KH_SEM_REFERENCE_CPU && d_.semantics != KH_SEM_CPML)
+      return fail(KH_ERR_INVALID, "unknown CPML semantics");
+    // Regions with material conductivity (PhysicsFlags.has_sigma_{B,D}).
+    sigmask_b_ = region_mask(msigb_h_);
+    sigmask_d_ = region_mask(msigd_h_);
+    const bool any_msig = !msigb_h_[0].empty() || !msigb_h_[1].empty() || !msigb_h_[2].empty() ||
+                          !msigd_h_[0].empty() || !msigd_h_[1].empty() || !msigd_h_[2].empty();
+    if (d_.semantics == KH_SEM_CPML && any_msig && any_pml)
+      return fail(KH_ERR_UNSUPPORTED,
+                  "the CUDA-path CPML kernels take no material conductivity (CUDAKernels.jl:122-124)");
+    // The reference's generic_curl! has no method for C without U, or for a
+    // conductivity array with U but no C (Helpers.jl:39-270): reject.
+    for (int r = 0; r < 27; ++r) {
+      const int rr[3] = {r % 3, (r / 3) % 3, r / 9};
+      if (!region_nonempty(rr)) continue;
+      bool f[3];
+      for (int a = 0; a < 3; ++a) f[a] = rr[a] != 1;
+      if (!(f[0] || f[1] || f[2])) continue;
+      for (int c = 0; c < 3; ++c) {
+        const int nx = (c + 1) % 3, pv = (c + 2) % 3;
+        for (int h = 0; h < 2; ++h) {
+          const uint32_t mask = h ? sigmask_b_ : sigmask_d_;
+          const bool arr = h ? !msigb_h_[c].empty() : !msigd_h_[c].empty();
+          const bool hasC = ((mask >> r) & 1u) && (f[nx] || f[pv]);
+          const bool hasU = f[nx];
+          if ((hasC && !hasU) || (!hasC && hasU && arr))
+            return fail(KH_ERR_UNSUPPORTED,
+                        "material conductivity in this CPML region has no generic_curl! method "
+                        "in the reference (Helpers.jl:39-270)");
+        }
+      }
+    }
+
+    kh_status st = KH_OK;
+#define KH_TRY(x)            \
+  do {                       \
+    st = (x);                \
+    if (st != KH_OK) return st; \
+  } while (0)
+    for (int c = 0; c < 3; ++c) {
+      KH_TRY(alloc_field(&E_[c]));
+      KH_TRY(alloc_field(&H_[c]));
+    }
+    // classification and source tables
+    std::vector<uint32_t> cls(static_cast<size_t>(total_), 0u);
+    std::vector<uint8_t> tiles(size_t(nxb_) * n_[1] * n_[2], 0);
+    bool anySpecialE = false, anySpecialH = false;
+    auto cidx = [&](int i, int j, int k) { return origin_ + (long long)k * plane_ + (long long)j * pitch_ + i; };
+    auto mark = [&](int i, int j, int k, uint32_t bits) {
+      cls[cidx(i, j, k)] |= bits;
+      tiles[(size_t(k) * n_[1] + j) * nxb_ + i / (32 * VN)] |= (bits & kh::kSpecialE) ? 1 : 0;
+      tiles[(size_t(k) * n_[1] + j) * nxb_ + i / (32 * VN)] |= (bits & kh::kSpecialH) ? 2 : 0;
+    };
+    const size_t ncenter = size_t(n_[0]) * n_[1] * n_[2];
+    if (!chi3_h_.empty()) {
+      for (size_t q = 0; q < ncenter; ++q)
+        if (chi3_h_[q] != T(0)) {
+          const int i = int(q % n_[0]), j = int((q / n_[0]) % n_[1]), k = int(q / (size_t(n_[0]) * n_[1]));
+          mark(i, j, k, kh::kSpecialE | kh::kHasChi3);
+          anySpecialE = true;
+        }
+    }
+    for (auto& p : poles_)
+      for (size_t q = 0; q < ncenter; ++q)
+        if (p.sigma[q] != T(0)) {
+          const int i = int(q % n_[0]), j = int((q / n_[0]) % n_[1]), k = int(q / (size_t(n_[0]) * n_[1]));
+          mark(i, j, k, kh::kSpecialE | kh::kHasPole);
+          anySpecialE = true;
+        }
+    // Sparse source table: entries per cell in injection order
+    // (components Ex..Hz, then sources in order; Kernels.jl:455-463, Sources.jl:330-340).
+    struct Ent { long long cell; int src, comp; std::complex<double> amp; };
+    std::vector<Ent> ents;
+    for (int comp = 0; comp < 6; ++comp)
+      for (size_t si = 0; si < srcs_.size(); ++si) {
+        const SrcH& s = srcs_[si];
+        if (s.d.component != comp) continue;
+        for (int k = 0; k < s.d.dims[2]; ++k)
+          for (int j = 0; j < s.d.dims[1]; ++j)
+            for (int i = 0; i < s.d.dims[0]; ++i) {
+              const int gi = s.d.start[0] + i, gj = s.d.start[1] + j, gk = s.d.start[2] + k;
+              // cells outside the updated range are never consumed by the reference
+              if (gi < 0 || gj < 0 || gk < 0 || gi >= n_[0] || gj >= n_[1] || gk >= n_[2]) continue;
+              const std::complex<double> a = s.amp[(size_t(k) * s.d.dims[1] + j) * s.d.dims[0] + i];
+              const std::complex<T> aT(T(a.real()), T(a.imag()));
+              if (aT.real() == T(0) && aT.imag() == T(0)) continue;
+              ents.push_back({cidx(gi, gj, gk), int(si), comp, std::complex<double>(aT.real(), aT.imag())});
+              mark(gi, gj, gk, comp < 3 ? (kh::kSpecialE | kh::kHasSrcE) : (kh::kSpecialH | kh::kHasSrcH));
+              if (comp < 3) anySpecialE = true; else anySpecialH = true;
+            }
+      }
+    std::stable_sort(ents.begin(), ents.end(), [](const Ent& a, const Ent& b) { return a.cell < b.cell; });
+    std::vector<int> slot_off(1, 0), ent_src, ent_comp;
+    std::vector<Cplx<T>> ent_amp;
+    for (size_t e = 0; e < ents.size();) {
+      size_t e2 = e;
+      const int slot = int(slot_off.size() - 1);
+      if (slot >= (1 << 24)) return fail(KH_ERR_UNSUPPORTED, "too many source cells");
+      while (e2 < ents.size() && ents[e2].cell == ents[e].cell) {
+        ent_src.push_back(ents[e2].src);
+        ent_comp.push_back(ents[e2].comp);
+        ent_amp.push_back({T(ents[e2].amp.real()), T(ents[e2].amp.imag())});
+        ++e2;
+      }
+      slot_off.push_back(int(ent_src.size()));
+      cls[ents[e].cell] |= uint32_t(slot) << kh::kSlotShift;
+      e = e2;
+    }
+    n_special_e_ = 0;
+    for (size_t q = 0; q < cls.size(); ++q) n_special_e_ += (cls[q] & kh::kSpecialE) ? 1 : 0;
+
+    // state arrays that some cell needs
+    const bool msb = !msigb_h_[0].empty() || !msigb_h_[1].empty() || !msigb_h_[2].empty();
+    const bool msd = !msigd_h_[0].empty() || !msigd_h_[1].empty() || !msigd_h_[2].empty();
+    for (int c = 0; c < 3; ++c) {
+      const int nx = (c + 1) % 3, pv = (c + 2) % 3;
+      if (any_pml || anySpecialH) KH_TRY(alloc_field(&B_[c]));
+      if (any_pml || anySpecialE) KH_TRY(alloc_field(&D_[c]));
+      if (pml_axis_[nx]) { KH_TRY(alloc_field(&UB_[c])); KH_TRY(alloc_field(&UD_[c])); }
+      if (pml_axis_[c]) { KH_TRY(alloc_field(&WB_[c])); KH_TRY(alloc_field(&WD_[c])); }
+      if (msb && sigmask_b_ && (pml_axis_[nx] || pml_axis_[pv])) KH_TRY(alloc_field(&CB_[c]));
+      if (msd && sigmask_d_ && (pml_axis_[nx] || pml_axis_[pv])) KH_TRY(alloc_field(&CD_[c]));
+    }
+    // materials
+    for (int c = 0; c < 3; ++c) {
+      if (!eps_h_[c].empty()) KH_TRY(upload_center(eps_h_[c], &eps_[c], false));
+      if (!mu_h_[c].empty()) KH_TRY(upload_center(mu_h_[c], &mu_[c], false));
+      if (!msigd_h_[c].empty()) KH_TRY(upload_center(msigd_h_[c], &msigd_[c], false));
+      if (!msigb_h_[c].empty()) KH_TRY(upload_center(msigb_h_[c], &msigb_[c], false));
+    }
+    if ((eps_[0] != nullptr) != (eps_[2] != nullptr) || (eps_[0] != nullptr) != (eps_[1] != nullptr))
+      return fail(KH_ERR_INVALID, "per-voxel ε⁻¹ must be given for all three components");
+    if ((mu_[0] != nullptr) != (mu_[2] != nullptr) || (mu_[0] != nullptr) != (mu_[1] != nullptr))
+      return fail(KH_ERR_INVALID, "per-voxel μ⁻¹ must be given for all three components");
+    if (!chi3_h_.empty()) KH_TRY(upload_center(chi3_h_, &chi3_, false));
+    for (auto& p : poles_) {
+      PoleD pd;
+      KH_TRY(upload_center(p.sigma, &pd.sigma, false));
+      for (int c = 0; c < 3; ++c) {
+        KH_TRY(alloc_field(&pd.P[c]));
+        KH_TRY(alloc_field(&pd.Pp[c]));
+      }
+      pd.c = p.c;
+      poles_d_.push_back(pd);
+    }
+    for (int a = 0; a < 3; ++a) {
+      KH_TRY(upload_raw(sigb_h_[a].data(), sigb_h_[a].size() * sizeof(T), (void**)&sigb_[a]));
+      KH_TRY(upload_raw(sigd_h_[a].data(), sigd_h_[a].size() * sizeof(T), (void**)&sigd_[a]));
+    }
+    if (anySpecialE || anySpecialH) {
+      KH_TRY(upload_raw(cls.data(), cls.size() * sizeof(uint32_t), (void**)&cls_));
+      KH_TRY(upload_raw(tiles.data(), tiles.size(), (void**)&tiles_));
+    }
+    nsrc_ = int(srcs_.size());
+    if (!ent_src.empty()) {
+      KH_TRY(upload_raw(slot_off.data(), slot_off.size() * sizeof(int), (void**)&slot_off_));
+      KH_TRY(upload_raw(ent_src.data(), ent_src.size() * sizeof(int), (void**)&ent_src_));
+      KH_TRY(upload_raw(ent_comp.data(), ent_comp.size() * sizeof(int), (void**)&ent_comp_));
+      KH_TRY(upload_raw(ent_amp.data(), ent_amp.size() * sizeof(Cplx<T>), (void**)&ent_amp_));
+    }
+    // monitors
+    for (auto& m : mons_) {
+      m.ncell = (long long)m.dims[0] * m.dims[1] * m.dims[2];
+      const size_t bytes = size_t(m.ncell) * m.nf * sizeof(Cplx<T>);
+      KH_TRY(alloc_raw(bytes, (void**)&m.F, true));
+      if (sizeof(T) == 4) KH_TRY(alloc_raw(bytes, (void**)&m.C, true));
+    }
+    // last_source_time (TimeSources.jl:40-47); a CW source never cuts off.
+    has_cw_ = false;
+    last_time_ = -INFINITY;
+    for (auto& s : srcs_) {
+      if (s.d.time_kind == KH_TIME_CW) has_cw_ = true;
+      else last_time_ = std::max(last_time_, double(T(s.d.cutoff)));
+    }
+    KH_CUDA(cudaEventCreateWithFlags(&copy_done_, cudaEventDisableTiming));
+    KH_CUDA(cudaEventCreateWithFlags(&batch_done_, cudaEventDisableTiming));
+    KH_CUDA(cudaDeviceSynchronize());
+    prepared_ = true;
+    return KH_OK;
+#undef KH_TRY
+  }
+
+  // ---------------- stepping ----------------
+  kh_status step(int64_t nsteps, cudaStream_t stream) override {
+    if (!prepared_) return fail(KH_ERR_INVALID, "step before prepare");
+    if (nsteps < 0) return fail(KH_ERR_INVALID, "negative step count");
+    int64_t done = 0;
+    while (done < nsteps) {
+      const int nb = int(std::min<int64_t>(kBatch, nsteps - done));
+      kh_status st = run_batch(nb, stream);
+      if (st != KH_OK) return st;
+      done += nb;
+    }
+    return KH_OK;
+  }
+
+  int64_t timestep() const override { return timestep_; }
+  int sources_active() const override { return sources_active_ ? 1 : 0; }
+
+  // ---------------- results ----------------
+  kh_status get_field(int comp, double* out) override {
+    if (!prepared_) return fail(KH_ERR_INVALID, "get_field before prepare");
+    if (comp < 0 || comp > 5 || !out) return fail(KH_ERR_INVALID, "bad get_field arguments");
+    std::vector<T> h(static_cast<size_t>(total_));
+    KH_CUDA(cudaDeviceSynchronize());
+    KH_CUDA(cudaMemcpy(h.data(), comp < 3 ? E_[comp] : H_[comp - 3], total_ * sizeof(T),
+                       cudaMemcpyDeviceToHost));
+    static const int add[6][3] = {{0, 1, 1}, {1, 0, 1}, {1, 1, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    const int cd[3] = {n_[0] + add[comp][0], n_[1] + add[comp][1], n_[2] + add[comp][2]};
+    for (int k = 0; k < cd[2]; ++k)
+      for (int j = 0; j < cd[1]; ++j)
+        for (int i = 0; i < cd[0]; ++i)
+          out[(size_t(k) * cd[1] + j) * cd[0] + i] =
+              double(h[origin_ + (long long)k * plane_ + (long long)j * pitch_ + i]);
+    return KH_OK;
+  }
+
+  kh_status read_dft(int id, double* out) override {
+    if (id < 0 || id >= int(mons_.size()) || !out) return fail(KH_ERR_INVALID, "bad monitor id");
+    if (!prepared_) return fail(KH_ERR_INVALID, "read_dft before prepare");
+    const Mon& m = mons_[id];
+    const size_t cnt = size_t(m.ncell) * m.nf;
+    std::vector<Cplx<T>> F(cnt), C;
+    KH_CUDA(cudaDeviceSynchronize());
+    KH_CUDA(cudaMemcpy(F.data(), m.F, cnt * sizeof(Cplx<T>), cudaMemcpyDeviceToHost));
+    if (m.C) {
+      C.resize(cnt);
+      KH_CUDA(cudaMemcpy(C.data(), m.C, cnt * sizeof(Cplx<T>), cudaMemcpyDeviceToHost));
+    }
+    for (size_t q = 0; q < cnt; ++q) {
+      double re = double(F[q].re), im = double(F[q].im);
+      if (m.C) { re -= double(C[q].re); im -= double(C[q].im); }
+      out[2 * q] = re;
+      out[2 * q + 1] = im;
+    }
+    return KH_OK;
+  }
+
+  kh_status monitor_info(int id, int32_t* dims, int32_t* nf) const override {
+    if (id < 0 || id >= int(mons_.size())) return KH_ERR_INVALID;
+    for (int a = 0; a < 3; ++a) dims[a] = mons_[id].dims[a];
+    *nf = mons_[id].nf;
+    return KH_OK;
+  }
+
+  kh_status flux(const int32_t* ids, int normal, double dA, double* out) override {
+    if (!prepared_) return fail(KH_ERR_INVALID, "flux before prepare");
+    if (!ids || !out || normal < 0 || normal > 2) return fail(KH_ERR_INVALID, "bad flux arguments");
+    const Mon* m[4];
+    for (int q = 0; q < 4; ++q) {
+      if (ids[q] < 0 || ids[q] >= int(mons_.size())) return fail(KH_ERR_INVALID, "bad monitor id");
+      m[q] = &mons_[ids[q]];
+      if (m[q]->nf != m[0]->nf) return fail(KH_ERR_INVALID, "flux monitors differ in frequencies");
+    }
+    double* dout = nullptr;
+    KH_CUDA(cudaMalloc(&dout, sizeof(double) * m[0]->nf));
+    kh::launch_flux<T>(m[0]->F, m[1]->F, m[2]->F, m[3]->F, m[0]->C, m[1]->C, m[2]->C, m[3]->C,
+                       m[0]->dims, m[1]->dims, m[2]->dims, m[3]->dims, normal, m[0]->nf, dA, dout,
+                       nullptr);
+    ++launches;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(out, dout, sizeof(double) * m[0]->nf, cudaMemcpyDeviceToHost);
+    cudaFree(dout);
+    if (e != cudaSuccess) return fail(KH_ERR_CUDA, cudaGetErrorString(e));
+    return KH_OK;
+  }
+
+  kh_status reset() override {
+    if (!prepared_) return fail(KH_ERR_INVALID, "reset before prepare");
+    KH_CUDA(cudaDeviceSynchronize());
+    for (auto& s : state_) KH_CUDA(cudaMemset(s.first, 0, s.second));
+    timestep_ = 0;
+    sources_active_ = true;
+    return KH_OK;
+  }
+
+  int64_t state_bytes() const override {
+    int64_t b = 16;
+    for (auto& s : state_) b += int64_t(s.second);
+    return b;
+  }
+
+  kh_status export_state(void* dst, int64_t bytes) override {
+    if (!prepared_ || !dst || bytes != state_bytes()) return fail(KH_ERR_INVALID, "bad export buffer");
+    KH_CUDA(cudaDeviceSynchronize());
+    char* p = static_cast<char*>(dst);
+    int64_t hdr[2] = {timestep_, sources_active_ ? 1 : 0};
+    std::memcpy(p, hdr, 16);
+    p += 16;
+    for (auto& s : state_) {
+      KH_CUDA(cudaMemcpy(p, s.first, s.second, cudaMemcpyDeviceToHost));
+      p += s.second;
+    }
+    return KH_OK;
+  }
+
+  kh_status import_state(const void* src, int64_t bytes) override {
+    if (!prepared_ || !src || bytes != state_bytes()) return fail(KH_ERR_INVALID, "bad import buffer");
+    KH_CUDA(cudaDeviceSynchronize());
+    const char* p = static_cast<const char*>(src);
+    int64_t hdr[2];
+    std::memcpy(hdr, p, 16);
+    p += 16;
+    for (auto& s : state_) {
+      KH_CUDA(cudaMemcpy(s.first, p, s.second, cudaMemcpyHostToDevice));
+      p += s.second;
+    }
+    timestep_ = hdr[0];
+    sources_active_ = hdr[1] != 0;
+    return KH_OK;
+  }
+
+  // Compulsory-traffic model: the reference's 9 + 12 words per cell
+  // (benchmark/benchmark_metrics.jl:236-241) plus CPML auxiliaries of each
+  // region (2 words per auxiliary per component: read + write, with the B/D
+  // state counted where a U or W exists), dispersive and χ3 terms, and DFT
+  // monitor traffic amortised over the decimation.
+  double model_bytes_per_step() const override {
+    double h, e, d;
+    model_split(h, e, d);
+    return h + e + d;
+  }
+
+  void model_split(double& h_bytes, double& e_bytes, double& dft_bytes) const override {
+    const bool pervox_eps = eps_h_[0].size() > 0;
+    const bool pervox_mu = mu_h_[0].size() > 0;
+    const long long cells = 1LL * n_[0] * n_[1] * n_[2];
+    // H: E 3 rd + H 3 rd + H 3 wr (+ μ⁻¹ 3 rd); E: H 3 rd + E 3 rd + E 3 wr (+ ε⁻¹ 3 rd)
+    double hw = (9 + (pervox_mu ? 3 : 0)) * double(cells);
+    double ew = (9 + (pervox_eps ? 3 : 0)) * double(cells);
+    for (int r = 0; r < 27; ++r) {
+      const int rr[3] = {r % 3, (r / 3) % 3, r / 9};
+      long long cnt = 1;
+      bool f[3];
+      for (int a = 0; a < 3; ++a) {
+        int lo, hi;
+        axis_interval(a, rr[a], lo, hi);
+        cnt *= std::max(0, hi - lo);
+        f[a] = rr[a] != 1;
+      }
+      if (cnt == 0 || !(f[0] || f[1] || f[2])) continue;
+      int aux = 0;
+      for (int c = 0; c < 3; ++c) {
+        const int u = f[(c + 1) % 3] ? 1 : 0, w = f[c] ? 1 : 0, t = (u || w) ? 1 : 0;
+        aux += 2 * (u + w + t);
+      }
+      hw += double(aux) * double(cnt);  // B side
+      ew += double(aux) * double(cnt);  // D side
+    }
+    if (!chi3_h_.empty() || !poles_.empty()) {
+      const size_t ncenter = size_t(n_[0]) * n_[1] * n_[2];
+      for (size_t q = 0; q < ncenter; ++q) {
+        double w = 0;
+        bool sp = false;
+        if (!chi3_h_.empty() && chi3_h_[q] != T(0)) { w += 1; sp = true; }
+        for (auto& p : poles_)
+          if (p.sigma[q] != T(0)) { w += 1 + 12; sp = true; }  // σ + P, P_prev read + write
+        if (sp) w += 6;  // D state read + write
+        ew += w;
+      }
+    }
+    h_bytes = hw * sizeof(T);
+    e_bytes = ew * sizeof(T);
+    dft_bytes = 0;
+    for (auto& m : mons_) {
+      // field read + accumulator (and Kahan term) read + write per frequency
+      const double per = double(m.ncell) * (sizeof(T) + m.nf * 2.0 * sizeof(Cplx<T>) * (m.C ? 2 : 1));
+      dft_bytes += per / double(m.dec);
+    }
+  }
+
+  kh_status step_timed(int64_t nsteps, cudaStream_t stream, double* h_ms, double* e_ms,
+                       double* dft_ms) override {
+    if (!prepared_) return fail(KH_ERR_INVALID, "step before prepare");
+    if (nsteps < 0) return fail(KH_ERR_INVALID, "negative step count");
+    Timing t;
+    int64_t done = 0;
+    while (done < nsteps) {
+      const int nb = int(std::min<int64_t>(kBatch, nsteps - done));
+      kh_status st = run_batch(nb, stream, &t);
+      if (st != KH_OK) return st;
+      done += nb;
+    }
+    if (h_ms) *h_ms = t.h;
+    if (e_ms) *e_ms = t.e;
+    if (dft_ms) *dft_ms = t.dft;
+    return KH_OK;
+  }
+
+ private:
+  static constexpr int kBatch = 512;
+
+  struct Timing {
+    double h = 0, e = 0, dft = 0;
+  };
+  struct PoleH {
+    kh_pole_coeffs c;
+    std::vector<T> sigma;
+  };
+  struct PoleD {
+    kh_pole_coeffs c;
+    T* sigma = nullptr;
+    T* P[3] = {nullptr, nullptr, nullptr};
+    T* Pp[3] = {nullptr, nullptr, nullptr};
+  };
+  struct SrcH {
+    kh_source_desc d;
+    std::vector<std::complex<double>> amp;
+    std::vector<std::complex<T>> table;
+  };
+  struct Mon {
+    int comp, start[3], dims[3], nf, dec;
+    std::vector<double> freqs;
+    long long ncell = 0;
+    Cplx<T>* F = nullptr;
+    Cplx<T>* C = nullptr;
+  };
+
+  kh_status fail(kh_status s, const std::string& msg) {
+    err = msg;
+    return s;
+  }
+
+  void axis_interval(int a, int r, int& lo, int& hi) const {
+    if (d_.pml_lo[a] >= n_[a] && n_[a] > 0) {  // whole axis flagged
+      if (r == 0) { lo = 0; hi = n_[a]; } else { lo = hi = 0; }
+      return;
+    }
+    if (r == 0) { lo = 0; hi = d_.pml_lo[a]; }
+    else if (r == 1) { lo = d_.pml_lo[a]; hi = n_[a] - d_.pml_hi[a]; }
+    else { lo = n_[a] - d_.pml_hi[a]; hi = n_[a]; }
+    if (hi < lo) hi = lo;
+  }
+
+  bool region_nonempty(const int* rr) const {
+    for (int a = 0; a < 3; ++a) {
+      int lo, hi;
+      axis_interval(a, rr[a], lo, hi);
+      if (hi <= lo) return false;
+    }
+    return true;
+  }
+
+  uint32_t region_mask(const std::vector<T>* msig) const {
+    uint32_t mask = 0;
+    for (int r = 0; r < 27; ++r) {
+      const int rr[3] = {r % 3, (r / 3) % 3, r / 9};
+      if (!region_nonempty(rr)) continue;
+      int b[3][2];
+      for (int a = 0; a < 3; ++a) axis_interval(a, rr[a], b[a][0], b[a][1]);
+      bool nz = false;
+      for (int c = 0; c < 3 && !nz; ++c) {
+        if (msig[c].empty()) continue;
+        for (int k = b[2][0]; k < b[2][1] && !nz; ++k)
+          for (int j = b[1][0]; j < b[1][1] && !nz; ++j)
+            for (int i = b[0][0]; i < b[0][1]; ++i)
+              if (msig[c][(size_t(k) * n_[1] + j) * n_[0] + i] != T(0)) { nz = true; break; }
+      }
+      if (nz) mask |= 1u << r;
+    }
+    return mask;
+  }
+
+  kh_status alloc_raw(size_t bytes, void** out, bool is_state) {
+    void* p = nullptr;
+    KH_CUDA(cudaMalloc(&p, bytes));
+    allocs_.push_back(p);
+    KH_CUDA(cudaMemset(p, 0, bytes));
+    if (is_state) state_.push_back({p, bytes});
+    *out = p;
+    return KH_OK;
+  }
+  kh_status alloc_field(T** out) { return alloc_raw(size_t(total_) * sizeof(T), (void**)out, true); }
+
+  kh_status upload_raw(const void* h, size_t bytes, void** out) {
+    KH_CUDA(cudaMalloc(out, bytes));
+    allocs_.push_back(*out);
+    KH_CUDA(cudaMemcpy(*out, h, bytes, cudaMemcpyHostToDevice));
+    return KH_OK;
+  }
+
+  // Center-range host array (x fastest) → padded device layout.
+  kh_status upload_center(const std::vector<T>& h, T** out, bool is_state) {
+    std::vector<T> pad(static_cast<size_t>(total_), T(0));
+    for (int k = 0; k < n_[2]; ++k)
+      for (int j = 0; j < n_[1]; ++j)
+        std::memcpy(&pad[origin_ + (long long)k * plane_ + (long long)j * pitch_],
+                    &h[(size_t(k) * n_[1] + j) * n_[0]], sizeof(T) * n_[0]);
+    void* p = nullptr;
+    kh_status st = alloc_raw(pad.size() * sizeof(T), &p, is_state);
+    if (st != KH_OK) return st;
+    KH_CUDA(cudaMemcpy(p, pad.data(), pad.size() * sizeof(T), cudaMemcpyHostToDevice));
+    *out = static_cast<T*>(p);
+    return KH_OK;
+  }
+
+  // eval_time_source in the run's precision (TimeSources.jl:61-64, 123-132, 178-184)
+  std::complex<T> eval_time(const SrcH& s, double t, int64_t step, bool h_half) const {
+    const T two_pi = T(2) * T(M_PI);
+    if (s.d.time_kind == KH_TIME_GAUSSIAN) {
+      const T tt = T(t) - T(s.d.peak_time);
+      if (tt > T(s.d.cutoff)) return {T(0), T(0)};
+      const T w = T(s.d.width);
+      const T g = std::exp((-tt) * tt / ((T(2) * w) * w));
+      const T b = ((-two_pi) * T(s.d.fcen)) * tt;
+      return {g * std::cos(b), g * std::sin(b)};
+    }
+    if (s.d.time_kind == KH_TIME_CW) {
+      const T b = ((-two_pi) * T(s.d.fcen)) * T(t);
+      return {std::cos(b), std::sin(b)};
+    }
+    if (T(t) > T(s.d.cutoff)) return {T(0), T(0)};
+    const int64_t q = 2 * step + (h_half ? 0 : 1);
+    if (q >= int64_t(s.table.size())) return {T(0), T(0)};
+    return s.table[q];
+  }
+
+  kh_status run_batch(int nb, cudaStream_t stream, Timing* timing = nullptr) {
+    // A batch on a new stream waits for the previous batch, whose kernels read
+    // the shared time-factor table this batch is about to overwrite.
+    if (last_stream_ != stream && batch_done_) KH_CUDA(cudaStreamWaitEvent(stream, batch_done_, 0));
+    // Host pass: source activity, time factors and DFT phases for nb steps.
+    struct StepPlan {
+      bool sa;
+      size_t fH, fE;                      // offsets into the table (Cplx<T> units)
+      std::vector<std::pair<int, size_t>> dftH, dftE;  // (monitor, phase offset)
+    };
+    std::vector<StepPlan> plan(nb);
+    std::vector<Cplx<T>> tab;
+    for (int s = 0; s < nb; ++s) {
+      const int64_t ts = timestep_ + s;
+      const double t = double(T(ts) * dt_);  // round_time
+      if (sources_active_ && !has_cw_ && nsrc_ > 0 && t > last_time_) sources_active_ = false;
+      StepPlan& P = plan[s];
+      P.sa = sources_active_ && nsrc_ > 0 && ent_src_ != nullptr;
+      const double tE = t + double(dt_ / T(2));
+      P.fH = tab.size();
+      if (P.sa)
+        for (auto& src : srcs_) {
+          std::complex<T> f = eval_time(src, t, ts, true);
+          tab.push_back({f.real(), f.imag()});
+        }
+      P.fE = tab.size();
+      if (P.sa)
+        for (auto& src : srcs_) {
+          std::complex<T> f = eval_time(src, tE, ts, false);
+          tab.push_back({f.real(), f.imag()});
+        }
+      for (int mi = 0; mi < int(mons_.size()); ++mi) {
+        const Mon& m = mons_[mi];
+        if (m.dec > 1 && ts % m.dec != 0) continue;
+        const bool hm = m.comp >= 3;
+        const double time = hm ? t : tE;
+        const size_t off = tab.size();
+        for (int f = 0; f < m.nf; ++f) {
+          // Δt·exp(i·f·2π·time): θ formed as the reference forms it
+          // (complex_backend_number(im*2π*time), Monitors.jl:287-297); FP32 runs
+          // evaluate the phase in FP64 and round once.
+          double re, im;
+          if (sizeof(T) == 8) {
+            const double th = double(T(m.freqs[f])) * double(T(6.283185307179586 * time));
+            re = double(dt_) * std::cos(th);
+            im = double(dt_) * std::sin(th);
+          } else {
+            const double th = double(T(m.freqs[f])) * (6.283185307179586 * time);
+            re = double(dt_) * std::cos(th);
+            im = double(dt_) * std::sin(th);
+          }
+          tab.push_back({T(re), T(im)});
+        }
+        (hm ? P.dftH : P.dftE).push_back({mi, off});
+      }
+    }
+    // Upload the table (pinned staging, one copy per batch).
+    const size_t bytes = std::max<size_t>(tab.size(), 1) * sizeof(Cplx<T>);
+    if (bytes > tab_cap_) {
+      KH_CUDA(cudaStreamSynchronize(stream));
+      if (tab_dev_) cudaFree(tab_dev_);
+      if (pinned_) cudaFreeHost(pinned_);
+      tab_dev_ = nullptr;
+      pinned_ = nullptr;
+      KH_CUDA(cudaMalloc(&tab_dev_, bytes * 2));
+      KH_CUDA(cudaMallocHost(&pinned_, bytes * 2));
+      tab_cap_ = bytes * 2;
+    } else if (pending_copy_) {
+      KH_CUDA(cudaEventSynchronize(copy_done_));
+    }
+    if (!tab.empty()) {
+      std::memcpy(pinned_, tab.data(), tab.size() * sizeof(Cplx<T>));
+      KH_CUDA(cudaMemcpyAsync(tab_dev_, pinned_, tab.size() * sizeof(Cplx<T>),
+                              cudaMemcpyHostToDevice, stream));
+      KH_CUDA(cudaEventRecord(copy_done_, stream));
+      pending_copy_ = true;
+    }
+    const Cplx<T>* dtab = static_cast<const Cplx<T>*>(tab_dev_);
+
+    // Timed runs bracket every launch group with events: 5 per step.
+    if (timing) {
+      while (events_.size() < size_t(5 * nb)) {
+        cudaEvent_t ev;
+        KH_CUDA(cudaEventCreate(&ev));
+        events_.push_back(ev);
+      }
+    }
+    auto mark = [&](int s, int k) {
+      if (timing) cudaEventRecord(events_[5 * s + k], stream);
+    };
+    kh::HalfStepParams<T> ph = base_params(true), pe = base_params(false);
+    for (int s = 0; s < nb; ++s) {
+      const StepPlan& P = plan[s];
+      ph.sources_active = P.sa ? 1 : 0;
+      ph.f_now = dtab + P.fH;
+      mark(s, 0);
+      kh::launch_half_step<T>(true, ph, stream);
+      ++launches;
+      mark(s, 1);
+      for (auto& dm : P.dftH) launch_dft_for(dm.first, dtab + dm.second, stream);
+      mark(s, 2);
+      pe.sources_active = P.sa ? 1 : 0;
+      pe.f_now = dtab + P.fE;
+      kh::launch_half_step<T>(false, pe, stream);
+      ++launches;
+      mark(s, 3);
+      for (auto& dm : P.dftE) launch_dft_for(dm.first, dtab + dm.second, stream);
+      mark(s, 4);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(KH_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    KH_CUDA(cudaEventRecord(batch_done_, stream));
+    last_stream_ = stream;
+    timestep_ += nb;
+    if (timing) {
+      KH_CUDA(cudaEventSynchronize(events_[5 * nb - 1]));
+      for (int s = 0; s < nb; ++s) {
+        float a = 0, b = 0, c = 0, d = 0;
+        KH_CUDA(cudaEventElapsedTime(&a, events_[5 * s], events_[5 * s + 1]));
+        KH_CUDA(cudaEventElapsedTime(&b, events_[5 * s + 1], events_[5 * s + 2]));
+        KH_CUDA(cudaEventElapsedTime(&c, events_[5 * s + 2], events_[5 * s + 3]));
+        KH_CUDA(cudaEventElapsedTime(&d, events_[5 * s + 3], events_[5 * s + 4]));
+        timing->h += a;
+        timing->dft += b + d;
+        timing->e += c;
+      }
+    }
+    return KH_OK;
+  }
+
+  void launch_dft_for(int mi, const Cplx<T>* phase, cudaStream_t stream) {
+    const Mon& m = mons_[mi];
+    kh::DftParams<T> p;
+    p.field = m.comp < 3 ? E_[m.comp] : H_[m.comp - 3];
+    p.pitch = pitch_;
+    p.plane = plane_;
+    p.origin = origin_;
+    for (int a = 0; a < 3; ++a) {
+      p.start[a] = m.start[a];
+      p.dims[a] = m.dims[a];
+    }
+    p.nf = m.nf;
+    p.phase = phase;
+    p.F = m.F;
+    p.comp = m.C;
+    kh::launch_dft<T>(p, stream);
+    ++launches;
+  }
+
+  kh::HalfStepParams<T> base_params(bool h) const {
+    kh::HalfStepParams<T> p;
+    std::memset(&p, 0, sizeof(p));
+    p.nx = n_[0];
+    p.ny = n_[1];
+    p.nz = n_[2];
+    p.pitch = pitch_;
+    p.plane = plane_;
+    p.origin = origin_;
+    p.nxb = nxb_;
+    p.dt = dt_;
+    for (int a = 0; a < 3; ++a) p.inv_d[a] = T(1) / delta_[a];
+    for (int c = 0; c < 3; ++c) {
+      p.A[c] = h ? E_[c] : H_[c];
+      p.O[c] = h ? H_[c] : E_[c];
+      p.Ts[c] = h ? B_[c] : D_[c];
+      p.U[c] = h ? UB_[c] : UD_[c];
+      p.W[c] = h ? WB_[c] : WD_[c];
+      p.C[c] = h ? CB_[c] : CD_[c];
+      p.m_inv[c] = h ? mu_[c] : eps_[c];
+      p.msig[c] = h ? msigb_[c] : msigd_[c];
+      p.sig[c] = h ? sigb_[c] : sigd_[c];
+      p.pml_lo[c] = lo_[c];
+      p.pml_hi[c] = hi_[c];
+    }
+    p.cpml = d_.semantics == KH_SEM_CPML ? 1 : 0;
+    p.m_scalar = h ? T(d_.mu_inv) : T(d_.eps_inv);
+    p.sigma_region_mask = h ? sigmask_b_ : sigmask_d_;
+    p.tile_flag = tiles_;
+    p.cell_class = cls_;
+    p.tile_bit = h ? 2 : 1;
+    p.slot_off = slot_off_;
+    p.ent_src = ent_src_;
+    p.ent_comp = ent_comp_;
+    p.ent_amp = ent_amp_;
+    p.chi3 = h ? nullptr : chi3_;
+    p.npoles = h ? 0 : int(poles_d_.size());
+    if (!h)
+      for (size_t q = 0; q < poles_d_.size(); ++q) {
+        const PoleD& d = poles_d_[q];
+        kh::PoleParams<T>& pp = p.poles[q];
+        pp.gamma1_inv = T(d.c.gamma1_inv);
+        pp.gamma1 = T(d.c.gamma1);
+        pp.coeff_p = T(2) - T(d.c.omega0_dt_sq);
+        pp.drive = d.c.is_drude ? T(d.c.drude_coeff) : T(d.c.sigma_omega0_dt_sq);
+        pp.is_drude = d.c.is_drude;
+        pp.sigma = d.sigma;
+        for (int c = 0; c < 3; ++c) {
+          pp.P[c] = d.P[c];
+          pp.Pprev[c] = d.Pp[c];
+        }
+      }
+    return p;
+  }
+
+  kh_sim_desc d_;
+  int n_[3];
+  T dt_, delta_[3];
+  long long pitch_, plane_, origin_, total_;
+  int nxb_;
+  int lo_[3] = {0, 0, 0}, hi_[3] = {0, 0, 0};
+  bool pml_axis_[3] = {false, false, false};
+  uint32_t sigmask_b_ = 0, sigmask_d_ = 0;
+  bool prepared_ = false;
+
+  std::vector<T> sigb_h_[3], sigd_h_[3], eps_h_[3], mu_h_[3], msigd_h_[3], msigb_h_[3], chi3_h_;
+  std::vector<PoleH> poles_;
+  std::vector<PoleD> poles_d_;
+  std::vector<SrcH> srcs_;
+  std::vector<Mon> mons_;
+  int nsrc_ = 0;
+  long long n_special_e_ = 0;
+
+  std::vector<void*> allocs_;
+  std::vector<std::pair<void*, size_t>> state_;
+  T *E_[3] = {}, *H_[3] = {}, *B_[3] = {}, *D_[3] = {};
+  T *UB_[3] = {}, *UD_[3] = {}, *WB_[3] = {}, *WD_[3] = {}, *CB_[3] = {}, *CD_[3] = {};
+  T *eps_[3] = {}, *mu_[3] = {}, *msigd_[3] = {}, *msigb_[3] = {}, *chi3_ = nullptr;
+  T *sigb_[3] = {}, *sigd_[3] = {};
+  uint32_t* cls_ = nullptr;
+  uint8_t* tiles_ = nullptr;
+  int *slot_off_ = nullptr, *ent_src_ = nullptr, *ent_comp_ = nullptr;
+  Cplx<T>* ent_amp_ = nullptr;
+
+  void* tab_dev_ = nullptr;
+  void* pinned_ = nullptr;
+  size_t tab_cap_ = 0;
+  bool pending_copy_ = false;
+  cudaEvent_t copy_done_ = nullptr;
+  cudaEvent_t batch_done_ = nullptr;
+  cudaStream_t last_stream_ = nullptr;
+  std::vector<cudaEvent_t> events_;
+
+  int64_t timestep_ = 0;
+  bool sources_active_ = true, has_cw_ = false;
+  double last_time_ = 0;
+};
+
+}  // namespace
+
+struct kh_sim {
+  std::unique_ptr<SimBase> impl;
+  std::string err;
+};
+
+extern "C" {
+
+const char* kh_version(void) { return kVersion; }
+
+kh_status kh_device_info(int32_t* sm_count, int32_t* cc_major, int32_t* cc_minor) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return KH_ERR_CUDA;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) return KH_ERR_CUDA;
+  if (sm_count) *sm_count = prop.multiProcessorCount;
+  if (cc_major) *cc_major = prop.major;
+  if (cc_minor) *cc_minor = prop.minor;
+  return KH_OK;
+}
+
+kh_status kh_sim_create(const kh_sim_desc* desc, kh_sim** out) {
+  if (!desc || !out) return KH_ERR_INVALID;
+  *out = nullptr;
+  if (desc->n[0] <= 0 || desc->n[1] <= 0 || desc->n[2] <= 0) return KH_ERR_INVALID;
+  if (desc->dtype != KH_F32 && desc->dtype != KH_F64) return KH_ERR_INVALID;
+  if (!(desc->dt > 0) || !(desc->delta[0] > 0) || !(desc->delta[1] > 0) || !(desc->delta[2] > 0))
+    return KH_ERR_INVALID;
+  kh_sim* s = new (std::nothrow) kh_sim();
+  if (!s) return KH_ERR_OOM;
+  if (desc->dtype == KH_F32) s->impl.reset(new Sim<float>(*desc));
+  else s->impl.reset(new Sim<double>(*desc));
+  *out = s;
+  return KH_OK;
+}
+
+void kh_sim_destroy(kh_sim* sim) { delete sim; }
+
+const char* kh_last_error(const kh_sim* sim) {
+  if (!sim) return "null handle";
+  return sim->impl->err.c_str();
+}
+
+kh_status kh_sim_set_material(kh_sim* sim, int32_t kind, int32_t comp, const double* values) {
+  if (!sim) return KH_ERR_INVALID;
+  return sim->impl->set_material(kind, comp, values);
+}
+
+kh_status kh_sim_add_pole(kh_sim* sim, const kh_pole_coeffs* coeffs, const double* sigma) {
+  if (!sim || !coeffs) return KH_ERR_INVALID;
+  return sim->impl->add_pole(*coeffs, sigma);
+}
+
+kh_status kh_sim_add_source(kh_sim* sim, const kh_source_desc* src) {
+  if (!sim || !src) return KH_ERR_INVALID;
+  return sim->impl->add_source(*src);
+}
+
+kh_status kh_sim_add_dft_monitor(kh_sim* sim, int32_t component, const int32_t start[3],
+                                 const int32_t dims[3], int32_t nfreq, const double* freqs,
+                                 int32_t decimation, int32_t* out_id) {
+  if (!sim) return KH_ERR_INVALID;
+  return sim->impl->add_monitor(component, start, dims, nfreq, freqs, decimation, out_id);
+}
+
+kh_status kh_sim_prepare(kh_sim* sim) {
+  if (!sim) return KH_ERR_INVALID;
+  return sim->impl->prepare();
+}
+
+kh_status kh_sim_step(kh_sim* sim, int64_t nsteps, void* stream) {
+  if (!sim) return KH_ERR_INVALID;
+  return sim->impl->step(nsteps, static_cast<cudaStream_t>(stream));
+}
+
+kh_status kh_sim_synchronize(kh_sim* sim) {
+  if (!sim) return KH_ERR_INVALID;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) {
+    sim->impl->err = cudaGetErrorString(e);
+    return KH_ERR_CUDA;
+  }
+  return KH_OK;
+}
+
+kh_status kh_sim_timestep(const kh_sim* sim, int64_t* out) {
+  if (!sim || !out) return KH_ERR_INVALID;
+  *out = sim->impl->timestep();
+  return KH_OK;
+}
+
+kh_status kh_sim_sources_active(const kh_sim* sim, int32_t* out) {
+  if (!sim || !out) return KH_ERR_INVALID;
+  *out = sim->impl->sources_active();
+  return KH_OK;
+}
+
+kh_status kh_sim_launch_count(const kh_sim* sim, int64_t* out) {
+  if (!sim || !out) return KH_ERR_INVALID;
+  *out = sim->impl->launches;
+  return KH_OK;
+}
+
+kh_status kh_sim_get_field(kh_sim* sim, int32_t component, double* out) {
+  if (!sim) return KH_ERR_INVALID;
+  return sim->impl->get_field(component, out);
+}
+
+kh_status kh_sim_read_dft(kh_sim* sim, int32_t monitor_id, double* out) {
+  if (!sim) return KH_ERR_INVALID;
+  return sim->impl->read_dft(monitor_id, out);
+}
+
+kh_status kh_sim_monitor_info(const kh_sim* sim, int32_t monitor_id, int32_t dims[3], int32_t* nfreq) {
+  if (!sim || !dims || !nfreq) return KH_ERR_INVALID;
+  return sim->impl->monitor_info(monitor_id, dims, nfreq);
+}
+
+kh_status kh_sim_flux(kh_sim* sim, const int32_t ids[4], int32_t normal_axis, double dA, double* out) {
+  if (!sim) return KH_ERR_INVALID;
+  return sim->impl->flux(ids, normal_axis, dA, out);
+}
+
+kh_status kh_sim_reset(kh_sim* sim) {
+  if (!sim) return KH_ERR_INVALID;
+  return sim->impl->reset();
+}
+
+kh_status kh_sim_state_bytes(const kh_sim* sim, int64_t* out) {
+  if (!sim || !out) return KH_ERR_INVALID;
+  *out = sim->impl->state_bytes();
+  return KH_OK;
+}
+
+kh_status kh_sim_export_state(kh_sim* sim, void* host_dst, int64_t bytes) {
+  if (!sim) return KH_ERR_INVALID;
+  return sim->impl->export_state(host_dst, bytes);
+}
+
+kh_status kh_sim_import_state(kh_sim* sim, const void* host_src, int64_t bytes) {
+  if (!sim) return KH_ERR_INVALID;
+  return sim->impl->import_state(host_src, bytes);
+}
+
+kh_status kh_sim_model_bytes_split(const kh_sim* sim, double* h_half, double* e_half, double* dft) {
+  if (!sim || !h_half || !e_half || !dft) return KH_ERR_INVALID;
+  sim->impl->model_split(*h_half, *e_half, *dft);
+  return KH_OK;
+}
+
+kh_status kh_sim_step_timed(kh_sim* sim, int64_t nsteps, void* stream, double* h_ms, double* e_ms,
+                            double* dft_ms) {
+  if (!sim) return KH_ERR_INVALID;
+  return sim->impl->step_timed(nsteps, static_cast<cudaStream_t>(stream), h_ms, e_ms, dft_ms);
+}
+
+kh_status kh_sim_model_bytes_per_step(const kh_sim* sim, double* out) {
+  if (!sim || !out) return KH_ERR_INVALID;
+  *out = sim->impl->model_bytes_per_step();
+  return KH_OK;
+}
+
+}  // extern "C"

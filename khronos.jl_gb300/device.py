@@ -1,0 +1,177 @@
+"""GpuSim: one SimSpec realised as a kh_sim handle of libkhronos_gb300.so."""
+from __future__ import annotations
+
+import ctypes as C
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import _abi
+from .grid import COMPONENT_EXTRA
+from .spec import SimSpec, flat_complex, flat_f
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class GpuSim:
+    """Device-resident simulation driven through the C ABI."""
+
+    def __init__(self, spec: SimSpec, lib=None):
+        self.spec = spec
+        self.lib = lib or _abi.load()
+        self.handle = C.c_void_p()
+        self._keep = []  # host arrays referenced by the descriptor during creation
+        d = _abi.SimDesc()
+        for a in range(3):
+            d.n[a] = int(spec.n[a])
+            d.delta[a] = float(spec.delta[a])
+            d.pml_lo[a] = int(spec.pml_lo[a])
+            d.pml_hi[a] = int(spec.pml_hi[a])
+            for name in ("sigma_b", "sigma_d"):
+                arr = getattr(spec, name)[a]
+                if arr is not None:
+                    h = np.ascontiguousarray(arr, dtype=np.float64)
+                    self._keep.append(h)
+                    getattr(d, name)[a] = _dptr(h)
+        d.dtype = int(spec.dtype)
+        d.dt = float(spec.dt)
+        d.eps_inv = float(spec.eps_inv)
+        d.mu_inv = float(spec.mu_inv)
+        d.semantics = int(spec.semantics)
+        self._check(self.lib.kh_sim_create(C.byref(d), C.byref(self.handle)))
+        try:
+            for kind, comp, arr in spec.materials:
+                h = flat_f(arr)
+                self._check(self.lib.kh_sim_set_material(self.handle, kind, comp, _dptr(h)))
+            for p in spec.poles:
+                pc = _abi.PoleCoeffs(**p.coeffs)
+                h = flat_f(p.sigma)
+                self._check(self.lib.kh_sim_add_pole(self.handle, C.byref(pc), _dptr(h)))
+            for s in spec.sources:
+                sd = _abi.SourceDesc()
+                sd.component = s.component
+                for a in range(3):
+                    sd.start[a] = int(s.start[a])
+                    sd.dims[a] = int(s.dims[a])
+                amp = flat_complex(s.amp)
+                sd.amp = _dptr(amp)
+                sd.time_kind = s.time_kind
+                sd.fcen, sd.width, sd.peak_time, sd.cutoff = s.fcen, s.width, s.peak_time, s.cutoff
+                tab = None
+                if s.table is not None:
+                    tab = flat_complex(np.asarray(s.table).reshape(-1))
+                    sd.table_len = int(np.asarray(s.table).shape[0])
+                    sd.table = _dptr(tab)
+                self._check(self.lib.kh_sim_add_source(self.handle, C.byref(sd)))
+            self.monitor_ids: List[int] = []
+            for m in spec.monitors:
+                st = (C.c_int32 * 3)(*m.start)
+                dm = (C.c_int32 * 3)(*m.dims)
+                fr = np.ascontiguousarray(m.freqs, dtype=np.float64)
+                mid = C.c_int32()
+                self._check(self.lib.kh_sim_add_dft_monitor(self.handle, m.component, st, dm, len(fr),
+                                                            _dptr(fr), int(m.decimation), C.byref(mid)))
+                self.monitor_ids.append(mid.value)
+            self._check(self.lib.kh_sim_prepare(self.handle))
+        except Exception:
+            self.close()
+            raise
+        self._keep.clear()
+
+    def _check(self, st):
+        _abi.check(st, self.lib, self.handle)
+
+    def close(self):
+        if self.handle:
+            self.lib.kh_sim_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- stepping ---------------------------------------------------------
+    def step(self, nsteps: int = 1, stream: Optional[int] = None):
+        self._check(self.lib.kh_sim_step(self.handle, int(nsteps), C.c_void_p(stream) if stream else None))
+
+    def synchronize(self):
+        self._check(self.lib.kh_sim_synchronize(self.handle))
+
+    @property
+    def timestep(self) -> int:
+        v = C.c_int64()
+        self._check(self.lib.kh_sim_timestep(self.handle, C.byref(v)))
+        return v.value
+
+    @property
+    def sources_active(self) -> bool:
+        v = C.c_int32()
+        self._check(self.lib.kh_sim_sources_active(self.handle, C.byref(v)))
+        return bool(v.value)
+
+    @property
+    def launches(self) -> int:
+        v = C.c_int64()
+        self._check(self.lib.kh_sim_launch_count(self.handle, C.byref(v)))
+        return v.value
+
+    # -- results ------------------------------------------------------------
+    def field(self, comp: int) -> np.ndarray:
+        """Component array in the reference's component dimensions, indexed [i, j, k]."""
+        dims = tuple(self.spec.n[a] + COMPONENT_EXTRA[comp][a] for a in range(3))
+        out = np.zeros(int(np.prod(dims)), dtype=np.float64)
+        self._check(self.lib.kh_sim_get_field(self.handle, comp, _dptr(out)))
+        return out.reshape(dims, order="F")
+
+    def dft(self, monitor_index: int) -> np.ndarray:
+        """DFT accumulator of a monitor, shape (Nx, Ny, Nz, Nf), complex128."""
+        m = self.spec.monitors[monitor_index]
+        cnt = int(np.prod(m.dims)) * len(m.freqs)
+        out = np.zeros(2 * cnt, dtype=np.float64)
+        self._check(self.lib.kh_sim_read_dft(self.handle, self.monitor_ids[monitor_index], _dptr(out)))
+        z = out[0::2] + 1j * out[1::2]
+        return z.reshape(tuple(m.dims) + (len(m.freqs),), order="F")
+
+    def flux(self, monitor_indices: Sequence[int], normal_axis: int, dA: float) -> np.ndarray:
+        ids = (C.c_int32 * 4)(*[self.monitor_ids[i] for i in monitor_indices])
+        nf = len(self.spec.monitors[monitor_indices[0]].freqs)
+        out = np.zeros(nf, dtype=np.float64)
+        self._check(self.lib.kh_sim_flux(self.handle, ids, int(normal_axis), float(dA), _dptr(out)))
+        return out
+
+    def model_bytes_per_step(self) -> float:
+        v = C.c_double()
+        self._check(self.lib.kh_sim_model_bytes_per_step(self.handle, C.byref(v)))
+        return v.value
+
+    def model_bytes_split(self):
+        """(H half-step, E half-step, DFT) model bytes of one step."""
+        h, e, d = C.c_double(), C.c_double(), C.c_double()
+        self._check(self.lib.kh_sim_model_bytes_split(self.handle, C.byref(h), C.byref(e), C.byref(d)))
+        return h.value, e.value, d.value
+
+    def step_timed(self, nsteps: int, stream: Optional[int] = None):
+        """Step with CUDA events around every launch; returns (H ms, E ms, DFT ms) summed."""
+        h, e, d = C.c_double(), C.c_double(), C.c_double()
+        self._check(self.lib.kh_sim_step_timed(self.handle, int(nsteps), C.c_void_p(stream) if stream else None,
+                                               C.byref(h), C.byref(e), C.byref(d)))
+        return h.value, e.value, d.value
+
+    # -- state ----------------------------------------------------------------
+    def reset(self):
+        self._check(self.lib.kh_sim_reset(self.handle))
+
+    def export_state(self) -> bytes:
+        n = C.c_int64()
+        self._check(self.lib.kh_sim_state_bytes(self.handle, C.byref(n)))
+        buf = (C.c_char * n.value)()
+        self._check(self.lib.kh_sim_export_state(self.handle, buf, n.value))
+        return bytes(buf)
+
+    def import_state(self, data: bytes):
+        buf = (C.c_char * len(data)).from_buffer_copy(data)
+        self._check(self.lib.kh_sim_import_state(self.handle, buf, len(data)))

@@ -1,0 +1,261 @@
+"""Simulation: host mirror of Khronos's user API over the CUDA step loop.
+
+Mirrors the reference's ``Simulation(...)`` / ``prepare_simulation!`` /
+``run(sim; until, until_after_sources)`` / ``get_flux`` calls
+(src/DataStructures.jl:714-801, src/Simulation.jl:92-387,
+src/Monitors/FluxMonitor.jl:92-156).  Geometry is given as per-voxel material
+arrays on the Center range (rasterisation of shapes is set-up, not part of the
+step loop); everything else follows the reference's arithmetic.
+"""
+from __future__ import annotations
+
+import math
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import grid as G
+from .monitors import DFTMonitor, FluxMonitor, auto_decimation, flux_from_dft
+from .sources import ContinuousWaveSource, CustomSource, GaussianPulseSource
+from .spec import (KH_F32, KH_F64, MAT_CHI3, MAT_EPS_INV, MAT_MU_INV, MAT_SIGMA_B, MAT_SIGMA_D,
+                   SEM_CPML, SEM_REFERENCE_CPU,
+                   TIME_CW, TIME_GAUSSIAN, TIME_TABLE, LorentzianSusceptibility, MonitorSpec, PoleSpec,
+                   SimSpec, SourceSpec, ade_coefficients)
+
+
+class Simulation:
+    """A 3D Khronos simulation whose step loop runs on the GPU.
+
+    ``semantics`` selects the CPML stage logic: "cpml" (default) follows the
+    reference's CUDA PML kernels and is stable; "reference_cpu" restates the
+    reference's CPU-backend dispatch exactly, including the dropped σ_prev
+    stage that makes that path grow without bound once PML is present.
+
+    Materials (all optional; arrays are (Nx, Ny, Nz), cell-indexed):
+      eps_inv: scalar or 3 arrays (ε⁻¹ per Yee component), mu_inv likewise,
+      sigma_d / sigma_b: 3 conductivity arrays, chi3: one Center array,
+      poles: list of (LorentzianSusceptibility, σ array) — ε⁻¹ must already
+      carry the χ1 semi-implicit correction (``apply_chi1_correction``).
+    """
+
+    def __init__(self, *, cell_size, resolution, sources=(), cell_center=(0.0, 0.0, 0.0),
+                 boundaries=None, monitors=(), dtype="f32", courant=0.5, eps_inv=1.0, mu_inv=1.0,
+                 sigma_d=None, sigma_b=None, chi3=None, poles=(), semantics="cpml"):
+        self.grid = G.Grid.build(cell_size, cell_center, resolution, dtype, courant)
+        self.dtype = dtype
+        self.sources = list(sources)
+        self.boundaries = boundaries
+        self.monitors = list(monitors)
+        self.eps_inv = eps_inv
+        self.mu_inv = mu_inv
+        self.sigma_d = sigma_d
+        self.sigma_b = sigma_b
+        self.chi3 = chi3
+        self.poles = list(poles)
+        if semantics not in ("cpml", "reference_cpu"):
+            raise ValueError("semantics must be 'cpml' or 'reference_cpu'")
+        self.semantics = semantics
+        self._dev = None
+        self._dft_monitors: List[DFTMonitor] = []
+
+    # -- convenience --------------------------------------------------------
+    @property
+    def n(self):
+        return self.grid.n
+
+    @property
+    def dt(self):
+        return self.grid.dt
+
+    def round_time(self, timestep: Optional[int] = None) -> float:
+        """round_time(sim) = Float64(timestep·Δt) in the run's precision (Simulation.jl:22)."""
+        ts = self.timestep if timestep is None else timestep
+        T = self.grid.T
+        return float(T(T(ts) * self.grid.dt))
+
+    def last_source_time(self) -> float:
+        """max cutoff over sources; ∞ if any CW source (TimeSources.jl:40-47, Kernels.jl:27-35)."""
+        T = self.grid.T
+        if not self.sources:
+            return math.inf
+        return max(s.time_profile.cutoff_time(T) for s in self.sources)
+
+    # -- prepare ------------------------------------------------------------
+    def spec(self) -> SimSpec:
+        """Host-side set-up of prepare_simulation! as a backend-independent SimSpec."""
+        g = self.grid
+        T = g.T
+        sp = SimSpec(n=g.n, dtype=KH_F32 if T is np.float32 else KH_F64,
+                     delta=tuple(float(d) for d in g.delta), dt=float(g.dt),
+                     semantics=SEM_CPML if self.semantics == "cpml" else SEM_REFERENCE_CPU)
+        if self.boundaries is not None:
+            lo, hi = G.pml_widths(g, self.boundaries)
+            sp.pml_lo, sp.pml_hi = lo, hi
+            for a in range(3):
+                L, R = self.boundaries[a]
+                s = G.cell_sigma(g, a, L, R).astype(np.float64)
+                sp.sigma_b[a] = s
+                sp.sigma_d[a] = s.copy()
+        # materials
+        if np.isscalar(self.eps_inv):
+            sp.eps_inv = float(T(self.eps_inv))
+        else:
+            for c in range(3):
+                sp.materials.append((MAT_EPS_INV, c, np.asarray(self.eps_inv[c], dtype=np.float64)))
+        if np.isscalar(self.mu_inv):
+            sp.mu_inv = float(T(self.mu_inv))
+        else:
+            for c in range(3):
+                sp.materials.append((MAT_MU_INV, c, np.asarray(self.mu_inv[c], dtype=np.float64)))
+        for kind, arrs in ((MAT_SIGMA_D, self.sigma_d), (MAT_SIGMA_B, self.sigma_b)):
+            if arrs is not None:
+                for c in range(3):
+                    if arrs[c] is not None:
+                        sp.materials.append((kind, c, np.asarray(arrs[c], dtype=np.float64)))
+        if self.chi3 is not None:
+            sp.materials.append((MAT_CHI3, 0, np.asarray(self.chi3, dtype=np.float64)))
+        for sus, sigma in self.poles:
+            sp.poles.append(PoleSpec(coeffs=ade_coefficients(sus, float(g.dt)),
+                                     sigma=np.asarray(sigma, dtype=np.float64)))
+        # sources (assemble_sources, Sources.jl:44-92)
+        for src in self.sources:
+            tp = src.time_profile
+            for comp in src.components():
+                gv, amp = src.amplitude_array(g, comp)
+                s = SourceSpec(component=comp, start=gv.start0, dims=tuple(amp.shape), amp=amp,
+                               time_kind=TIME_GAUSSIAN)
+                if isinstance(tp, GaussianPulseSource):
+                    st = tp.stored(T)
+                    s.fcen, s.width, s.peak_time, s.cutoff = (float(st["fcen"]), float(st["width"]),
+                                                              float(st["peak_time"]), float(st["cutoff"]))
+                elif isinstance(tp, ContinuousWaveSource):
+                    s.time_kind = TIME_CW
+                    s.fcen = float(T(tp.fcen))
+                elif isinstance(tp, CustomSource):
+                    s.time_kind = TIME_TABLE
+                    s.fcen = float(T(tp.fcen))
+                    s.cutoff = float(T(tp.end_time))
+                    tab = np.zeros((tp.table_steps, 2), dtype=np.complex128)
+                    dt = g.dt
+                    for n in range(tp.table_steps):
+                        t0 = float(T(T(n) * dt))
+                        t1 = t0 + float(dt / T(2))
+                        tab[n, 0] = complex(tp.src_func(float(T(t0))))
+                        tab[n, 1] = complex(tp.src_func(float(T(t1))))
+                    s.table = tab
+                else:
+                    raise TypeError(f"unsupported time profile {type(tp).__name__}")
+                sp.sources.append(s)
+        # monitors: auto-decimation then init (Simulation.jl:165-172)
+        D = auto_decimation(self.sources, g.dt) if self.sources else 1
+        self._dft_monitors = []
+        for m in self.monitors:
+            if m.decimation == 1 and D > 1:
+                m.decimation = D
+            if isinstance(m, FluxMonitor):
+                self._dft_monitors.extend(m.expand(g))
+            else:
+                self._dft_monitors.append(m)
+        for m in self._dft_monitors:
+            gv = g.grid_volume(m.center, m.size, m.component)
+            m.gv = gv
+            sp.monitors.append(MonitorSpec(component=m.component, start=gv.start0, dims=gv.dims,
+                                           freqs=np.array([float(T(f)) for f in m.frequencies]),
+                                           decimation=int(m.decimation)))
+        return sp
+
+    def prepare(self):
+        """prepare_simulation!: build the spec and the device state."""
+        if self._dev is not None:
+            return self
+        from .device import GpuSim
+
+        sp = self.spec()
+        self._spec = sp
+        self._dev = GpuSim(sp)
+        for idx, m in enumerate(self._dft_monitors):
+            m.monitor_id = idx
+            m.sim = self
+        for m in self.monitors:
+            m.sim = self
+        return self
+
+    # -- running --------------------------------------------------------------
+    @property
+    def timestep(self) -> int:
+        return self._dev.timestep if self._dev is not None else 0
+
+    def step(self, nsteps: int = 1, stream: Optional[int] = None):
+        self.prepare()
+        self._dev.step(nsteps, stream)
+
+    def steps_until(self, until: float) -> int:
+        """Steps `run(sim; until)` takes: while !(round_time > until) step!."""
+        ts = self.timestep
+        n = 0
+        while not (self.round_time(ts + n) > until):
+            n += 1
+        return n
+
+    def run(self, until: Optional[float] = None, until_after_sources: Optional[float] = None):
+        """run(sim; until | until_after_sources) (Simulation.jl:295-382)."""
+        if (until is None) == (until_after_sources is None):
+            raise ValueError("Must specify exactly one of until / until_after_sources")
+        self.prepare()
+        if until_after_sources is not None:
+            last = self.last_source_time()
+            n = 0
+            ts = self.timestep
+            while self.round_time(ts + n) <= last:
+                n += 1
+            self.step(n)
+            until = until_after_sources
+        self.step(self.steps_until(until))
+
+    # -- results ----------------------------------------------------------------
+    def get_field(self, comp: int) -> np.ndarray:
+        self.prepare()
+        return self._dev.field(comp)
+
+    def _read_dft(self, m: DFTMonitor) -> np.ndarray:
+        return self._dev.dft(m.monitor_id)
+
+    def _flux(self, fm: FluxMonitor) -> np.ndarray:
+        ids = [m.monitor_id for m in fm.e_monitors + fm.h_monitors]
+        return self._dev.flux(ids, fm.normal_axis, fm.dA)
+
+    def get_flux(self, fm: FluxMonitor, on_device: bool = True) -> np.ndarray:
+        if on_device:
+            return self._flux(fm)
+        e1, e2 = (self._read_dft(m) for m in fm.e_monitors)
+        h1, h2 = (self._read_dft(m) for m in fm.h_monitors)
+        return flux_from_dft(fm.normal_axis, e1, e2, h1, h2, fm.dA)
+
+    def close(self):
+        if self._dev is not None:
+            self._dev.close()
+            self._dev = None
+
+
+def apply_chi1_correction(eps_inv, poles, dt, T=np.float64):
+    """ε⁻¹ → ε⁻¹ / (1 + ε⁻¹·χ1), χ1 = Σ_p γ₁⁻¹·C_p·σ_p/2 (Geometry.jl:1236-1250, 1335-1341).
+
+    Applied cell by cell (the reference indexes the three component arrays by
+    the linear index of a Center-sized array; with component-sized arrays that
+    is an offset, and the aligned cell-by-cell form is the intended one).
+    """
+    chi1 = None
+    for sus, sigma in poles:
+        c = ade_coefficients(sus, float(dt))
+        k = c["gamma1_inv"] * (c["drude_coeff"] if c["is_drude"] else c["sigma_omega0_dt_sq"]) / 2
+        term = np.asarray(sigma, dtype=T) * T(k)
+        chi1 = term if chi1 is None else chi1 + term
+    if chi1 is None:
+        return eps_inv
+    out = []
+    for e in eps_inv:
+        e = np.array(e, dtype=T, copy=True)
+        mask = chi1 != 0
+        e[mask] = e[mask] / (T(1) + e[mask] * chi1[mask])
+        out.append(e)
+    return out

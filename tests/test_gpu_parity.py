@@ -1,0 +1,245 @@
+"""CUDA step loop vs the CPU oracle, through the C ABI, on seeded inputs.
+
+Bar: FP64 fields and DFT values within 1e-10 relative L2 of the oracle (both
+CPML semantics); FP32 within 2e-4 relative L2 of the FP32 oracle (different
+rounding: FMA contraction and the B/D-free update of plain cells).
+"""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import dft_errors, field_errors, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"f64": 1e-10, "f32": 2e-4}
+
+
+def safe_rel(a, b):
+    s = max(float(np.max(np.abs(b))), 1e-300)
+    return rel_l2(a / s, b / s)
+
+
+def compare(spec, steps, oracle, gpu_lib, tol, check_dft=True, chunks=1):
+    from khronos_gb300.device import GpuSim
+
+    gpu = GpuSim(spec, lib=gpu_lib)
+    ref = oracle.OracleSim(spec)
+    per = steps // chunks
+    for _ in range(chunks):
+        gpu.step(per)
+        ref.step(per)
+    assert gpu.timestep == ref.timestep
+    assert gpu.sources_active == ref.sources_active
+    worst = {}
+    fa = [gpu.field(c) for c in range(6)]
+    fb = [ref.field(c) for c in range(6)]
+    for c in range(6):
+        assert np.all(np.isfinite(fa[c])) == np.all(np.isfinite(fb[c]))
+    for c, e in enumerate(field_errors(fa, fb)):
+        worst[f"field{c}"] = e
+    if check_dft and spec.monitors:
+        da = [gpu.dft(m) for m in range(len(spec.monitors))]
+        db = [ref.dft(m) for m in range(len(spec.monitors))]
+        for m, e in enumerate(dft_errors(da, db)):
+            worst[f"dft{m}"] = e
+    gpu.close()
+    ref.close()
+    bad = {k: v for k, v in worst.items() if not v <= tol}
+    assert not bad, f"relative L2 above {tol}: {bad}"
+    return worst
+
+
+@pytest.mark.parametrize("semantics", ["cpml", "reference_cpu"])
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_dipole_small(kh, oracle, gpu_lib, semantics, dtype):
+    from khronos_gb300 import configs
+
+    w = configs.dipole(dtype=dtype, steps=160, resolution=10)
+    w.sim.semantics = semantics
+    steps = 160 if (semantics == "cpml" or dtype == "f64") else 60  # f32 CPU path overflows later
+    compare(w.sim.spec(), steps, oracle, gpu_lib, TOL[dtype])
+
+
+@pytest.mark.parametrize("semantics", ["cpml", "reference_cpu"])
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_waveguide_scaled(kh, oracle, gpu_lib, semantics, dtype):
+    from khronos_gb300 import configs
+
+    w = configs.waveguide(dtype=dtype, scale=0.25)
+    w.sim.semantics = semantics
+    steps = 120 if (semantics == "cpml" or dtype == "f64") else 50
+    compare(w.sim.spec(), steps, oracle, gpu_lib, TOL[dtype], chunks=2)
+
+
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_dispersive_scaled(kh, oracle, gpu_lib, dtype):
+    from khronos_gb300 import configs
+
+    w = configs.dispersive(dtype=dtype, scale=0.25)
+    compare(w.sim.spec(), 150, oracle, gpu_lib, TOL[dtype])
+
+
+def _odd_sim(kh, semantics="cpml", dtype="f64", boundaries=((0.3, 0.2), (0.2, 0.4), (0.4, 0.3)), **kw):
+    srcs = [
+        kh.UniformSource(time_profile=kh.GaussianPulseSource(fcen=0.8, fwidth=0.3), component=kh.EZ,
+                         center=(0.31, -0.22, 0.13), size=(0, 0, 0)),
+        kh.UniformSource(time_profile=kh.GaussianPulseSource(fcen=0.8, fwidth=0.3), component=kh.EZ,
+                         center=(0.31, -0.22, 0.13), size=(0, 0, 0), amplitude=0.5 - 0.25j),
+        kh.UniformSource(time_profile=kh.ContinuousWaveSource(fcen=0.6), component=kh.HY,
+                         center=(-0.5, 0.3, -0.2), size=(0, 0.4, 0)),
+        kh.UniformSource(time_profile=kh.CustomSource(src_func=lambda t: math.sin(3 * t) * math.exp(-t / 4),
+                                                      fcen=0.5, fwidth=0.3, end_time=6.0, table_steps=400),
+                         component=kh.EX, center=(0.1, 0.1, -0.4), size=(0.3, 0, 0)),
+    ]
+    mons = [kh.DFTMonitor(component=kh.EZ, center=(0.2, 0, 0), size=(0, math.inf, math.inf),
+                          frequencies=[0.7, 0.8]),
+            kh.DFTMonitor(component=kh.HX, center=(0, 0, 0.3), size=(0.6, 0.5, 0), frequencies=[0.8],
+                          decimation=3)]
+    return kh.Simulation(cell_size=(3.7, 2.3, 1.9), resolution=10, sources=srcs, boundaries=boundaries,
+                         monitors=mons, dtype=dtype, semantics=semantics, **kw)
+
+
+@pytest.mark.parametrize("semantics", ["cpml", "reference_cpu"])
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_odd_grid_mixed_sources(kh, oracle, gpu_lib, semantics, dtype):
+    """37×23×19 (not a multiple of the vector width), asymmetric PML, stacked
+    sources on one cell, an H source, CW and tabulated time profiles, a monitor
+    reaching the staggered wall layer, decimation."""
+    sim = _odd_sim(kh, semantics, dtype)
+    steps = 150 if (semantics == "cpml" or dtype == "f64") else 40
+    compare(sim.spec(), steps, oracle, gpu_lib, TOL[dtype])
+
+
+@pytest.mark.parametrize("boundaries", [None, ((0.5, 0.5), (0, 0), (0, 0)), ((0, 0), (0, 0), (0.3, 0.0))])
+def test_partial_or_no_pml(kh, oracle, gpu_lib, boundaries):
+    sim = _odd_sim(kh, "cpml", "f64", boundaries=boundaries)
+    compare(sim.spec(), 120, oracle, gpu_lib, TOL["f64"])
+
+
+def test_whole_axis_pml_fallback(kh, oracle, gpu_lib):
+    """PML thicker than half the axis: the reference plans a single chunk whose
+    PML flags cover whole axes (Chunking.jl:907-931)."""
+    src = kh.UniformSource(time_profile=kh.GaussianPulseSource(fcen=0.8, fwidth=0.3), component=kh.EZ)
+    sim = kh.Simulation(cell_size=(1.2, 1.0, 0.8), resolution=10, sources=[src],
+                        boundaries=[[0.7, 0.7]] * 3, dtype="f64")
+    sp = sim.spec()
+    assert sp.pml_lo == sp.n and sp.pml_hi == (0, 0, 0)
+    compare(sp, 80, oracle, gpu_lib, TOL["f64"], check_dft=False)
+
+
+def test_source_cutoff_transition(kh, oracle, gpu_lib):
+    """A short pulse whose cutoff falls inside the run: sources switch off on
+    the same step in both (Kernels.jl:27-35)."""
+    src = kh.UniformSource(time_profile=kh.GaussianPulseSource(fcen=1.0, fwidth=2.0), component=kh.EY,
+                           center=(0.05, 0.0, -0.1), size=(0.4, 0.3, 0))
+    sim = kh.Simulation(cell_size=(2.0, 2.0, 2.0), resolution=10, sources=[src],
+                        boundaries=[[0.3, 0.3]] * 3, dtype="f64")
+    sp = sim.spec()
+    from khronos_gb300.device import GpuSim
+
+    gpu = GpuSim(sp, lib=gpu_lib)
+    ref = oracle.OracleSim(sp)
+    n_cut = sim.steps_until(sp.sources[0].cutoff) + 1
+    gpu.step(n_cut - 2)
+    ref.step(n_cut - 2)
+    assert gpu.sources_active and ref.sources_active
+    gpu.step(4)
+    ref.step(4)
+    assert not gpu.sources_active and not ref.sources_active
+    gpu.step(40)
+    ref.step(40)
+    errs = field_errors([gpu.field(c) for c in range(6)], [ref.field(c) for c in range(6)])
+    assert max(errs) <= TOL["f64"]
+
+
+def test_per_voxel_mu_and_chi3_without_pml(kh, oracle, gpu_lib):
+    rng = np.random.default_rng(5)
+    n = (24, 20, 16)
+    mu = [1.0 / rng.uniform(1.0, 2.0, size=n) for _ in range(3)]
+    eps = [1.0 / rng.uniform(1.0, 4.0, size=n) for _ in range(3)]
+    chi3 = np.where(rng.uniform(size=n) > 0.7, 0.05, 0.0)
+    src = kh.UniformSource(time_profile=kh.GaussianPulseSource(fcen=0.8, fwidth=0.4), component=kh.EX,
+                           center=(0, 0, 0), size=(0.5, 0.5, 0.5), amplitude=4.0)
+    sim = kh.Simulation(cell_size=(2.4, 2.0, 1.6), resolution=10, sources=[src], dtype="f64",
+                        eps_inv=eps, mu_inv=mu, chi3=chi3)
+    compare(sim.spec(), 100, oracle, gpu_lib, TOL["f64"], check_dft=False)
+
+
+def test_material_conductivity_reference_cpu(kh, oracle, gpu_lib):
+    """σD/σB act only inside PML chunks on the CPU path; without PML they are
+    ignored (step_curl_and_update! has no conductivity argument)."""
+    n = (20, 18, 16)
+    sd = [np.full(n, 0.3) for _ in range(3)]
+    src = kh.UniformSource(time_profile=kh.GaussianPulseSource(fcen=0.8, fwidth=0.4), component=kh.EZ)
+    sim = kh.Simulation(cell_size=(2.0, 1.8, 1.6), resolution=10, sources=[src], dtype="f64",
+                        sigma_d=sd, sigma_b=sd, semantics="reference_cpu")
+    compare(sim.spec(), 60, oracle, gpu_lib, TOL["f64"], check_dft=False)
+
+
+def test_material_conductivity_with_pml_is_rejected(kh, gpu_lib, oracle):
+    """The reference has no generic_curl! method for conductivity in face
+    chunks (C allocated without U): both refuse the configuration."""
+    from khronos_gb300 import _abi
+    from khronos_gb300.device import GpuSim
+
+    n = (20, 18, 16)
+    sd = [np.full(n, 0.3) for _ in range(3)]
+    src = kh.UniformSource(time_profile=kh.GaussianPulseSource(fcen=0.8, fwidth=0.4), component=kh.EZ)
+    for sem in ("reference_cpu", "cpml"):
+        sim = kh.Simulation(cell_size=(2.0, 1.8, 1.6), resolution=10, sources=[src], dtype="f64",
+                            sigma_d=sd, boundaries=[[0.3, 0.3]] * 3, semantics=sem)
+        with pytest.raises(_abi.KhError) as e:
+            GpuSim(sim.spec(), lib=gpu_lib)
+        assert e.value.status == _abi.KH_ERR_UNSUPPORTED
+        with pytest.raises(RuntimeError):
+            oracle.OracleSim(sim.spec())
+
+
+def test_flux_on_device_matches_host(kh, oracle, gpu_lib):
+    from khronos_gb300 import configs
+    from khronos_gb300.device import GpuSim
+    from khronos_gb300.monitors import flux_from_dft
+
+    w = configs.waveguide(dtype="f64", scale=0.25)
+    sp = w.sim.spec()
+    gpu = GpuSim(sp, lib=gpu_lib)
+    ref = oracle.OracleSim(sp)
+    gpu.step(200)
+    ref.step(200)
+    base = 0
+    for fm in w.flux_monitors:
+        ids = list(range(base, base + 4))
+        base += 4
+        dev = gpu.flux(ids, fm.normal_axis, fm.dA)
+        host = flux_from_dft(fm.normal_axis, *[ref.dft(i) for i in ids], fm.dA)
+        assert np.allclose(dev, host, rtol=1e-9, atol=1e-12 * np.max(np.abs(host)))
+
+
+def test_reset_and_state_roundtrip(kh, gpu_lib):
+    """N steps == k steps + export/import + N-k steps; reset() reproduces a fresh run."""
+    from khronos_gb300 import configs
+    from khronos_gb300.device import GpuSim
+
+    w = configs.waveguide(dtype="f32", scale=0.25)
+    sp = w.sim.spec()
+    a = GpuSim(sp, lib=gpu_lib)
+    a.step(90)
+    fa = [a.field(c) for c in range(6)]
+    da = a.dft(0)
+    b = GpuSim(sp, lib=gpu_lib)
+    b.step(37)
+    blob = b.export_state()
+    c = GpuSim(sp, lib=gpu_lib)
+    c.import_state(blob)
+    assert c.timestep == 37
+    c.step(53)
+    for comp in range(6):
+        assert np.array_equal(c.field(comp), fa[comp])
+    assert np.array_equal(c.dft(0), da)
+    a.reset()
+    assert a.timestep == 0 and a.sources_active
+    a.step(90)
+    for comp in range(6):
+        assert np.array_equal(a.field(comp), fa[comp])
