@@ -222,25 +222,9 @@ def run_ours(args, world, rank, local_rank):
     gpu.close()
 
     # ---- end to end through the C ABI with host buffers ------------------------
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    g2 = GpuSim(spec)  # host arrays -> device (materials, σ, sources, monitors)
-    g2.step(args.steps, sh)
-    dft_host = [g2.dft(m) for m in range(len(spec.monitors))]
-    fluxes = [g2.flux(list(range(4 * i, 4 * i + 4)), fm.normal_axis, fm.dA)
-              for i, fm in enumerate(w.flux_monitors)]
-    torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    g2.close()
-    h2d = sum(a.nbytes for _, _, a in spec.materials) // 2  # values cross as the run's FP32
-    h2d += sum(s.amp.size * 16 for s in spec.sources) + sum(x.size * 8 for x in spec.sigma_b + spec.sigma_d
-                                                            if x is not None)
-    d2h = sum(d.size * 16 for d in dft_host) + sum(f.size * 8 for f in fluxes)
-    t2 = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-    if dist:
-        dist.all_reduce(t2, op=dist.ReduceOp.MAX)
-    e2e_value = world * cells * args.steps / float(t2.item()) / 1e9
-
+    e2e = None
+    if not args.no_e2e:
+        e2e = end_to_end(args, spec, w, sh, world, dist, cells)
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -266,10 +250,9 @@ def run_ours(args, world, rank, local_rank):
                      "step_achieved": (h_bytes + e_bytes + dft_bytes) / (ms_max / args.steps / 1e3) / 1e9},
         "clocks": clk.summary(),
         "gpu_launches": launches,
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d / args.steps,
-                "d2h_bytes_per_step": d2h / args.steps,
-                "scope": "GpuSim(spec) from host arrays + K steps + DFT arrays and flux read back to host"},
     }
+    if e2e is not None:
+        line["e2e"] = e2e
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(spec)
     print(json.dumps(line), flush=True)
@@ -278,13 +261,42 @@ def run_ours(args, world, rank, local_rank):
     return 0
 
 
+def end_to_end(args, spec, w, sh, world, dist, cells):
+    """Same metric through the C ABI from host buffers: create + upload, K steps,
+    DFT arrays and fluxes read back to the host, all inside the timed region."""
+    import torch
+    from khronos_gb300.device import GpuSim
+
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    g2 = GpuSim(spec)  # host arrays -> device (materials, σ, sources, monitors)
+    g2.step(args.steps, sh)
+    dft_host = [g2.dft(m) for m in range(len(spec.monitors))]
+    fluxes = [g2.flux(list(range(4 * i, 4 * i + 4)), fm.normal_axis, fm.dA)
+              for i, fm in enumerate(w.flux_monitors)]
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    g2.close()
+    h2d = sum(a.nbytes for _, _, a in spec.materials) // 2  # values cross as the run's FP32
+    h2d += sum(s.amp.size * 16 for s in spec.sources) + sum(x.size * 8 for x in spec.sigma_b + spec.sigma_d
+                                                            if x is not None)
+    d2h = sum(d.size * 16 for d in dft_host) + sum(f.size * 8 for f in fluxes)
+    t2 = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+    if dist:
+        dist.all_reduce(t2, op=dist.ReduceOp.MAX)
+    return {"value": world * cells * args.steps / float(t2.item()) / 1e9, "unit": UNIT,
+            "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
+            "scope": "GpuSim(spec) from host arrays + K steps + DFT arrays and flux read back to host"}
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--steps", type=int, default=4000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3

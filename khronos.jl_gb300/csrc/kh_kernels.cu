@@ -2,62 +2,76 @@
 //
 // One fused kernel per half-step replaces the reference's per-chunk dispatch
 // (step_H_fused!/step_E_fused!, src/Kernels/Kernels.jl:164-454): the curl,
-// the CPML cascade (Helpers.jl:30-270), the constitutive update
-// (Helpers.jl:323-409), source injection (Sources.jl:346-357) and, on the E
-// half, the χ3 correction (Dispersive.jl:127-147) and the ADE pole update
-// (Dispersive.jl:25-88) all happen in one pass over the grid.
+// the CPML cascade (Helpers.jl:30-270, CUDAKernels.jl:150-281), the
+// constitutive update (Helpers.jl:323-409), source injection
+// (Sources.jl:346-357) and, on the E half, the χ3 correction
+// (Dispersive.jl:127-147) and the ADE pole update (Dispersive.jl:25-88) all
+// happen in one pass over the grid.
 //
-// Work decomposition: a warp owns 32 × VEC consecutive x cells of one row
-// (VEC = 16 bytes of the run's type) and marches over kPlanesPerCta z planes;
-// the CTA holds kBlockY rows.  x neighbours come from warp shuffles, the z
-// neighbour plane is carried in registers from the previous plane (2.5D
-// register rotation), y neighbours are vector loads that hit L1 (the row
-// above belongs to the next warp of the same CTA).
+// Work decomposition: a warp owns 32 × VN consecutive x cells of one row and
+// marches over kPlanesPerCta z planes; the CTA holds kBlockY rows.  x
+// neighbours come from warp shuffles, the z-neighbour plane is carried in
+// registers from the previous plane (2.5D register rotation), y neighbours are
+// vector loads that hit L1/L2 (the row above belongs to the next warp of the
+// same CTA).
+//
+// Every array a thread needs for its VN cells is loaded as one vector before
+// any arithmetic, so a plane costs one memory round trip also in CPML rows.
 //
 // Which arrays a cell touches is a static property of the cell:
 //  * plain cells (no CPML region flag, no source/χ3/pole) keep no B/D state:
 //    O += m⁻¹·K.  This equals m⁻¹·(T + K) of the reference up to rounding and
 //    is exact when m⁻¹ = 1;
-//  * all other cells keep B/D and follow the reference's dispatch on which
-//    CPML auxiliaries its region allocates (Chunking.jl:1069-1146).
+//  * all other cells keep B/D and follow the reference's stage logic for the
+//    CPML auxiliaries their region allocates (Chunking.jl:1069-1146).
 #include <cuda_runtime.h>
 
 #include "kh_kernels.cuh"
 
 namespace kh {
 
-template <typename T>
+template <typename T, int VN>
 struct VT;
 template <>
-struct VT<float> {
+struct VT<float, 4> {
   using V = float4;
 };
 template <>
-struct VT<double> {
+struct VT<float, 2> {
+  using V = float2;
+};
+template <>
+struct VT<double, 2> {
   using V = double2;
 };
 
-template <typename T>
-__device__ __forceinline__ void vld(const T* ptr, T (&v)[Vec<T>::N]) {
-  using V = typename VT<T>::V;
+template <typename T, int VN>
+__device__ __forceinline__ void vld(const T* ptr, T (&v)[VN]) {
+  using V = typename VT<T, VN>::V;
   V x = *reinterpret_cast<const V*>(ptr);
-  if constexpr (Vec<T>::N == 4) {
+  if constexpr (VN == 4) {
     v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
   } else {
     v[0] = x.x; v[1] = x.y;
   }
 }
 
-template <typename T>
-__device__ __forceinline__ void vst(T* ptr, const T (&v)[Vec<T>::N]) {
-  using V = typename VT<T>::V;
+template <typename T, int VN>
+__device__ __forceinline__ void vst(T* ptr, const T (&v)[VN]) {
+  using V = typename VT<T, VN>::V;
   V x;
-  if constexpr (Vec<T>::N == 4) {
+  if constexpr (VN == 4) {
     x.x = v[0]; x.y = v[1]; x.z = v[2]; x.w = v[3];
   } else {
     x.x = v[0]; x.y = v[1];
   }
   *reinterpret_cast<V*>(ptr) = x;
+}
+
+template <typename T, int VN>
+__device__ __forceinline__ void vzero(T (&v)[VN]) {
+#pragma unroll
+  for (int q = 0; q < VN; ++q) v[q] = T(0);
 }
 
 // update_field_from_curl (Helpers.jl:30-33)
@@ -70,17 +84,20 @@ __device__ __forceinline__ T ufc(T A, T B, T s) {
   return ((T(1) - s) * A + B) / (T(1) + s);
 }
 
-// Per-cell update of one cell that keeps B/D state, or sits in a CPML region,
-// or carries a source, χ3 or a pole.
+// Update of one cell that sits in a CPML region or carries a source, χ3 or a
+// pole.  t/u/w are the cell's B|D state and CPML U/W values (loaded and stored
+// by the caller), m its μ⁻¹|ε⁻¹, c3 its χ3.  Conductivity (C, σ) and pole
+// arrays are rare and read here directly.
 template <typename T, bool H>
 __device__ __forceinline__ void general_cell(const HalfStepParams<T>& p, long long q, int i, int j,
                                              int k, bool fx, bool fy, bool fz, uint32_t cls,
-                                             bool special, const T (&K)[3], T (&O)[3]) {
+                                             bool special, const T (&K)[3], const T (&m)[3],
+                                             T (&O)[3], T (&t)[3], T (&u)[3], T (&w)[3], T c3) {
   const bool f[3] = {fx, fy, fz};
   const int ix3[3] = {i, j, k};
   const bool region = fx || fy || fz;
   bool regC = false;
-  if (region) {
+  if (region && p.sigma_region_mask) {
     const int rx = i < p.pml_lo[0] ? 0 : (i >= p.nx - p.pml_hi[0] ? 2 : 1);
     const int ry = j < p.pml_lo[1] ? 0 : (j >= p.ny - p.pml_hi[1] ? 2 : 1);
     const int rz = k < p.pml_lo[2] ? 0 : (k >= p.nz - p.pml_hi[2] ? 2 : 1);
@@ -119,89 +136,80 @@ __device__ __forceinline__ void general_cell(const HalfStepParams<T>& p, long lo
     const bool hasW = region && f[c];
     const bool hasC = regC && (f[nx_] || f[pv]);
     const bool hasSD = region && p.msig[c] != nullptr;
-    const T m = p.m_inv[c] ? p.m_inv[c][q] : p.m_scalar;
     const bool keepT = special || (p.cpml ? region : (hasU || hasW || hasC || hasSD));
     if (!keepT) {
-      O[c] = O[c] + m * K[c];
+      O[c] = O[c] + m[c] * K[c];
       continue;
     }
-    T t = p.Ts[c][q];
+    T tc = t[c];
     if (!region) {
-      t = t + K[c];  // step_curl_and_update! (ReferenceKernels.jl:340-345)
+      tc = tc + K[c];  // step_curl_and_update! (ReferenceKernels.jl:340-345)
     } else if (p.cpml) {
       // _cuda_pml_BH_kernel!/_cuda_pml_DE_kernel! stages (CUDAKernels.jl:150-281)
       const T sn = p.sig[nx_][ix3[nx_]];
       const T sp = p.sig[pv][ix3[pv]];
       T in_t = K[c];
       if (f[nx_] && sn != T(0)) {
-        const T u = p.U[c][q];
-        const T un = ufc(u, K[c], sn);
-        p.U[c][q] = un;
-        in_t = un - u;
+        const T un = ufc(u[c], K[c], sn);
+        in_t = un - u[c];
+        u[c] = un;
       }
-      t = (f[pv] && sp != T(0)) ? ((T(1) - sp) * t + in_t) / (T(1) + sp) : t + in_t;
+      tc = (f[pv] && sp != T(0)) ? ((T(1) - sp) * tc + in_t) / (T(1) + sp) : tc + in_t;
     } else {
       const T sn = p.sig[nx_][ix3[nx_]];
       const T sp = p.sig[pv][ix3[pv]];
       if (hasC && hasU) {
         const T sD = hasSD ? T(0.5) * (p.dt * p.msig[c][q]) : T(0);
-        const T u = p.U[c][q];
+        const T uo = u[c];
         if (hasSD && sD != T(0)) {  // three-stage cascade (Helpers.jl:60-67)
           const T cc = p.C[c][q];
           const T cn = ufc(cc, K[c], sD);
           p.C[c][q] = cn;
-          const T un = ufc_old(u, cn, cc, sn);
-          p.U[c][q] = un;
-          t = ufc_old(t, un, u, sp);
+          u[c] = ufc_old(uo, cn, cc, sn);
         } else {  // two-stage cascade (Helpers.jl:53-59, 72-78)
-          const T un = ufc(u, K[c], sn);
-          p.U[c][q] = un;
-          t = ufc_old(t, un, u, sp);
+          u[c] = ufc(uo, K[c], sn);
         }
+        tc = ufc_old(tc, u[c], uo, sp);
       } else if (hasU) {  // C absent (Helpers.jl:113-139)
         if (sn == T(0)) {
-          t = ufc(t, K[c], sp);
+          tc = ufc(tc, K[c], sp);
         } else {
-          const T u = p.U[c][q];
-          const T un = ufc(u, K[c], sn);
-          p.U[c][q] = un;
-          t = ufc_old(t, un, u, sp);
+          const T uo = u[c];
+          u[c] = ufc(uo, K[c], sn);
+          tc = ufc_old(tc, u[c], uo, sp);
         }
       } else if (hasSD) {  // C and U absent, conductivity present (Helpers.jl:225-240)
         const T sD = T(0.5) * (p.dt * p.msig[c][q]);
-        t = ufc(t, K[c], sD);
+        tc = ufc(tc, K[c], sD);
       } else {  // C and U absent: σ_prev dropped (Helpers.jl:208-223)
-        t = t + K[c];
+        tc = tc + K[c];
       }
     }
-    p.Ts[c][q] = t;
-    T net = t;
+    t[c] = tc;
+    T net = tc;
     if (hasS[c]) net += S[c];
     if constexpr (!H) {
       if (cls & kHasPole) net -= Ptot[c];
     }
     const T sc = region ? p.sig[c][ix3[c]] : T(0);
     if (hasW && sc != T(0)) {  // update_field_generic W cascade (Helpers.jl:333-339)
-      const T w = p.W[c][q];
-      const T wn = m * net;
-      p.W[c][q] = wn;
-      O[c] = (O[c] + (T(1) + sc) * wn) - (T(1) - sc) * w;
+      const T wo = w[c];
+      const T wn = m[c] * net;
+      w[c] = wn;
+      O[c] = (O[c] + (T(1) + sc) * wn) - (T(1) - sc) * wo;
     } else {
-      O[c] = m * net;
+      O[c] = m[c] * net;
     }
   }
 
   if constexpr (!H) {
     // χ3 Kerr correction (Dispersive.jl:127-147)
-    if (cls & kHasChi3) {
-      const T c3 = p.chi3[q];
-      if (c3 != T(0)) {
-        const T esq = (O[0] * O[0] + O[1] * O[1]) + O[2] * O[2];
-        const T corr = T(1) / (T(1) + c3 * esq);
-        O[0] = O[0] * corr;
-        O[1] = O[1] * corr;
-        O[2] = O[2] * corr;
-      }
+    if ((cls & kHasChi3) && c3 != T(0)) {
+      const T esq = (O[0] * O[0] + O[1] * O[1]) + O[2] * O[2];
+      const T corr = T(1) / (T(1) + c3 * esq);
+      O[0] = O[0] * corr;
+      O[1] = O[1] * corr;
+      O[2] = O[2] * corr;
     }
     // ADE poles with E^{n+1} (Dispersive.jl:25-88)
     if (cls & kHasPole) {
@@ -224,9 +232,8 @@ __device__ __forceinline__ void general_cell(const HalfStepParams<T>& p, long lo
 }
 
 // One fused half-step.  H = true: B/H from curl E; H = false: D/E from curl H.
-template <typename T, bool H>
+template <typename T, int VN, bool H>
 __global__ void __launch_bounds__(32 * kBlockY) half_step_kernel(const HalfStepParams<T> p) {
-  constexpr int VN = Vec<T>::N;
   constexpr int s = H ? 1 : -1;
   const int lane = threadIdx.x;
   const int j = blockIdx.y * kBlockY + threadIdx.y;
@@ -239,12 +246,23 @@ __global__ void __launch_bounds__(32 * kBlockY) half_step_kernel(const HalfStepP
   const long long row = p.origin + (long long)j * p.pitch + x0;
   const long long ystep = (long long)s * p.pitch;
   const long long zstep = (long long)s * p.plane;
-
   const bool fy = j < p.pml_lo[1] || j >= p.ny - p.pml_hi[1];
+  const bool pervox = p.m_inv[0] != nullptr;
+
+  // per-cell x flags of this thread's vector (static along the march)
+  bool fxv[VN];
+  bool anyfx = false;
+#pragma unroll
+  for (int v = 0; v < VN; ++v) {
+    const int i = x0 + v;
+    fxv[v] = i < p.nx && (i < p.pml_lo[0] || i >= p.nx - p.pml_hi[0]);
+    anyfx |= fxv[v];
+  }
+
   // rotated z-neighbour planes of A0, A1
   T r0[VN], r1[VN];
-#pragma unroll
-  for (int v = 0; v < VN; ++v) { r0[v] = T(0); r1[v] = T(0); }
+  vzero(r0);
+  vzero(r1);
   if (lane_ok) {
     const long long q0 = row + (long long)k0 * p.plane + (H ? 0 : -p.plane);
     vld(p.A[0] + q0, r0);
@@ -254,8 +272,8 @@ __global__ void __launch_bounds__(32 * kBlockY) half_step_kernel(const HalfStepP
   for (int k = k0; k < k1; ++k) {
     const long long q = row + (long long)k * p.plane;
     T l0[VN], l1[VN], a2[VN], y0[VN], y2[VN];
-#pragma unroll
-    for (int v = 0; v < VN; ++v) { l0[v] = l1[v] = a2[v] = y0[v] = y2[v] = T(0); }
+    vzero(l0); vzero(l1); vzero(a2); vzero(y0); vzero(y2);
+    T O[3][VN], m[3][VN];
     if (lane_ok) {
       if constexpr (H) {  // l = A(k+1)
         vld(p.A[0] + q + zstep, l0);
@@ -267,12 +285,24 @@ __global__ void __launch_bounds__(32 * kBlockY) half_step_kernel(const HalfStepP
       vld(p.A[2] + q, a2);
       vld(p.A[0] + q + ystep, y0);
       vld(p.A[2] + q + ystep, y2);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) vld(p.O[c] + q, O[c]);
+      if (pervox) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) vld(p.m_inv[c] + q, m[c]);
+      }
+    }
+    if (!pervox) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int v = 0; v < VN; ++v) m[c][v] = p.m_scalar;
     }
     // cur = A0/A1 at plane k, nb = at plane k+s
-    T* cur0 = H ? r0 : l0;
-    T* cur1 = H ? r1 : l1;
-    T* nb0 = H ? l0 : r0;
-    T* nb1 = H ? l1 : r1;
+    const T(&cur0)[VN] = H ? r0 : l0;
+    const T(&cur1)[VN] = H ? r1 : l1;
+    const T(&nb0)[VN] = H ? l0 : r0;
+    const T(&nb1)[VN] = H ? l1 : r1;
 
     // x neighbours of A1 and A2 at plane k
     T x1s[VN], x2s[VN];
@@ -301,58 +331,85 @@ __global__ void __launch_bounds__(32 * kBlockY) half_step_kernel(const HalfStepP
     }
 
     if (lane_ok) {
-      T O0[VN], O1[VN], O2[VN];
-      vld(p.O[0] + q, O0);
-      vld(p.O[1] + q, O1);
-      vld(p.O[2] + q, O2);
-      T m0[VN], m1[VN], m2[VN];
-      const bool pervox = p.m_inv[0] != nullptr;
-      if (pervox) {
-        vld(p.m_inv[0] + q, m0);
-        vld(p.m_inv[1] + q, m1);
-        vld(p.m_inv[2] + q, m2);
-      }
-      const bool fz = k < p.pml_lo[2] || k >= p.nz - p.pml_hi[2];
-      const bool yz = fy || fz;
-      uint32_t tf = 0;
-      if (p.tile_flag) tf = p.tile_flag[((long long)k * p.ny + j) * p.nxb + xb] & p.tile_bit;
+      T K[3][VN];
 #pragma unroll
       for (int v = 0; v < VN; ++v) {
-        const int i = x0 + v;
-        if (i >= p.nx) continue;
-        const T K0 = p.dt * (p.inv_d[2] * (nb1[v] - cur1[v]) - p.inv_d[1] * (y2[v] - a2[v]));
-        const T K1 = p.dt * (p.inv_d[0] * (x2s[v] - a2[v]) - p.inv_d[2] * (nb0[v] - cur0[v]));
-        const T K2 = p.dt * (p.inv_d[1] * (y0[v] - cur0[v]) - p.inv_d[0] * (x1s[v] - cur1[v]));
-        const bool fx = i < p.pml_lo[0] || i >= p.nx - p.pml_hi[0];
-        const uint32_t cls = tf ? p.cell_class[q + v] : 0u;
-        const bool special = cls & (H ? kSpecialH : kSpecialE);
-        if (!(fx || yz || special)) {
-          const T a = pervox ? m0[v] : p.m_scalar;
-          const T b = pervox ? m1[v] : p.m_scalar;
-          const T c = pervox ? m2[v] : p.m_scalar;
-          O0[v] = O0[v] + a * K0;
-          O1[v] = O1[v] + b * K1;
-          O2[v] = O2[v] + c * K2;
-        } else {
-          const T Kc[3] = {K0, K1, K2};
-          T Oc[3] = {O0[v], O1[v], O2[v]};
-          general_cell<T, H>(p, q + v, i, j, k, fx, fy, fz, cls, special, Kc, Oc);
-          O0[v] = Oc[0];
-          O1[v] = Oc[1];
-          O2[v] = Oc[2];
+        K[0][v] = p.dt * (p.inv_d[2] * (nb1[v] - cur1[v]) - p.inv_d[1] * (y2[v] - a2[v]));
+        K[1][v] = p.dt * (p.inv_d[0] * (x2s[v] - a2[v]) - p.inv_d[2] * (nb0[v] - cur0[v]));
+        K[2][v] = p.dt * (p.inv_d[1] * (y0[v] - cur0[v]) - p.inv_d[0] * (x1s[v] - cur1[v]));
+      }
+      const bool fz = k < p.pml_lo[2] || k >= p.nz - p.pml_hi[2];
+      const bool anyRegion = fy || fz || anyfx;
+      uint32_t cls[VN];
+      bool anySpecial = false;
+      const bool tf = p.tile_flag && (p.tile_flag[((long long)k * p.ny + j) * p.nxb + xb] & p.tile_bit);
+#pragma unroll
+      for (int v = 0; v < VN; ++v) {
+        cls[v] = (tf && x0 + v < p.nx) ? p.cell_class[q + v] : 0u;
+        anySpecial |= (cls[v] & (H ? kSpecialH : kSpecialE)) != 0;
+      }
+      if (!anyRegion && !anySpecial) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+          for (int v = 0; v < VN; ++v) O[c][v] = O[c][v] + m[c][v] * K[c][v];
+      } else {
+        // all auxiliaries this vector may touch, loaded before any arithmetic
+        const bool axis_any[3] = {anyfx, fy, fz};
+        T t[3][VN], u[3][VN], w[3][VN], c3[VN];
+        bool lt[3], lu[3], lw[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          lt[c] = p.Ts[c] != nullptr;
+          lu[c] = p.U[c] != nullptr && axis_any[(c + 1) % 3];
+          lw[c] = p.W[c] != nullptr && axis_any[c];
+          if (lt[c]) vld(p.Ts[c] + q, t[c]); else vzero(t[c]);
+          if (lu[c]) vld(p.U[c] + q, u[c]); else vzero(u[c]);
+          if (lw[c]) vld(p.W[c] + q, w[c]); else vzero(w[c]);
+        }
+        if (!H && anySpecial && p.chi3) vld(p.chi3 + q, c3); else vzero(c3);
+#pragma unroll
+        for (int v = 0; v < VN; ++v) {
+          const int i = x0 + v;
+          if (i >= p.nx) continue;
+          const bool special = (cls[v] & (H ? kSpecialH : kSpecialE)) != 0;
+          if (!(fxv[v] || fy || fz || special)) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) O[c][v] = O[c][v] + m[c][v] * K[c][v];
+            continue;
+          }
+          const T Kc[3] = {K[0][v], K[1][v], K[2][v]};
+          const T mc[3] = {m[0][v], m[1][v], m[2][v]};
+          T Oc[3] = {O[0][v], O[1][v], O[2][v]};
+          T tc[3] = {t[0][v], t[1][v], t[2][v]};
+          T uc[3] = {u[0][v], u[1][v], u[2][v]};
+          T wc[3] = {w[0][v], w[1][v], w[2][v]};
+          general_cell<T, H>(p, q + v, i, j, k, fxv[v], fy, fz, cls[v], special, Kc, mc, Oc, tc, uc, wc,
+                             c3[v]);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            O[c][v] = Oc[c];
+            t[c][v] = tc[c];
+            u[c][v] = uc[c];
+            w[c][v] = wc[c];
+          }
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          if (lt[c]) vst(p.Ts[c] + q, t[c]);
+          if (lu[c]) vst(p.U[c] + q, u[c]);
+          if (lw[c]) vst(p.W[c] + q, w[c]);
         }
       }
       if (x0 + VN <= p.nx) {
-        vst(p.O[0] + q, O0);
-        vst(p.O[1] + q, O1);
-        vst(p.O[2] + q, O2);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) vst(p.O[c] + q, O[c]);
       } else {
 #pragma unroll
         for (int v = 0; v < VN; ++v) {
           if (x0 + v < p.nx) {
-            p.O[0][q + v] = O0[v];
-            p.O[1][q + v] = O1[v];
-            p.O[2][q + v] = O2[v];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) p.O[c][q + v] = O[c][v];
           }
         }
       }
@@ -364,13 +421,23 @@ __global__ void __launch_bounds__(32 * kBlockY) half_step_kernel(const HalfStepP
   }
 }
 
-template <typename T>
-void launch_half_step(bool h_half, const HalfStepParams<T>& p, void* stream) {
+template <typename T, int VN>
+static void launch_vn(bool h_half, const HalfStepParams<T>& p, cudaStream_t st) {
   dim3 block(32, kBlockY, 1);
   dim3 grid(p.nxb, (p.ny + kBlockY - 1) / kBlockY, (p.nz + kPlanesPerCta - 1) / kPlanesPerCta);
+  if (h_half) half_step_kernel<T, VN, true><<<grid, block, 0, st>>>(p);
+  else half_step_kernel<T, VN, false><<<grid, block, 0, st>>>(p);
+}
+
+template <typename T>
+void launch_half_step(bool h_half, const HalfStepParams<T>& p, void* stream) {
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  if (h_half) half_step_kernel<T, true><<<grid, block, 0, st>>>(p);
-  else half_step_kernel<T, false><<<grid, block, 0, st>>>(p);
+  if constexpr (sizeof(T) == 4) {
+    if (p.vec == 4) launch_vn<T, 4>(h_half, p, st);
+    else launch_vn<T, 2>(h_half, p, st);
+  } else {
+    launch_vn<T, 2>(h_half, p, st);
+  }
 }
 
 // ---------------------------------------------------------------------------

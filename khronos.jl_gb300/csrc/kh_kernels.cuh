@@ -27,6 +27,7 @@ constexpr uint32_t kHasSrcE = 1u << 4;
 constexpr uint32_t kHasSrcH = 1u << 5;
 constexpr int kSlotShift = 8;            // source slot index in the upper 24 bits
 
+// Row alignment unit of the layout: 16 bytes of the run's type.
 template <typename T>
 struct Vec;
 template <>
@@ -57,7 +58,8 @@ template <typename T>
 struct HalfStepParams {
   int nx, ny, nz;
   long long pitch, plane, origin;
-  int nxb;  // x tiles of 32*VEC cells
+  int vec;  // cells per thread along x (VN): 4 or 2 for FP32, 2 for FP64
+  int nxb;  // x tiles of 32*vec cells
   T dt, inv_d[3];
 
   const T* A[3];  // curl source field (E for the H half, H for the E half)

@@ -12,6 +12,7 @@
 #include <cmath>
 #include <complex>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -77,7 +78,15 @@ class Sim : public SimBase {
     plane_ = pitch_ * (n_[1] + 2);
     origin_ = plane_ + pitch_ + VN;
     total_ = plane_ * (n_[2] + 2);
-    nxb_ = int((n_[0] + 32 * VN - 1) / (32 * VN));
+    // cells per thread along x: 2 (8-byte FP32 / 16-byte FP64 vectors).  With
+    // 2 cells a 320-cell row fills 5 warps exactly and the kernel holds fewer
+    // registers; KHRONOS_GB300_VEC=4 selects 16-byte FP32 vectors.
+    vec_ = 2;
+    if (sizeof(T) == 4) {
+      const char* ev = std::getenv("KHRONOS_GB300_VEC");
+      if (ev && std::atoi(ev) == 4) vec_ = 4;
+    }
+    nxb_ = int((n_[0] + 32 * vec_ - 1) / (32 * vec_));
     for (int a = 0; a < 3; ++a) {
       sigb_h_[a].assign(n_[a], T(0));
       sigd_h_[a].assign(n_[a], T(0));
@@ -233,8 +242,8 @@ class Sim : public SimBase {
     auto cidx = [&](int i, int j, int k) { return origin_ + (long long)k * plane_ + (long long)j * pitch_ + i; };
     auto mark = [&](int i, int j, int k, uint32_t bits) {
       cls[cidx(i, j, k)] |= bits;
-      tiles[(size_t(k) * n_[1] + j) * nxb_ + i / (32 * VN)] |= (bits & kh::kSpecialE) ? 1 : 0;
-      tiles[(size_t(k) * n_[1] + j) * nxb_ + i / (32 * VN)] |= (bits & kh::kSpecialH) ? 2 : 0;
+      tiles[(size_t(k) * n_[1] + j) * nxb_ + i / (32 * vec_)] |= (bits & kh::kSpecialE) ? 1 : 0;
+      tiles[(size_t(k) * n_[1] + j) * nxb_ + i / (32 * vec_)] |= (bits & kh::kSpecialH) ? 2 : 0;
     };
     const size_t ncenter = size_t(n_[0]) * n_[1] * n_[2];
     if (!chi3_h_.empty()) {
@@ -859,6 +868,7 @@ class Sim : public SimBase {
     p.plane = plane_;
     p.origin = origin_;
     p.nxb = nxb_;
+    p.vec = vec_;
     p.dt = dt_;
     for (int a = 0; a < 3; ++a) p.inv_d[a] = T(1) / delta_[a];
     for (int c = 0; c < 3; ++c) {
@@ -909,6 +919,7 @@ class Sim : public SimBase {
   T dt_, delta_[3];
   long long pitch_, plane_, origin_, total_;
   int nxb_;
+  int vec_;
   int lo_[3] = {0, 0, 0}, hi_[3] = {0, 0, 0};
   bool pml_axis_[3] = {false, false, false};
   uint32_t sigmask_b_ = 0, sigmask_d_ = 0;
