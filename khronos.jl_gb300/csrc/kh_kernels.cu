@@ -74,28 +74,18 @@ __device__ __forceinline__ void vzero(T (&v)[VN]) {
   for (int q = 0; q < VN; ++q) v[q] = T(0);
 }
 
-// update_field_from_curl (Helpers.jl:30-33)
-template <typename T>
-__device__ __forceinline__ T ufc_old(T A, T B, T Bold, T s) {
-  return (((T(1) - s) * A + B) - Bold) / (T(1) + s);
-}
-template <typename T>
-__device__ __forceinline__ T ufc(T A, T B, T s) {
-  return ((T(1) - s) * A + B) / (T(1) + s);
-}
-
-// Update of one cell that sits in a CPML region or carries a source, χ3 or a
-// pole.  t/u/w are the cell's B|D state and CPML U/W values (loaded and stored
-// by the caller), m its μ⁻¹|ε⁻¹, c3 its χ3.  Conductivity (C, σ) and pole
-// arrays are rare and read here directly.
+// Update of one cell that carries a source, χ3, a pole or a material
+// conductivity (and may also sit in a CPML region).  t/u/w are the cell's B|D
+// state and CPML U/W values (loaded and stored by the caller), m its μ⁻¹|ε⁻¹,
+// a[] its CPML coefficients along x, y, z, c3 its χ3.  Conductivity (C, σ)
+// and pole arrays are rare and read here directly.
 template <typename T, bool H>
 __device__ __forceinline__ void general_cell(const HalfStepParams<T>& p, long long q, int i, int j,
-                                             int k, bool fx, bool fy, bool fz, uint32_t cls,
-                                             bool special, const T (&K)[3], const T (&m)[3],
-                                             T (&O)[3], T (&t)[3], T (&u)[3], T (&w)[3], T c3) {
-  const bool f[3] = {fx, fy, fz};
-  const int ix3[3] = {i, j, k};
-  const bool region = fx || fy || fz;
+                                             int k, const bool (&f)[3], const AxisCoef<T> (&a)[3],
+                                             uint32_t cls, bool special, const T (&K)[3],
+                                             const T (&m)[3], T (&O)[3], T (&t)[3], T (&u)[3],
+                                             T (&w)[3], T c3) {
+  const bool region = f[0] || f[1] || f[2];
   bool regC = false;
   if (region && p.sigma_region_mask) {
     const int rx = i < p.pml_lo[0] ? 0 : (i >= p.nx - p.pml_hi[0] ? 2 : 1);
@@ -105,33 +95,42 @@ __device__ __forceinline__ void general_cell(const HalfStepParams<T>& p, long lo
   }
 
   // Source term S of this half-step (update_source!, Sources.jl:346-357).
-  T S[3] = {T(0), T(0), T(0)};
-  bool hasS[3] = {false, false, false};
+  T S0 = T(0), S1 = T(0), S2 = T(0);
+  bool h0 = false, h1 = false, h2 = false;
   if (p.sources_active && (cls & (H ? kHasSrcH : kHasSrcE))) {
     const int slot = int(cls >> kSlotShift);
     const int e1 = p.slot_off[slot + 1];
     for (int e = p.slot_off[slot]; e < e1; ++e) {
       const int c = p.ent_comp[e] - (H ? 3 : 0);  // entries carry components 0..5
-      if (c < 0 || c > 2) continue;
-      const Cplx<T> a = p.ent_amp[e];
+      const Cplx<T> am = p.ent_amp[e];
       const Cplx<T> fv = p.f_now[p.ent_src[e]];
-      S[c] += fv.re * a.re - fv.im * a.im;  // real(f(t) · amplitude)
-      hasS[c] = true;
+      const T v = fv.re * am.re - fv.im * am.im;  // real(f(t) · amplitude)
+      if (c == 0) { S0 += v; h0 = true; }
+      else if (c == 1) { S1 += v; h1 = true; }
+      else if (c == 2) { S2 += v; h2 = true; }
     }
   }
+  const T S[3] = {S0, S1, S2};
+  const bool hasS[3] = {h0, h1, h2};
 
   // Total polarisation Σ_p P_p (accumulate_polarization_kernel!, Dispersive.jl:95-104).
   T Ptot[3] = {T(0), T(0), T(0)};
   if constexpr (!H) {
     if (cls & kHasPole) {
-      for (int pp = 0; pp < p.npoles; ++pp)
-        for (int c = 0; c < 3; ++c) Ptot[c] += p.poles[pp].P[c][q];
+      for (int pp = 0; pp < p.npoles; ++pp) {
+        Ptot[0] += p.poles[pp].P[0][q];
+        Ptot[1] += p.poles[pp].P[1][q];
+        Ptot[2] += p.poles[pp].P[2][q];
+      }
     }
   }
 
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     const int nx_ = (c + 1) % 3, pv = (c + 2) % 3;
+    const AxisCoef<T>& an = a[nx_];
+    const AxisCoef<T>& ap = a[pv];
+    const AxisCoef<T>& ao = a[c];
     const bool hasU = region && f[nx_];
     const bool hasW = region && f[c];
     const bool hasC = regC && (f[nx_] || f[pv]);
@@ -146,41 +145,37 @@ __device__ __forceinline__ void general_cell(const HalfStepParams<T>& p, long lo
       tc = tc + K[c];  // step_curl_and_update! (ReferenceKernels.jl:340-345)
     } else if (p.cpml) {
       // _cuda_pml_BH_kernel!/_cuda_pml_DE_kernel! stages (CUDAKernels.jl:150-281)
-      const T sn = p.sig[nx_][ix3[nx_]];
-      const T sp = p.sig[pv][ix3[pv]];
       T in_t = K[c];
-      if (f[nx_] && sn != T(0)) {
-        const T un = ufc(u[c], K[c], sn);
+      if (f[nx_] && an.s != T(0)) {
+        const T un = (an.om * u[c] + K[c]) * an.ir;
         in_t = un - u[c];
         u[c] = un;
       }
-      tc = (f[pv] && sp != T(0)) ? ((T(1) - sp) * tc + in_t) / (T(1) + sp) : tc + in_t;
+      tc = (f[pv] && ap.s != T(0)) ? (ap.om * tc + in_t) * ap.ir : tc + in_t;
     } else {
-      const T sn = p.sig[nx_][ix3[nx_]];
-      const T sp = p.sig[pv][ix3[pv]];
       if (hasC && hasU) {
         const T sD = hasSD ? T(0.5) * (p.dt * p.msig[c][q]) : T(0);
         const T uo = u[c];
         if (hasSD && sD != T(0)) {  // three-stage cascade (Helpers.jl:60-67)
           const T cc = p.C[c][q];
-          const T cn = ufc(cc, K[c], sD);
+          const T cn = ((T(1) - sD) * cc + K[c]) / (T(1) + sD);
           p.C[c][q] = cn;
-          u[c] = ufc_old(uo, cn, cc, sn);
+          u[c] = ((an.om * uo + cn) - cc) * an.ir;
         } else {  // two-stage cascade (Helpers.jl:53-59, 72-78)
-          u[c] = ufc(uo, K[c], sn);
+          u[c] = (an.om * uo + K[c]) * an.ir;
         }
-        tc = ufc_old(tc, u[c], uo, sp);
+        tc = ((ap.om * tc + u[c]) - uo) * ap.ir;
       } else if (hasU) {  // C absent (Helpers.jl:113-139)
-        if (sn == T(0)) {
-          tc = ufc(tc, K[c], sp);
+        if (an.s == T(0)) {
+          tc = (ap.om * tc + K[c]) * ap.ir;
         } else {
           const T uo = u[c];
-          u[c] = ufc(uo, K[c], sn);
-          tc = ufc_old(tc, u[c], uo, sp);
+          u[c] = (an.om * uo + K[c]) * an.ir;
+          tc = ((ap.om * tc + u[c]) - uo) * ap.ir;
         }
       } else if (hasSD) {  // C and U absent, conductivity present (Helpers.jl:225-240)
         const T sD = T(0.5) * (p.dt * p.msig[c][q]);
-        tc = ufc(tc, K[c], sD);
+        tc = ((T(1) - sD) * tc + K[c]) / (T(1) + sD);
       } else {  // C and U absent: σ_prev dropped (Helpers.jl:208-223)
         tc = tc + K[c];
       }
@@ -191,12 +186,11 @@ __device__ __forceinline__ void general_cell(const HalfStepParams<T>& p, long lo
     if constexpr (!H) {
       if (cls & kHasPole) net -= Ptot[c];
     }
-    const T sc = region ? p.sig[c][ix3[c]] : T(0);
-    if (hasW && sc != T(0)) {  // update_field_generic W cascade (Helpers.jl:333-339)
+    if (hasW && ao.s != T(0)) {  // update_field_generic W cascade (Helpers.jl:333-339)
       const T wo = w[c];
       const T wn = m[c] * net;
       w[c] = wn;
-      O[c] = (O[c] + (T(1) + sc) * wn) - (T(1) - sc) * wo;
+      O[c] = (O[c] + ao.op * wn) - ao.om * wo;
     } else {
       O[c] = m[c] * net;
     }
@@ -217,6 +211,7 @@ __device__ __forceinline__ void general_cell(const HalfStepParams<T>& p, long lo
         const PoleParams<T>& P = p.poles[pp];
         const T s = P.sigma[q];
         if (s == T(0)) continue;
+#pragma unroll
         for (int c = 0; c < 3; ++c) {
           const T px = P.P[c][q];
           const T pprev = P.Pprev[c][q];
@@ -231,8 +226,56 @@ __device__ __forceinline__ void general_cell(const HalfStepParams<T>& p, long lo
   }
 }
 
+// Update of a CPML-region cell without sources, χ3, poles or conductivity:
+// the common case of the absorbing shell, with the stage logic fixed at
+// compile time (CPML: CUDA-path stages; otherwise the CPU-path dispatch).
+template <typename T, bool CPML>
+__device__ __forceinline__ void pml_cell(const bool (&f)[3], const AxisCoef<T> (&a)[3], const T (&K)[3],
+                                         const T (&m)[3], T (&O)[3], T (&t)[3], T (&u)[3], T (&w)[3]) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const int nx_ = (c + 1) % 3, pv = (c + 2) % 3;
+    const AxisCoef<T>& an = a[nx_];
+    const AxisCoef<T>& ap = a[pv];
+    const AxisCoef<T>& ao = a[c];
+    if constexpr (CPML) {
+      T in_t = K[c];
+      if (f[nx_] && an.s != T(0)) {
+        const T un = (an.om * u[c] + K[c]) * an.ir;
+        in_t = un - u[c];
+        u[c] = un;
+      }
+      t[c] = (f[pv] && ap.s != T(0)) ? (ap.om * t[c] + in_t) * ap.ir : t[c] + in_t;
+    } else {
+      if (!(f[nx_] || f[c])) {  // no auxiliary in this chunk: plain update
+        O[c] = O[c] + m[c] * K[c];
+        continue;
+      }
+      if (f[nx_]) {
+        if (an.s == T(0)) {
+          t[c] = (ap.om * t[c] + K[c]) * ap.ir;
+        } else {
+          const T un = (an.om * u[c] + K[c]) * an.ir;
+          t[c] = ((ap.om * t[c] + un) - u[c]) * ap.ir;
+          u[c] = un;
+        }
+      } else {
+        t[c] = t[c] + K[c];  // σ_prev dropped (Helpers.jl:208-223)
+      }
+    }
+    const T net = t[c];
+    if (f[c] && ao.s != T(0)) {
+      const T wn = m[c] * net;
+      O[c] = (O[c] + ao.op * wn) - ao.om * w[c];
+      w[c] = wn;
+    } else {
+      O[c] = m[c] * net;
+    }
+  }
+}
+
 // One fused half-step.  H = true: B/H from curl E; H = false: D/E from curl H.
-template <typename T, int VN, bool H>
+template <typename T, int VN, bool H, bool CPML>
 __global__ void __launch_bounds__(32 * kBlockY) half_step_kernel(const HalfStepParams<T> p) {
   constexpr int s = H ? 1 : -1;
   const int lane = threadIdx.x;
@@ -248,16 +291,21 @@ __global__ void __launch_bounds__(32 * kBlockY) half_step_kernel(const HalfStepP
   const long long zstep = (long long)s * p.plane;
   const bool fy = j < p.pml_lo[1] || j >= p.ny - p.pml_hi[1];
   const bool pervox = p.m_inv[0] != nullptr;
+  const bool has_msig = p.msig[0] || p.msig[1] || p.msig[2];
 
-  // per-cell x flags of this thread's vector (static along the march)
+  // per-cell x flags and CPML coefficients of this thread's vector and the
+  // row's y coefficients: static along the z march
   bool fxv[VN];
+  AxisCoef<T> axv[VN];
   bool anyfx = false;
 #pragma unroll
   for (int v = 0; v < VN; ++v) {
     const int i = x0 + v;
     fxv[v] = i < p.nx && (i < p.pml_lo[0] || i >= p.nx - p.pml_hi[0]);
     anyfx |= fxv[v];
+    axv[v] = i < p.nx ? p.ax[0][i] : AxisCoef<T>{T(0), T(1), T(1), T(1)};
   }
+  const AxisCoef<T> ay = p.ax[1][j];
 
   // rotated z-neighbour planes of A0, A1
   T r0[VN], r1[VN];
@@ -368,6 +416,8 @@ __global__ void __launch_bounds__(32 * kBlockY) half_step_kernel(const HalfStepP
           if (lw[c]) vld(p.W[c] + q, w[c]); else vzero(w[c]);
         }
         if (!H && anySpecial && p.chi3) vld(p.chi3 + q, c3); else vzero(c3);
+        const AxisCoef<T> az = p.ax[2][k];
+        const bool heavy = anySpecial || has_msig;
 #pragma unroll
         for (int v = 0; v < VN; ++v) {
           const int i = x0 + v;
@@ -378,14 +428,19 @@ __global__ void __launch_bounds__(32 * kBlockY) half_step_kernel(const HalfStepP
             for (int c = 0; c < 3; ++c) O[c][v] = O[c][v] + m[c][v] * K[c][v];
             continue;
           }
+          const bool fc[3] = {fxv[v], fy, fz};
+          const AxisCoef<T> ac[3] = {axv[v], ay, az};
           const T Kc[3] = {K[0][v], K[1][v], K[2][v]};
           const T mc[3] = {m[0][v], m[1][v], m[2][v]};
           T Oc[3] = {O[0][v], O[1][v], O[2][v]};
           T tc[3] = {t[0][v], t[1][v], t[2][v]};
           T uc[3] = {u[0][v], u[1][v], u[2][v]};
           T wc[3] = {w[0][v], w[1][v], w[2][v]};
-          general_cell<T, H>(p, q + v, i, j, k, fxv[v], fy, fz, cls[v], special, Kc, mc, Oc, tc, uc, wc,
-                             c3[v]);
+          if (heavy) {
+            general_cell<T, H>(p, q + v, i, j, k, fc, ac, cls[v], special, Kc, mc, Oc, tc, uc, wc, c3[v]);
+          } else {
+            pml_cell<T, CPML>(fc, ac, Kc, mc, Oc, tc, uc, wc);
+          }
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
             O[c][v] = Oc[c];
@@ -421,22 +476,28 @@ __global__ void __launch_bounds__(32 * kBlockY) half_step_kernel(const HalfStepP
   }
 }
 
-template <typename T, int VN>
+template <typename T, int VN, bool CPML>
 static void launch_vn(bool h_half, const HalfStepParams<T>& p, cudaStream_t st) {
   dim3 block(32, kBlockY, 1);
   dim3 grid(p.nxb, (p.ny + kBlockY - 1) / kBlockY, (p.nz + kPlanesPerCta - 1) / kPlanesPerCta);
-  if (h_half) half_step_kernel<T, VN, true><<<grid, block, 0, st>>>(p);
-  else half_step_kernel<T, VN, false><<<grid, block, 0, st>>>(p);
+  if (h_half) half_step_kernel<T, VN, true, CPML><<<grid, block, 0, st>>>(p);
+  else half_step_kernel<T, VN, false, CPML><<<grid, block, 0, st>>>(p);
+}
+
+template <typename T, int VN>
+static void launch_sem(bool h_half, const HalfStepParams<T>& p, cudaStream_t st) {
+  if (p.cpml) launch_vn<T, VN, true>(h_half, p, st);
+  else launch_vn<T, VN, false>(h_half, p, st);
 }
 
 template <typename T>
 void launch_half_step(bool h_half, const HalfStepParams<T>& p, void* stream) {
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if constexpr (sizeof(T) == 4) {
-    if (p.vec == 4) launch_vn<T, 4>(h_half, p, st);
-    else launch_vn<T, 2>(h_half, p, st);
+    if (p.vec == 4) launch_sem<T, 4>(h_half, p, st);
+    else launch_sem<T, 2>(h_half, p, st);
   } else {
-    launch_vn<T, 2>(h_half, p, st);
+    launch_sem<T, 2>(h_half, p, st);
   }
 }
 

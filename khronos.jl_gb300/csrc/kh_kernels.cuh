@@ -53,6 +53,17 @@ struct Cplx {
   T re, im;
 };
 
+// CPML coefficients of one cell along one axis: the σ sample and the factors
+// of update_field_from_curl ((1-σ)·A + B)/(1+σ) (Helpers.jl:30-33) with the
+// division replaced by a multiplication with 1/(1+σ).
+template <typename T>
+struct AxisCoef {
+  T s;    // σ (already scaled by Δt/2)
+  T om;   // 1 - σ
+  T ir;   // 1 / (1 + σ)
+  T op;   // 1 + σ
+};
+
 // Parameters of one fused half-step launch.
 template <typename T>
 struct HalfStepParams {
@@ -71,7 +82,7 @@ struct HalfStepParams {
   const T* m_inv[3];  // per-voxel μ⁻¹ / ε⁻¹ or nullptr
   T m_scalar;
   const T* msig[3];   // material conductivity σB / σD or nullptr
-  const T* sig[3];    // PML σ per axis at cell centres (length n_a, zeros outside PML)
+  const AxisCoef<T>* ax[3];  // CPML coefficients per axis at cell centres (length n_a)
   int pml_lo[3], pml_hi[3];
   int cpml;                    // 1: CUDA-path CPML stages, 0: CPU-path dispatch
   uint32_t sigma_region_mask;  // bit r (r = rx + 3 ry + 9 rz) set: region has conductivity

@@ -338,8 +338,16 @@ class Sim : public SimBase {
       poles_d_.push_back(pd);
     }
     for (int a = 0; a < 3; ++a) {
-      KH_TRY(upload_raw(sigb_h_[a].data(), sigb_h_[a].size() * sizeof(T), (void**)&sigb_[a]));
-      KH_TRY(upload_raw(sigd_h_[a].data(), sigd_h_[a].size() * sizeof(T), (void**)&sigd_[a]));
+      // CPML coefficient tables (σ, 1-σ, 1/(1+σ), 1+σ) in the run's precision
+      for (int h = 0; h < 2; ++h) {
+        const std::vector<T>& sg = h ? sigb_h_[a] : sigd_h_[a];
+        std::vector<kh::AxisCoef<T>> tab(sg.size());
+        for (size_t i = 0; i < sg.size(); ++i) {
+          const T sv = sg[i];
+          tab[i] = {sv, T(1) - sv, T(1) / (T(1) + sv), T(1) + sv};
+        }
+        KH_TRY(upload_raw(tab.data(), tab.size() * sizeof(kh::AxisCoef<T>), (void**)(h ? &axb_[a] : &axd_[a])));
+      }
     }
     if (anySpecialE || anySpecialH) {
       KH_TRY(upload_raw(cls.data(), cls.size() * sizeof(uint32_t), (void**)&cls_));
@@ -880,7 +888,7 @@ class Sim : public SimBase {
       p.C[c] = h ? CB_[c] : CD_[c];
       p.m_inv[c] = h ? mu_[c] : eps_[c];
       p.msig[c] = h ? msigb_[c] : msigd_[c];
-      p.sig[c] = h ? sigb_[c] : sigd_[c];
+      p.ax[c] = h ? axb_[c] : axd_[c];
       p.pml_lo[c] = lo_[c];
       p.pml_hi[c] = hi_[c];
     }
@@ -938,7 +946,7 @@ class Sim : public SimBase {
   T *E_[3] = {}, *H_[3] = {}, *B_[3] = {}, *D_[3] = {};
   T *UB_[3] = {}, *UD_[3] = {}, *WB_[3] = {}, *WD_[3] = {}, *CB_[3] = {}, *CD_[3] = {};
   T *eps_[3] = {}, *mu_[3] = {}, *msigd_[3] = {}, *msigb_[3] = {}, *chi3_ = nullptr;
-  T *sigb_[3] = {}, *sigd_[3] = {};
+  kh::AxisCoef<T> *axb_[3] = {}, *axd_[3] = {};
   uint32_t* cls_ = nullptr;
   uint8_t* tiles_ = nullptr;
   int *slot_off_ = nullptr, *ent_src_ = nullptr, *ent_comp_ = nullptr;
