@@ -33,10 +33,6 @@ namespace kh {
 template <typename T, int VN>
 struct VT;
 template <>
-struct VT<float, 4> {
-  using V = float4;
-};
-template <>
 struct VT<float, 2> {
   using V = float2;
 };
@@ -275,8 +271,11 @@ __device__ __forceinline__ void pml_cell(const bool (&f)[3], const AxisCoef<T> (
 }
 
 // One fused half-step.  H = true: B/H from curl E; H = false: D/E from curl H.
-template <typename T, int VN, bool H, bool CPML>
-__global__ void __launch_bounds__(32 * kBlockY) half_step_kernel(const HalfStepParams<T> p) {
+// FULL = false (LEAN) compiles only plain and CPML cells; cells marked special
+// there are source cells, updated as B|D-keeping cells (O = m⁻¹·T) and given
+// their source term by source_fix_kernel when sources are active.
+template <typename T, int VN, bool H, bool CPML, bool FULL>
+__global__ void __launch_bounds__(32 * kBlockY, kMinBlocks) half_step_kernel(const HalfStepParams<T> p) {
   constexpr int s = H ? 1 : -1;
   const int lane = threadIdx.x;
   const int j = blockIdx.y * kBlockY + threadIdx.y;
@@ -291,7 +290,6 @@ __global__ void __launch_bounds__(32 * kBlockY) half_step_kernel(const HalfStepP
   const long long zstep = (long long)s * p.plane;
   const bool fy = j < p.pml_lo[1] || j >= p.ny - p.pml_hi[1];
   const bool pervox = p.m_inv[0] != nullptr;
-  const bool has_msig = p.msig[0] || p.msig[1] || p.msig[2];
 
   // per-cell x flags and CPML coefficients of this thread's vector and the
   // row's y coefficients: static along the z march
@@ -415,9 +413,8 @@ __global__ void __launch_bounds__(32 * kBlockY) half_step_kernel(const HalfStepP
           if (lu[c]) vld(p.U[c] + q, u[c]); else vzero(u[c]);
           if (lw[c]) vld(p.W[c] + q, w[c]); else vzero(w[c]);
         }
-        if (!H && anySpecial && p.chi3) vld(p.chi3 + q, c3); else vzero(c3);
+        if (FULL && !H && anySpecial && p.chi3) vld(p.chi3 + q, c3); else vzero(c3);
         const AxisCoef<T> az = p.ax[2][k];
-        const bool heavy = anySpecial || has_msig;
 #pragma unroll
         for (int v = 0; v < VN; ++v) {
           const int i = x0 + v;
@@ -436,10 +433,18 @@ __global__ void __launch_bounds__(32 * kBlockY) half_step_kernel(const HalfStepP
           T tc[3] = {t[0][v], t[1][v], t[2][v]};
           T uc[3] = {u[0][v], u[1][v], u[2][v]};
           T wc[3] = {w[0][v], w[1][v], w[2][v]};
-          if (heavy) {
+          if constexpr (FULL) {
             general_cell<T, H>(p, q + v, i, j, k, fc, ac, cls[v], special, Kc, mc, Oc, tc, uc, wc, c3[v]);
           } else {
-            pml_cell<T, CPML>(fc, ac, Kc, mc, Oc, tc, uc, wc);
+            if (fc[0] || fc[1] || fc[2]) {
+              pml_cell<T, CPML>(fc, ac, Kc, mc, Oc, tc, uc, wc);
+            } else {  // source cell outside CPML: keeps its B|D state
+#pragma unroll
+              for (int c = 0; c < 3; ++c) {
+                tc[c] = tc[c] + Kc[c];
+                Oc[c] = mc[c] * tc[c];
+              }
+            }
           }
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
@@ -476,29 +481,62 @@ __global__ void __launch_bounds__(32 * kBlockY) half_step_kernel(const HalfStepP
   }
 }
 
-template <typename T, int VN, bool CPML>
-static void launch_vn(bool h_half, const HalfStepParams<T>& p, cudaStream_t st) {
+template <typename T, bool CPML, bool FULL>
+static void launch_variant(bool h_half, const HalfStepParams<T>& p, cudaStream_t st) {
   dim3 block(32, kBlockY, 1);
   dim3 grid(p.nxb, (p.ny + kBlockY - 1) / kBlockY, (p.nz + kPlanesPerCta - 1) / kPlanesPerCta);
-  if (h_half) half_step_kernel<T, VN, true, CPML><<<grid, block, 0, st>>>(p);
-  else half_step_kernel<T, VN, false, CPML><<<grid, block, 0, st>>>(p);
-}
-
-template <typename T, int VN>
-static void launch_sem(bool h_half, const HalfStepParams<T>& p, cudaStream_t st) {
-  if (p.cpml) launch_vn<T, VN, true>(h_half, p, st);
-  else launch_vn<T, VN, false>(h_half, p, st);
+  if (h_half) half_step_kernel<T, kVN, true, CPML, FULL><<<grid, block, 0, st>>>(p);
+  else half_step_kernel<T, kVN, false, CPML, FULL><<<grid, block, 0, st>>>(p);
 }
 
 template <typename T>
 void launch_half_step(bool h_half, const HalfStepParams<T>& p, void* stream) {
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  if constexpr (sizeof(T) == 4) {
-    if (p.vec == 4) launch_sem<T, 4>(h_half, p, st);
-    else launch_sem<T, 2>(h_half, p, st);
+  if (p.cpml) {
+    if (p.full) launch_variant<T, true, true>(h_half, p, st);
+    else launch_variant<T, true, false>(h_half, p, st);
   } else {
-    launch_sem<T, 2>(h_half, p, st);
+    if (p.full) launch_variant<T, false, true>(h_half, p, st);
+    else launch_variant<T, false, false>(h_half, p, st);
   }
+}
+
+// Source term of the cells a LEAN half-step updated as B|D-keeping cells:
+// O = m⁻¹·(T + S), the same arithmetic update_field_generic performs
+// (net = T; net += S; A = m⁻¹·net, Helpers.jl:329-347).
+template <typename T>
+__global__ void source_fix_kernel(const SourceFixParams<T> p) {
+  const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= p.nslots) return;
+  const long long q = p.slot_cell[slot];
+  const int base = p.h_half ? 3 : 0;
+  T S[3] = {T(0), T(0), T(0)};
+  bool has[3] = {false, false, false};
+  for (int e = p.slot_off[slot]; e < p.slot_off[slot + 1]; ++e) {
+    const int c = p.ent_comp[e] - base;
+    if (c < 0 || c > 2) continue;
+    const Cplx<T> a = p.ent_amp[e];
+    const Cplx<T> f = p.f_now[p.ent_src[e]];
+    const T v = f.re * a.re - f.im * a.im;
+    if (c == 0) { S[0] += v; has[0] = true; }
+    else if (c == 1) { S[1] += v; has[1] = true; }
+    else { S[2] += v; has[2] = true; }
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    if (!has[c]) continue;
+    const T m = p.m_inv[c] ? p.m_inv[c][q] : p.m_scalar;
+    T net = p.Ts[c][q];
+    net += S[c];
+    p.O[c][q] = m * net;
+  }
+}
+
+template <typename T>
+void launch_source_fix(const SourceFixParams<T>& p, void* stream) {
+  if (p.nslots <= 0) return;
+  const int threads = 128;
+  source_fix_kernel<T><<<(p.nslots + threads - 1) / threads, threads, 0, static_cast<cudaStream_t>(stream)>>>(p);
 }
 
 // ---------------------------------------------------------------------------
@@ -649,6 +687,8 @@ void launch_flux(const Cplx<T>* e1, const Cplx<T>* e2, const Cplx<T>* h1, const 
 
 template void launch_half_step<float>(bool, const HalfStepParams<float>&, void*);
 template void launch_half_step<double>(bool, const HalfStepParams<double>&, void*);
+template void launch_source_fix<float>(const SourceFixParams<float>&, void*);
+template void launch_source_fix<double>(const SourceFixParams<double>&, void*);
 template void launch_dft<float>(const DftParams<float>&, void*);
 template void launch_dft<double>(const DftParams<double>&, void*);
 template void launch_flux<float>(const Cplx<float>*, const Cplx<float>*, const Cplx<float>*,

@@ -17,6 +17,12 @@ namespace kh {
 constexpr int kMaxPoles = 4;
 constexpr int kBlockY = 4;      // rows per CTA
 constexpr int kPlanesPerCta = 16;
+// Resident CTAs per SM the half-step kernels are compiled for (caps registers
+// at 65536 / (kMinBlocks · 32 · kBlockY)).
+#ifndef KH_MIN_BLOCKS
+#define KH_MIN_BLOCKS 4
+#endif
+constexpr int kMinBlocks = KH_MIN_BLOCKS;
 
 // cell_class bits (full-domain uint32 array, read only inside flagged tiles)
 constexpr uint32_t kSpecialE = 1u << 0;  // D-state kept: E source, χ3 or pole
@@ -69,8 +75,8 @@ template <typename T>
 struct HalfStepParams {
   int nx, ny, nz;
   long long pitch, plane, origin;
-  int vec;  // cells per thread along x (VN): 4 or 2 for FP32, 2 for FP64
-  int nxb;  // x tiles of 32*vec cells
+  int nxb;  // x tiles of 32*VN cells
+  int full; // 1: cells with sources/χ3/poles/conductivity handled in-kernel (FULL variant)
   T dt, inv_d[3];
 
   const T* A[3];  // curl source field (E for the H half, H for the E half)
@@ -116,8 +122,35 @@ struct DftParams {
   Cplx<T>* comp;         // Kahan compensation (FP32) or nullptr
 };
 
+// Cells per thread along x in the half-step kernels (8-byte FP32 / 16-byte
+// FP64 vectors; a 320-cell row is 5 full warps).
+constexpr int kVN = 2;
+
+// Sparse source application for cells the LEAN kernel updated as B|D-keeping
+// cells: O = m⁻¹·(T + S) with S = Σ real(f(t)·amplitude) (Helpers.jl:329-332,
+// Sources.jl:346-357).  Exact when the cell has no W stage for the component
+// and no χ3/pole, which the host checks before choosing this path.
+template <typename T>
+struct SourceFixParams {
+  int nslots;
+  const long long* slot_cell;  // cell offset of each slot
+  const int* slot_off;
+  const int* ent_src;
+  const int* ent_comp;         // 0..5
+  const Cplx<T>* ent_amp;
+  const Cplx<T>* f_now;
+  T* O[3];
+  const T* Ts[3];
+  const T* m_inv[3];
+  T m_scalar;
+  int h_half;
+};
+
 template <typename T>
 void launch_half_step(bool h_half, const HalfStepParams<T>& p, void* stream);
+
+template <typename T>
+void launch_source_fix(const SourceFixParams<T>& p, void* stream);
 
 template <typename T>
 void launch_dft(const DftParams<T>& p, void* stream);

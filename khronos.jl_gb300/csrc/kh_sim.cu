@@ -78,15 +78,7 @@ class Sim : public SimBase {
     plane_ = pitch_ * (n_[1] + 2);
     origin_ = plane_ + pitch_ + VN;
     total_ = plane_ * (n_[2] + 2);
-    // cells per thread along x: 2 (8-byte FP32 / 16-byte FP64 vectors).  With
-    // 2 cells a 320-cell row fills 5 warps exactly and the kernel holds fewer
-    // registers; KHRONOS_GB300_VEC=4 selects 16-byte FP32 vectors.
-    vec_ = 2;
-    if (sizeof(T) == 4) {
-      const char* ev = std::getenv("KHRONOS_GB300_VEC");
-      if (ev && std::atoi(ev) == 4) vec_ = 4;
-    }
-    nxb_ = int((n_[0] + 32 * vec_ - 1) / (32 * vec_));
+    nxb_ = int((n_[0] + 32 * kh::kVN - 1) / (32 * kh::kVN));
     for (int a = 0; a < 3; ++a) {
       sigb_h_[a].assign(n_[a], T(0));
       sigd_h_[a].assign(n_[a], T(0));
@@ -242,8 +234,8 @@ class Sim : public SimBase {
     auto cidx = [&](int i, int j, int k) { return origin_ + (long long)k * plane_ + (long long)j * pitch_ + i; };
     auto mark = [&](int i, int j, int k, uint32_t bits) {
       cls[cidx(i, j, k)] |= bits;
-      tiles[(size_t(k) * n_[1] + j) * nxb_ + i / (32 * vec_)] |= (bits & kh::kSpecialE) ? 1 : 0;
-      tiles[(size_t(k) * n_[1] + j) * nxb_ + i / (32 * vec_)] |= (bits & kh::kSpecialH) ? 2 : 0;
+      tiles[(size_t(k) * n_[1] + j) * nxb_ + i / (32 * kh::kVN)] |= (bits & kh::kSpecialE) ? 1 : 0;
+      tiles[(size_t(k) * n_[1] + j) * nxb_ + i / (32 * kh::kVN)] |= (bits & kh::kSpecialH) ? 2 : 0;
     };
     const size_t ncenter = size_t(n_[0]) * n_[1] * n_[2];
     if (!chi3_h_.empty()) {
@@ -263,7 +255,7 @@ class Sim : public SimBase {
         }
     // Sparse source table: entries per cell in injection order
     // (components Ex..Hz, then sources in order; Kernels.jl:455-463, Sources.jl:330-340).
-    struct Ent { long long cell; int src, comp; std::complex<double> amp; };
+    struct Ent { long long cell; int src, comp; std::complex<double> amp; int i, j, k; };
     std::vector<Ent> ents;
     for (int comp = 0; comp < 6; ++comp)
       for (size_t si = 0; si < srcs_.size(); ++si) {
@@ -278,13 +270,14 @@ class Sim : public SimBase {
               const std::complex<double> a = s.amp[(size_t(k) * s.d.dims[1] + j) * s.d.dims[0] + i];
               const std::complex<T> aT(T(a.real()), T(a.imag()));
               if (aT.real() == T(0) && aT.imag() == T(0)) continue;
-              ents.push_back({cidx(gi, gj, gk), int(si), comp, std::complex<double>(aT.real(), aT.imag())});
+              ents.push_back({cidx(gi, gj, gk), int(si), comp, std::complex<double>(aT.real(), aT.imag()), gi, gj, gk});
               mark(gi, gj, gk, comp < 3 ? (kh::kSpecialE | kh::kHasSrcE) : (kh::kSpecialH | kh::kHasSrcH));
               if (comp < 3) anySpecialE = true; else anySpecialH = true;
             }
       }
     std::stable_sort(ents.begin(), ents.end(), [](const Ent& a, const Ent& b) { return a.cell < b.cell; });
     std::vector<int> slot_off(1, 0), ent_src, ent_comp;
+    std::vector<long long> slot_cell;
     std::vector<Cplx<T>> ent_amp;
     for (size_t e = 0; e < ents.size();) {
       size_t e2 = e;
@@ -297,11 +290,35 @@ class Sim : public SimBase {
         ++e2;
       }
       slot_off.push_back(int(ent_src.size()));
+      slot_cell.push_back(ents[e].cell);
       cls[ents[e].cell] |= uint32_t(slot) << kh::kSlotShift;
       e = e2;
     }
-    n_special_e_ = 0;
-    for (size_t q = 0; q < cls.size(); ++q) n_special_e_ += (cls[q] & kh::kSpecialE) ? 1 : 0;
+    // Which cells the LEAN kernels can take (see run_batch): a source cell's
+    // term can be added after the kernel when its component has no W stage
+    // there and the cell carries no χ3 or pole; CPU-path semantics keep B|D
+    // for every component of a special cell inside CPML, which LEAN does not.
+    auto flag = [&](int a, int idx) { return idx < lo_[a] || idx >= n_[a] - hi_[a]; };
+    has_src_[0] = has_src_[1] = false;
+    src_fix_ok_[0] = src_fix_ok_[1] = true;
+    for (const Ent& e : ents) {
+      const int half = e.comp >= 3 ? 1 : 0;
+      has_src_[half] = true;
+      const int own = e.comp % 3;
+      const bool fown = flag(own, own == 0 ? e.i : (own == 1 ? e.j : e.k));
+      if (fown) src_fix_ok_[half] = false;
+      if (!half && (cls[e.cell] & (kh::kHasChi3 | kh::kHasPole))) src_fix_ok_[0] = false;
+    }
+    special_in_region_[0] = special_in_region_[1] = false;
+    for (int k = 0; k < n_[2]; ++k)
+      for (int j = 0; j < n_[1]; ++j)
+        for (int i = 0; i < n_[0]; ++i) {
+          const uint32_t c = cls[cidx(i, j, k)];
+          if (!(c & (kh::kSpecialE | kh::kSpecialH))) continue;
+          if (!(flag(0, i) || flag(1, j) || flag(2, k))) continue;
+          if (c & kh::kSpecialE) special_in_region_[0] = true;
+          if (c & kh::kSpecialH) special_in_region_[1] = true;
+        }
 
     // state arrays that some cell needs
     const bool msb = !msigb_h_[0].empty() || !msigb_h_[1].empty() || !msigb_h_[2].empty();
@@ -359,6 +376,8 @@ class Sim : public SimBase {
       KH_TRY(upload_raw(ent_src.data(), ent_src.size() * sizeof(int), (void**)&ent_src_));
       KH_TRY(upload_raw(ent_comp.data(), ent_comp.size() * sizeof(int), (void**)&ent_comp_));
       KH_TRY(upload_raw(ent_amp.data(), ent_amp.size() * sizeof(Cplx<T>), (void**)&ent_amp_));
+      KH_TRY(upload_raw(slot_cell.data(), slot_cell.size() * sizeof(long long), (void**)&slot_cell_));
+      nslots_ = int(slot_cell.size());
     }
     // monitors
     for (auto& m : mons_) {
@@ -541,9 +560,13 @@ class Sim : public SimBase {
         f[a] = rr[a] != 1;
       }
       if (cnt == 0 || !(f[0] || f[1] || f[2])) continue;
+      // Σ_c 2·(U_c + W_c + T_c): T_c = U_c ∨ W_c on the CPU path; the CUDA-path
+      // stages also keep T_c where only the prev axis is PML (σ_prev stage).
+      const bool cpml = d_.semantics == KH_SEM_CPML;
       int aux = 0;
       for (int c = 0; c < 3; ++c) {
-        const int u = f[(c + 1) % 3] ? 1 : 0, w = f[c] ? 1 : 0, t = (u || w) ? 1 : 0;
+        const int u = f[(c + 1) % 3] ? 1 : 0, w = f[c] ? 1 : 0;
+        const int t = (u || w || (cpml && f[(c + 2) % 3])) ? 1 : 0;
         aux += 2 * (u + w + t);
       }
       hw += double(aux) * double(cnt);  // B side
@@ -808,20 +831,41 @@ class Sim : public SimBase {
       if (timing) cudaEventRecord(events_[5 * s + k], stream);
     };
     kh::HalfStepParams<T> ph = base_params(true), pe = base_params(false);
+    // LEAN unless this half needs the in-kernel general path (see prepare()).
+    const bool msb = msigb_[0] || msigb_[1] || msigb_[2];
+    const bool msd = msigd_[0] || msigd_[1] || msigd_[2];
+    const bool ref_cpu = d_.semantics == KH_SEM_REFERENCE_CPU;
+    const bool full_h_base = msb || (ref_cpu && special_in_region_[1]);
+    const bool full_e_base = msd || chi3_ != nullptr || !poles_d_.empty() || (ref_cpu && special_in_region_[0]);
+    kh::SourceFixParams<T> fh = fix_params(true), fe = fix_params(false);
     for (int s = 0; s < nb; ++s) {
       const StepPlan& P = plan[s];
       ph.sources_active = P.sa ? 1 : 0;
       ph.f_now = dtab + P.fH;
+      const bool src_h = P.sa && has_src_[1];
+      ph.full = (full_h_base || (src_h && !src_fix_ok_[1])) ? 1 : 0;
       mark(s, 0);
       kh::launch_half_step<T>(true, ph, stream);
       ++launches;
+      if (src_h && !ph.full) {
+        fh.f_now = dtab + P.fH;
+        kh::launch_source_fix<T>(fh, stream);
+        ++launches;
+      }
       mark(s, 1);
       for (auto& dm : P.dftH) launch_dft_for(dm.first, dtab + dm.second, stream);
       mark(s, 2);
       pe.sources_active = P.sa ? 1 : 0;
       pe.f_now = dtab + P.fE;
+      const bool src_e = P.sa && has_src_[0];
+      pe.full = (full_e_base || (src_e && !src_fix_ok_[0])) ? 1 : 0;
       kh::launch_half_step<T>(false, pe, stream);
       ++launches;
+      if (src_e && !pe.full) {
+        fe.f_now = dtab + P.fE;
+        kh::launch_source_fix<T>(fe, stream);
+        ++launches;
+      }
       mark(s, 3);
       for (auto& dm : P.dftE) launch_dft_for(dm.first, dtab + dm.second, stream);
       mark(s, 4);
@@ -866,6 +910,25 @@ class Sim : public SimBase {
     ++launches;
   }
 
+  kh::SourceFixParams<T> fix_params(bool h) const {
+    kh::SourceFixParams<T> f;
+    std::memset(&f, 0, sizeof(f));
+    f.nslots = nslots_;
+    f.slot_cell = slot_cell_;
+    f.slot_off = slot_off_;
+    f.ent_src = ent_src_;
+    f.ent_comp = ent_comp_;
+    f.ent_amp = ent_amp_;
+    for (int c = 0; c < 3; ++c) {
+      f.O[c] = h ? H_[c] : E_[c];
+      f.Ts[c] = h ? B_[c] : D_[c];
+      f.m_inv[c] = h ? mu_[c] : eps_[c];
+    }
+    f.m_scalar = h ? T(d_.mu_inv) : T(d_.eps_inv);
+    f.h_half = h ? 1 : 0;
+    return f;
+  }
+
   kh::HalfStepParams<T> base_params(bool h) const {
     kh::HalfStepParams<T> p;
     std::memset(&p, 0, sizeof(p));
@@ -876,7 +939,6 @@ class Sim : public SimBase {
     p.plane = plane_;
     p.origin = origin_;
     p.nxb = nxb_;
-    p.vec = vec_;
     p.dt = dt_;
     for (int a = 0; a < 3; ++a) p.inv_d[a] = T(1) / delta_[a];
     for (int c = 0; c < 3; ++c) {
@@ -927,7 +989,6 @@ class Sim : public SimBase {
   T dt_, delta_[3];
   long long pitch_, plane_, origin_, total_;
   int nxb_;
-  int vec_;
   int lo_[3] = {0, 0, 0}, hi_[3] = {0, 0, 0};
   bool pml_axis_[3] = {false, false, false};
   uint32_t sigmask_b_ = 0, sigmask_d_ = 0;
@@ -939,7 +1000,11 @@ class Sim : public SimBase {
   std::vector<SrcH> srcs_;
   std::vector<Mon> mons_;
   int nsrc_ = 0;
-  long long n_special_e_ = 0;
+  bool has_src_[2] = {false, false};         // [E half, H half]
+  bool src_fix_ok_[2] = {true, true};
+  bool special_in_region_[2] = {false, false};
+  long long* slot_cell_ = nullptr;
+  int nslots_ = 0;
 
   std::vector<void*> allocs_;
   std::vector<std::pair<void*, size_t>> state_;

@@ -119,6 +119,21 @@ def test_partial_or_no_pml(kh, oracle, gpu_lib, boundaries):
     compare(sim.spec(), 120, oracle, gpu_lib, TOL["f64"])
 
 
+@pytest.mark.parametrize("comp", ["EX", "EY", "HZ"])
+@pytest.mark.parametrize("semantics", ["cpml", "reference_cpu"])
+def test_source_inside_cpml(kh, oracle, gpu_lib, comp, semantics):
+    """A source plane inside the x-CPML: with a W stage on its component (Ex)
+    the source is applied in the full kernel, without one (Ey, Hz) after the
+    lean kernel; both must equal the oracle."""
+    src = kh.UniformSource(time_profile=kh.GaussianPulseSource(fcen=0.8, fwidth=0.3),
+                           component=getattr(kh, comp), center=(-1.05, 0.1, 0.0), size=(0, 0.8, 0.6))
+    mon = kh.DFTMonitor(component=kh.EY, center=(0.3, 0, 0), size=(0, 1.0, 1.0), frequencies=[0.8])
+    sim = kh.Simulation(cell_size=(2.6, 2.0, 1.8), resolution=10, sources=[src], monitors=[mon],
+                        boundaries=[[0.4, 0.4]] * 3, dtype="f64", semantics=semantics)
+    steps = 120 if semantics == "cpml" else 50
+    compare(sim.spec(), steps, oracle, gpu_lib, TOL["f64"])
+
+
 def test_whole_axis_pml_fallback(kh, oracle, gpu_lib):
     """PML thicker than half the axis: the reference plans a single chunk whose
     PML flags cover whole axes (Chunking.jl:907-931)."""
