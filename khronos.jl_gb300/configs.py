@@ -111,7 +111,7 @@ def waveguide(dtype="f32", steps=4000, scale=1.0, seed=1234) -> Workload:
     inner_y = size[1] - 2 * pml
     inner_z = size[2] - 2 * pml
     src = ProfileSource(time_profile=GaussianPulseSource(fcen=FCEN, fwidth=0.25 * FCEN),
-                        component=G.EY, center=(-5.0, 0.0, 0.0), size=(0.0, inner_y, inner_z),
+                        component=G.EY, center=(-5.0, 0.0, 0.0), size=(0.0, 0.9 * inner_y, 0.9 * inner_z),
                         profile_func=lambda x, y, z: math.exp(-((y ** 2 + z ** 2) / 0.4 ** 2)))
     fw = 0.25 * FCEN
     freqs = _freqs(21, FCEN - 0.5 * fw, FCEN + 0.5 * fw)

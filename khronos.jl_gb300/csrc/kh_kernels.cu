@@ -274,9 +274,226 @@ __device__ __forceinline__ void pml_cell(const bool (&f)[3], const AxisCoef<T> (
 // FULL = false (LEAN) compiles only plain and CPML cells; cells marked special
 // there are source cells, updated as B|D-keeping cells (O = m⁻¹·T) and given
 // their source term by source_fix_kernel when sources are active.
-template <typename T, int VN, bool H, bool CPML, bool FULL>
-__global__ void __launch_bounds__(32 * kBlockY, kMinBlocks) half_step_kernel(const HalfStepParams<T> p) {
+//
+// The z march is software-pipelined: every load of plane k+1 (fields,
+// neighbours, CPML state, cell classes) is issued before plane k is computed
+// and stored, so each warp keeps two planes of memory traffic in flight.
+template <typename T, int VN>
+struct PlaneLoads {
+  T l0[VN], l1[VN], a2[VN], y0[VN], y2[VN];  // A0/A1 fresh plane, A2, y neighbours
+  T xn1, xn2;                                // x neighbours of A1/A2 for the edge lane
+  T O[3][VN], m[3][VN];
+  T t[3][VN], u[3][VN], w[3][VN], c3[VN];
+  uint32_t cls[VN];
+  bool tf;                                   // plane's tile holds special cells
+};
+
+template <typename T, int VN, bool H, bool FULL>
+__device__ __forceinline__ void load_plane(const HalfStepParams<T>& p, PlaneLoads<T, VN>& L, int k,
+                                           long long row, int lane, bool lane_ok, bool pervox, bool fy,
+                                           bool anyfx, uint64_t tbits) {
   constexpr int s = H ? 1 : -1;
+  const long long q = row + (long long)k * p.plane;
+  vzero(L.l0); vzero(L.l1); vzero(L.a2); vzero(L.y0); vzero(L.y2);
+  L.xn1 = T(0);
+  L.xn2 = T(0);
+  L.tf = ((tbits >> (k & 63)) & 1ull) != 0;
+  const bool fz = k < p.pml_lo[2] || k >= p.nz - p.pml_hi[2];
+  const bool anyRegion = fy || fz || anyfx;
+  const bool axis_any[3] = {anyfx, fy, fz};
+  if (lane_ok) {
+    if constexpr (H) {  // l = A(k+1)
+      vld(p.A[0] + q + p.plane, L.l0);
+      vld(p.A[1] + q + p.plane, L.l1);
+    } else {  // l = A(k)
+      vld(p.A[0] + q, L.l0);
+      vld(p.A[1] + q, L.l1);
+    }
+    vld(p.A[2] + q, L.a2);
+    vld(p.A[0] + q + s * p.pitch, L.y0);
+    vld(p.A[2] + q + s * p.pitch, L.y2);
+    if constexpr (H) {
+      if (lane == 31) {
+        L.xn1 = p.A[1][q + VN];
+        L.xn2 = p.A[2][q + VN];
+      }
+    } else {
+      if (lane == 0) {
+        L.xn1 = p.A[1][q - 1];
+        L.xn2 = p.A[2][q - 1];
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) vld(p.O[c] + q, L.O[c]);
+    if (pervox) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) vld(p.m_inv[c] + q, L.m[c]);
+    }
+#pragma unroll
+    for (int v = 0; v < VN; ++v) L.cls[v] = (L.tf && lane_ok) ? p.cell_class[q + v] : 0u;
+    const bool aux = anyRegion || L.tf;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      if (aux && p.Ts[c]) vld(p.Ts[c] + q, L.t[c]); else vzero(L.t[c]);
+      if (anyRegion && p.U[c] && axis_any[(c + 1) % 3]) vld(p.U[c] + q, L.u[c]); else vzero(L.u[c]);
+      if (anyRegion && p.W[c] && axis_any[c]) vld(p.W[c] + q, L.w[c]); else vzero(L.w[c]);
+    }
+    if (FULL && !H && L.tf && p.chi3) vld(p.chi3 + q, L.c3); else vzero(L.c3);
+  } else {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      vzero(L.O[c]); vzero(L.t[c]); vzero(L.u[c]); vzero(L.w[c]);
+    }
+    vzero(L.c3);
+#pragma unroll
+    for (int v = 0; v < VN; ++v) L.cls[v] = 0u;
+  }
+  if (!pervox) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int v = 0; v < VN; ++v) L.m[c][v] = p.m_scalar;
+  }
+}
+
+// Update of plane k from its loads L; r0/r1 carry the rotated z-neighbour
+// plane of A0/A1 in and out.
+template <typename T, int VN, bool H, bool CPML, bool FULL>
+__device__ __forceinline__ void compute_plane(const HalfStepParams<T>& p, PlaneLoads<T, VN>& L, int k,
+                                              long long row, int lane, bool lane_ok, int x0, int j,
+                                              bool fy, bool anyfx, const bool (&fxv)[VN],
+                                              const AxisCoef<T> (&axv)[VN], const AxisCoef<T>& ay,
+                                              T (&r0)[VN], T (&r1)[VN]) {
+  const long long q = row + (long long)k * p.plane;
+  // cur = A0/A1 at plane k, nb = at plane k+s
+  const T(&cur0)[VN] = H ? r0 : L.l0;
+  const T(&cur1)[VN] = H ? r1 : L.l1;
+  const T(&nb0)[VN] = H ? L.l0 : r0;
+  const T(&nb1)[VN] = H ? L.l1 : r1;
+
+  // x neighbours of A1 and A2 at plane k
+  T x1s[VN], x2s[VN];
+  if constexpr (H) {
+    T n1 = __shfl_down_sync(0xffffffffu, cur1[0], 1);
+    T n2 = __shfl_down_sync(0xffffffffu, L.a2[0], 1);
+    if (lane == 31) {
+      n1 = L.xn1;
+      n2 = L.xn2;
+    }
+#pragma unroll
+    for (int v = 0; v < VN - 1; ++v) { x1s[v] = cur1[v + 1]; x2s[v] = L.a2[v + 1]; }
+    x1s[VN - 1] = n1;
+    x2s[VN - 1] = n2;
+  } else {
+    T n1 = __shfl_up_sync(0xffffffffu, cur1[VN - 1], 1);
+    T n2 = __shfl_up_sync(0xffffffffu, L.a2[VN - 1], 1);
+    if (lane == 0) {
+      n1 = L.xn1;
+      n2 = L.xn2;
+    }
+#pragma unroll
+    for (int v = 1; v < VN; ++v) { x1s[v] = cur1[v - 1]; x2s[v] = L.a2[v - 1]; }
+    x1s[0] = n1;
+    x2s[0] = n2;
+  }
+
+  if (lane_ok) {
+    T K[3][VN];
+#pragma unroll
+    for (int v = 0; v < VN; ++v) {
+      K[0][v] = p.dt * (p.inv_d[2] * (nb1[v] - cur1[v]) - p.inv_d[1] * (L.y2[v] - L.a2[v]));
+      K[1][v] = p.dt * (p.inv_d[0] * (x2s[v] - L.a2[v]) - p.inv_d[2] * (nb0[v] - cur0[v]));
+      K[2][v] = p.dt * (p.inv_d[1] * (L.y0[v] - cur0[v]) - p.inv_d[0] * (x1s[v] - cur1[v]));
+    }
+    const bool fz = k < p.pml_lo[2] || k >= p.nz - p.pml_hi[2];
+    const bool anyRegion = fy || fz || anyfx;
+    bool anySpecial = false;
+#pragma unroll
+    for (int v = 0; v < VN; ++v) anySpecial |= (L.cls[v] & (H ? kSpecialH : kSpecialE)) != 0;
+    if (!anyRegion && !anySpecial) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int v = 0; v < VN; ++v) L.O[c][v] = L.O[c][v] + L.m[c][v] * K[c][v];
+    } else {
+      const AxisCoef<T> az = p.ax[2][k];
+#pragma unroll
+      for (int v = 0; v < VN; ++v) {
+        const int i = x0 + v;
+        if (i >= p.nx) continue;
+        const bool special = (L.cls[v] & (H ? kSpecialH : kSpecialE)) != 0;
+        if (!(fxv[v] || fy || fz || special)) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) L.O[c][v] = L.O[c][v] + L.m[c][v] * K[c][v];
+          continue;
+        }
+        const bool fc[3] = {fxv[v], fy, fz};
+        const AxisCoef<T> ac[3] = {axv[v], ay, az};
+        const T Kc[3] = {K[0][v], K[1][v], K[2][v]};
+        const T mc[3] = {L.m[0][v], L.m[1][v], L.m[2][v]};
+        T Oc[3] = {L.O[0][v], L.O[1][v], L.O[2][v]};
+        T tc[3] = {L.t[0][v], L.t[1][v], L.t[2][v]};
+        T uc[3] = {L.u[0][v], L.u[1][v], L.u[2][v]};
+        T wc[3] = {L.w[0][v], L.w[1][v], L.w[2][v]};
+        if constexpr (FULL) {
+          general_cell<T, H>(p, q + v, i, j, k, fc, ac, L.cls[v], special, Kc, mc, Oc, tc, uc, wc, L.c3[v]);
+        } else {
+          if (fc[0] || fc[1] || fc[2]) {
+            pml_cell<T, CPML>(fc, ac, Kc, mc, Oc, tc, uc, wc);
+          } else {  // source cell outside CPML: keeps its B|D state
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              tc[c] = tc[c] + Kc[c];
+              Oc[c] = mc[c] * tc[c];
+            }
+          }
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          L.O[c][v] = Oc[c];
+          L.t[c][v] = tc[c];
+          L.u[c][v] = uc[c];
+          L.w[c][v] = wc[c];
+        }
+      }
+      const bool axis_any[3] = {anyfx, fy, fz};
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        if (p.Ts[c]) vst(p.Ts[c] + q, L.t[c]);
+        if (p.U[c] && axis_any[(c + 1) % 3]) vst(p.U[c] + q, L.u[c]);
+        if (p.W[c] && axis_any[c]) vst(p.W[c] + q, L.w[c]);
+      }
+    }
+    if (x0 + VN <= p.nx) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) vst(p.O[c] + q, L.O[c]);
+    } else {
+#pragma unroll
+      for (int v = 0; v < VN; ++v) {
+        if (x0 + v < p.nx) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) p.O[c][q + v] = L.O[c][v];
+        }
+      }
+    }
+  }
+  // rotate: H half keeps A(k+1) as the next plane's A(k); E half keeps
+  // A(k) as the next plane's A(k-1)
+#pragma unroll
+  for (int v = 0; v < VN; ++v) { r0[v] = L.l0[v]; r1[v] = L.l1[v]; }
+}
+
+// One fused half-step.  H = true: B/H from curl E; H = false: D/E from curl H.
+// FULL = false (LEAN) compiles only plain and CPML cells; cells marked special
+// there are source cells, updated as B|D-keeping cells (O = m⁻¹·T) and given
+// their source term by source_fix_kernel when sources are active.
+//
+// The z march is double-buffered with a prefetch distance of two planes: the
+// loads of plane k+2 are issued as soon as plane k has been consumed, so each
+// warp keeps about two planes of memory traffic in flight.
+template <typename T, int VN, bool H, bool CPML, bool FULL>
+__global__ void __launch_bounds__(32 * kBlockY, sizeof(T) == 4 ? kMinBlocks : 2)
+    half_step_kernel(const HalfStepParams<T> p) {
   const int lane = threadIdx.x;
   const int j = blockIdx.y * kBlockY + threadIdx.y;
   if (j >= p.ny) return;  // warp-uniform: blockDim.x == 32
@@ -286,10 +503,10 @@ __global__ void __launch_bounds__(32 * kBlockY, kMinBlocks) half_step_kernel(con
   const int k0 = blockIdx.z * kPlanesPerCta;
   const int k1 = min(k0 + kPlanesPerCta, p.nz);
   const long long row = p.origin + (long long)j * p.pitch + x0;
-  const long long ystep = (long long)s * p.pitch;
-  const long long zstep = (long long)s * p.plane;
   const bool fy = j < p.pml_lo[1] || j >= p.ny - p.pml_hi[1];
   const bool pervox = p.m_inv[0] != nullptr;
+  // special-tile bits of planes [64·(k0/64), +64) of this warp's row segment
+  const uint64_t tbits = p.tile_bits ? p.tile_bits[((long long)(k0 >> 6) * p.ny + j) * p.nxb + xb] : 0ull;
 
   // per-cell x flags and CPML coefficients of this thread's vector and the
   // row's y coefficients: static along the z march
@@ -305,7 +522,7 @@ __global__ void __launch_bounds__(32 * kBlockY, kMinBlocks) half_step_kernel(con
   }
   const AxisCoef<T> ay = p.ax[1][j];
 
-  // rotated z-neighbour planes of A0, A1
+  // rotated z-neighbour plane of A0, A1: A(k0) for the H half, A(k0-1) for E
   T r0[VN], r1[VN];
   vzero(r0);
   vzero(r1);
@@ -314,170 +531,16 @@ __global__ void __launch_bounds__(32 * kBlockY, kMinBlocks) half_step_kernel(con
     vld(p.A[0] + q0, r0);
     vld(p.A[1] + q0, r1);
   }
-
-  for (int k = k0; k < k1; ++k) {
-    const long long q = row + (long long)k * p.plane;
-    T l0[VN], l1[VN], a2[VN], y0[VN], y2[VN];
-    vzero(l0); vzero(l1); vzero(a2); vzero(y0); vzero(y2);
-    T O[3][VN], m[3][VN];
-    if (lane_ok) {
-      if constexpr (H) {  // l = A(k+1)
-        vld(p.A[0] + q + zstep, l0);
-        vld(p.A[1] + q + zstep, l1);
-      } else {  // l = A(k)
-        vld(p.A[0] + q, l0);
-        vld(p.A[1] + q, l1);
-      }
-      vld(p.A[2] + q, a2);
-      vld(p.A[0] + q + ystep, y0);
-      vld(p.A[2] + q + ystep, y2);
-#pragma unroll
-      for (int c = 0; c < 3; ++c) vld(p.O[c] + q, O[c]);
-      if (pervox) {
-#pragma unroll
-        for (int c = 0; c < 3; ++c) vld(p.m_inv[c] + q, m[c]);
-      }
+  PlaneLoads<T, VN> A, B;
+  load_plane<T, VN, H, FULL>(p, A, k0, row, lane, lane_ok, pervox, fy, anyfx, tbits);
+  if (k0 + 1 < k1) load_plane<T, VN, H, FULL>(p, B, k0 + 1, row, lane, lane_ok, pervox, fy, anyfx, tbits);
+  for (int k = k0; k < k1; k += 2) {
+    compute_plane<T, VN, H, CPML, FULL>(p, A, k, row, lane, lane_ok, x0, j, fy, anyfx, fxv, axv, ay, r0, r1);
+    if (k + 2 < k1) load_plane<T, VN, H, FULL>(p, A, k + 2, row, lane, lane_ok, pervox, fy, anyfx, tbits);
+    if (k + 1 < k1) {
+      compute_plane<T, VN, H, CPML, FULL>(p, B, k + 1, row, lane, lane_ok, x0, j, fy, anyfx, fxv, axv, ay, r0, r1);
+      if (k + 3 < k1) load_plane<T, VN, H, FULL>(p, B, k + 3, row, lane, lane_ok, pervox, fy, anyfx, tbits);
     }
-    if (!pervox) {
-#pragma unroll
-      for (int c = 0; c < 3; ++c)
-#pragma unroll
-        for (int v = 0; v < VN; ++v) m[c][v] = p.m_scalar;
-    }
-    // cur = A0/A1 at plane k, nb = at plane k+s
-    const T(&cur0)[VN] = H ? r0 : l0;
-    const T(&cur1)[VN] = H ? r1 : l1;
-    const T(&nb0)[VN] = H ? l0 : r0;
-    const T(&nb1)[VN] = H ? l1 : r1;
-
-    // x neighbours of A1 and A2 at plane k
-    T x1s[VN], x2s[VN];
-    if constexpr (H) {
-      T n1 = __shfl_down_sync(0xffffffffu, cur1[0], 1);
-      T n2 = __shfl_down_sync(0xffffffffu, a2[0], 1);
-      if (lane == 31 && lane_ok) {
-        n1 = p.A[1][q + VN];
-        n2 = p.A[2][q + VN];
-      }
-#pragma unroll
-      for (int v = 0; v < VN - 1; ++v) { x1s[v] = cur1[v + 1]; x2s[v] = a2[v + 1]; }
-      x1s[VN - 1] = n1;
-      x2s[VN - 1] = n2;
-    } else {
-      T n1 = __shfl_up_sync(0xffffffffu, cur1[VN - 1], 1);
-      T n2 = __shfl_up_sync(0xffffffffu, a2[VN - 1], 1);
-      if (lane == 0 && lane_ok) {
-        n1 = p.A[1][q - 1];
-        n2 = p.A[2][q - 1];
-      }
-#pragma unroll
-      for (int v = 1; v < VN; ++v) { x1s[v] = cur1[v - 1]; x2s[v] = a2[v - 1]; }
-      x1s[0] = n1;
-      x2s[0] = n2;
-    }
-
-    if (lane_ok) {
-      T K[3][VN];
-#pragma unroll
-      for (int v = 0; v < VN; ++v) {
-        K[0][v] = p.dt * (p.inv_d[2] * (nb1[v] - cur1[v]) - p.inv_d[1] * (y2[v] - a2[v]));
-        K[1][v] = p.dt * (p.inv_d[0] * (x2s[v] - a2[v]) - p.inv_d[2] * (nb0[v] - cur0[v]));
-        K[2][v] = p.dt * (p.inv_d[1] * (y0[v] - cur0[v]) - p.inv_d[0] * (x1s[v] - cur1[v]));
-      }
-      const bool fz = k < p.pml_lo[2] || k >= p.nz - p.pml_hi[2];
-      const bool anyRegion = fy || fz || anyfx;
-      uint32_t cls[VN];
-      bool anySpecial = false;
-      const bool tf = p.tile_flag && (p.tile_flag[((long long)k * p.ny + j) * p.nxb + xb] & p.tile_bit);
-#pragma unroll
-      for (int v = 0; v < VN; ++v) {
-        cls[v] = (tf && x0 + v < p.nx) ? p.cell_class[q + v] : 0u;
-        anySpecial |= (cls[v] & (H ? kSpecialH : kSpecialE)) != 0;
-      }
-      if (!anyRegion && !anySpecial) {
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-#pragma unroll
-          for (int v = 0; v < VN; ++v) O[c][v] = O[c][v] + m[c][v] * K[c][v];
-      } else {
-        // all auxiliaries this vector may touch, loaded before any arithmetic
-        const bool axis_any[3] = {anyfx, fy, fz};
-        T t[3][VN], u[3][VN], w[3][VN], c3[VN];
-        bool lt[3], lu[3], lw[3];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          lt[c] = p.Ts[c] != nullptr;
-          lu[c] = p.U[c] != nullptr && axis_any[(c + 1) % 3];
-          lw[c] = p.W[c] != nullptr && axis_any[c];
-          if (lt[c]) vld(p.Ts[c] + q, t[c]); else vzero(t[c]);
-          if (lu[c]) vld(p.U[c] + q, u[c]); else vzero(u[c]);
-          if (lw[c]) vld(p.W[c] + q, w[c]); else vzero(w[c]);
-        }
-        if (FULL && !H && anySpecial && p.chi3) vld(p.chi3 + q, c3); else vzero(c3);
-        const AxisCoef<T> az = p.ax[2][k];
-#pragma unroll
-        for (int v = 0; v < VN; ++v) {
-          const int i = x0 + v;
-          if (i >= p.nx) continue;
-          const bool special = (cls[v] & (H ? kSpecialH : kSpecialE)) != 0;
-          if (!(fxv[v] || fy || fz || special)) {
-#pragma unroll
-            for (int c = 0; c < 3; ++c) O[c][v] = O[c][v] + m[c][v] * K[c][v];
-            continue;
-          }
-          const bool fc[3] = {fxv[v], fy, fz};
-          const AxisCoef<T> ac[3] = {axv[v], ay, az};
-          const T Kc[3] = {K[0][v], K[1][v], K[2][v]};
-          const T mc[3] = {m[0][v], m[1][v], m[2][v]};
-          T Oc[3] = {O[0][v], O[1][v], O[2][v]};
-          T tc[3] = {t[0][v], t[1][v], t[2][v]};
-          T uc[3] = {u[0][v], u[1][v], u[2][v]};
-          T wc[3] = {w[0][v], w[1][v], w[2][v]};
-          if constexpr (FULL) {
-            general_cell<T, H>(p, q + v, i, j, k, fc, ac, cls[v], special, Kc, mc, Oc, tc, uc, wc, c3[v]);
-          } else {
-            if (fc[0] || fc[1] || fc[2]) {
-              pml_cell<T, CPML>(fc, ac, Kc, mc, Oc, tc, uc, wc);
-            } else {  // source cell outside CPML: keeps its B|D state
-#pragma unroll
-              for (int c = 0; c < 3; ++c) {
-                tc[c] = tc[c] + Kc[c];
-                Oc[c] = mc[c] * tc[c];
-              }
-            }
-          }
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            O[c][v] = Oc[c];
-            t[c][v] = tc[c];
-            u[c][v] = uc[c];
-            w[c][v] = wc[c];
-          }
-        }
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          if (lt[c]) vst(p.Ts[c] + q, t[c]);
-          if (lu[c]) vst(p.U[c] + q, u[c]);
-          if (lw[c]) vst(p.W[c] + q, w[c]);
-        }
-      }
-      if (x0 + VN <= p.nx) {
-#pragma unroll
-        for (int c = 0; c < 3; ++c) vst(p.O[c] + q, O[c]);
-      } else {
-#pragma unroll
-        for (int v = 0; v < VN; ++v) {
-          if (x0 + v < p.nx) {
-#pragma unroll
-            for (int c = 0; c < 3; ++c) p.O[c][q + v] = O[c][v];
-          }
-        }
-      }
-    }
-    // rotate: H half keeps A(k+1) as the next plane's A(k); E half keeps
-    // A(k) as the next plane's A(k-1)
-#pragma unroll
-    for (int v = 0; v < VN; ++v) { r0[v] = l0[v]; r1[v] = l1[v]; }
   }
 }
 

@@ -93,9 +93,10 @@ struct HalfStepParams {
   int cpml;                    // 1: CUDA-path CPML stages, 0: CPU-path dispatch
   uint32_t sigma_region_mask;  // bit r (r = rx + 3 ry + 9 rz) set: region has conductivity
 
-  const uint8_t* tile_flag;   // per (xb, j, k): special cells present
+  // per (k/64, j, xb): bit k%64 set when that plane's row segment of 32·VN
+  // cells holds special cells of this half
+  const uint64_t* tile_bits;
   const uint32_t* cell_class; // per cell
-  uint8_t tile_bit;           // which tile_flag bit this half reads
 
   // sources (folded into the half-step)
   int sources_active;

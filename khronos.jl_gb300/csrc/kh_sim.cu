@@ -368,7 +368,19 @@ class Sim : public SimBase {
     }
     if (anySpecialE || anySpecialH) {
       KH_TRY(upload_raw(cls.data(), cls.size() * sizeof(uint32_t), (void**)&cls_));
-      KH_TRY(upload_raw(tiles.data(), tiles.size(), (void**)&tiles_));
+      // per-row-segment plane bitmasks: word (k/64, j, xb), bit k%64
+      const int nkw = (n_[2] + 63) / 64;
+      std::vector<uint64_t> bits_e(size_t(nkw) * n_[1] * nxb_, 0ull), bits_h(bits_e.size(), 0ull);
+      for (int k = 0; k < n_[2]; ++k)
+        for (int j = 0; j < n_[1]; ++j)
+          for (int xb = 0; xb < nxb_; ++xb) {
+            const uint8_t tv = tiles[(size_t(k) * n_[1] + j) * nxb_ + xb];
+            const size_t wi = (size_t(k >> 6) * n_[1] + j) * nxb_ + xb;
+            if (tv & 1) bits_e[wi] |= 1ull << (k & 63);
+            if (tv & 2) bits_h[wi] |= 1ull << (k & 63);
+          }
+      KH_TRY(upload_raw(bits_e.data(), bits_e.size() * sizeof(uint64_t), (void**)&tbits_e_));
+      KH_TRY(upload_raw(bits_h.data(), bits_h.size() * sizeof(uint64_t), (void**)&tbits_h_));
     }
     nsrc_ = int(srcs_.size());
     if (!ent_src.empty()) {
@@ -957,9 +969,8 @@ class Sim : public SimBase {
     p.cpml = d_.semantics == KH_SEM_CPML ? 1 : 0;
     p.m_scalar = h ? T(d_.mu_inv) : T(d_.eps_inv);
     p.sigma_region_mask = h ? sigmask_b_ : sigmask_d_;
-    p.tile_flag = tiles_;
+    p.tile_bits = h ? tbits_h_ : tbits_e_;
     p.cell_class = cls_;
-    p.tile_bit = h ? 2 : 1;
     p.slot_off = slot_off_;
     p.ent_src = ent_src_;
     p.ent_comp = ent_comp_;
@@ -1013,7 +1024,7 @@ class Sim : public SimBase {
   T *eps_[3] = {}, *mu_[3] = {}, *msigd_[3] = {}, *msigb_[3] = {}, *chi3_ = nullptr;
   kh::AxisCoef<T> *axb_[3] = {}, *axd_[3] = {};
   uint32_t* cls_ = nullptr;
-  uint8_t* tiles_ = nullptr;
+  uint64_t *tbits_e_ = nullptr, *tbits_h_ = nullptr;
   int *slot_off_ = nullptr, *ent_src_ = nullptr, *ent_comp_ = nullptr;
   Cplx<T>* ent_amp_ = nullptr;
 
