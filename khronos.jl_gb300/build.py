@@ -18,7 +18,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = ROOT / "_build" / "khronos_gb300"
 LIB = PKG / "libkhronos_gb300.so"
-SOURCES = ["kh_kernels.cu", "kh_sim.cu"]
+SOURCES = ["kh_kernels.cu", "kh_tma.cu", "kh_sim.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -33,7 +33,7 @@ def _stale() -> bool:
     if not LIB.exists():
         return True
     t = LIB.stat().st_mtime
-    deps = [CSRC / s for s in SOURCES] + [CSRC / "kh_kernels.cuh", ROOT / "include" / "khronos_gb300.h"]
+    deps = [CSRC / s for s in SOURCES] + [CSRC / "kh_kernels.cuh", CSRC / "kh_cell.cuh", ROOT / "include" / "khronos_gb300.h"]
     return any(d.stat().st_mtime > t for d in deps)
 
 

@@ -10,6 +10,8 @@
 //   is never written: it is the reference's zero ghost layer / staggered wall.
 #pragma once
 
+#include <cuda.h>  // CUtensorMap (descriptors are encoded through the runtime's driver entry point)
+
 #include <cstdint>
 
 namespace kh {
@@ -110,7 +112,35 @@ struct HalfStepParams {
   const T* chi3;
   int npoles;
   PoleParams<T> poles[kMaxPoles];
+
+  int* err;  // set to KH_ERR_TIMEOUT by a kernel whose bounded wait gave up
 };
+
+// TMA-staged half-step: tile of kTmaX × kTmaY cells per CTA (one warp per
+// row, 2 cells per lane), kTmaStages-deep shared-memory ring per CTA.
+constexpr int kTmaX = 64;
+constexpr int kTmaY = 4;
+constexpr int kTmaStages = 4;
+
+// Tensor maps of one half-step over the padded layout (x = pitch, y = ny+2,
+// z = nz+2): the curl-source arrays with a box of (kTmaX + 16 bytes) ×
+// (kTmaY + 1) × 1 (x and y halo on the side the curl reads), the updated
+// arrays and the per-voxel m⁻¹ with a box of kTmaX × kTmaY × 1.
+struct alignas(128) TmaMaps {
+  CUtensorMap a[3];
+  CUtensorMap o[3];
+  CUtensorMap m[3];
+};
+
+template <typename T>
+size_t tma_smem_bytes();
+
+template <typename T>
+void launch_half_step_tma(bool h_half, const HalfStepParams<T>& p, const TmaMaps& maps, void* stream);
+
+// One-time per-process kernel attribute set-up (dynamic shared memory size).
+template <typename T>
+int prepare_tma_kernels();
 
 template <typename T>
 struct DftParams {

@@ -21,6 +21,8 @@
 #include "../../include/khronos_gb300.h"
 #include "kh_kernels.cuh"
 
+#include <cudaTypedefs.h>
+
 using kh::Cplx;
 
 namespace {
@@ -49,6 +51,7 @@ struct SimBase {
   virtual kh_status export_state(void* dst, int64_t bytes) = 0;
   virtual kh_status import_state(const void* src, int64_t bytes) = 0;
   virtual double model_bytes_per_step() const = 0;
+  virtual kh_status device_error() = 0;
   virtual void model_split(double& h, double& e, double& dft) const = 0;
   virtual kh_status step_timed(int64_t n, cudaStream_t s, double* h_ms, double* e_ms,
                                double* dft_ms) = 0;
@@ -407,6 +410,12 @@ class Sim : public SimBase {
     }
     KH_CUDA(cudaEventCreateWithFlags(&copy_done_, cudaEventDisableTiming));
     KH_CUDA(cudaEventCreateWithFlags(&batch_done_, cudaEventDisableTiming));
+    KH_TRY(alloc_raw(sizeof(int), (void**)&err_dev_, false));
+    // Half-step kernel: TMA-staged unless KHRONOS_GB300_KERNEL=simt selects the
+    // register-pipelined one.
+    const char* kv = std::getenv("KHRONOS_GB300_KERNEL");
+    use_tma_ = !(kv && std::string(kv) == "simt");
+    if (use_tma_) KH_TRY(build_tma_maps());
     KH_CUDA(cudaDeviceSynchronize());
     prepared_ = true;
     return KH_OK;
@@ -436,6 +445,7 @@ class Sim : public SimBase {
     if (comp < 0 || comp > 5 || !out) return fail(KH_ERR_INVALID, "bad get_field arguments");
     std::vector<T> h(static_cast<size_t>(total_));
     KH_CUDA(cudaDeviceSynchronize());
+    if (kh_status es = check_device_error(); es != KH_OK) return es;
     KH_CUDA(cudaMemcpy(h.data(), comp < 3 ? E_[comp] : H_[comp - 3], total_ * sizeof(T),
                        cudaMemcpyDeviceToHost));
     static const int add[6][3] = {{0, 1, 1}, {1, 0, 1}, {1, 1, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
@@ -455,6 +465,7 @@ class Sim : public SimBase {
     const size_t cnt = size_t(m.ncell) * m.nf;
     std::vector<Cplx<T>> F(cnt), C;
     KH_CUDA(cudaDeviceSynchronize());
+    if (kh_status es = check_device_error(); es != KH_OK) return es;
     KH_CUDA(cudaMemcpy(F.data(), m.F, cnt * sizeof(Cplx<T>), cudaMemcpyDeviceToHost));
     if (m.C) {
       C.resize(cnt);
@@ -857,7 +868,8 @@ class Sim : public SimBase {
       const bool src_h = P.sa && has_src_[1];
       ph.full = (full_h_base || (src_h && !src_fix_ok_[1])) ? 1 : 0;
       mark(s, 0);
-      kh::launch_half_step<T>(true, ph, stream);
+      if (use_tma_) kh::launch_half_step_tma<T>(true, ph, maps_h_, stream);
+      else kh::launch_half_step<T>(true, ph, stream);
       ++launches;
       if (src_h && !ph.full) {
         fh.f_now = dtab + P.fH;
@@ -871,7 +883,8 @@ class Sim : public SimBase {
       pe.f_now = dtab + P.fE;
       const bool src_e = P.sa && has_src_[0];
       pe.full = (full_e_base || (src_e && !src_fix_ok_[0])) ? 1 : 0;
-      kh::launch_half_step<T>(false, pe, stream);
+      if (use_tma_) kh::launch_half_step_tma<T>(false, pe, maps_e_, stream);
+      else kh::launch_half_step<T>(false, pe, stream);
       ++launches;
       if (src_e && !pe.full) {
         fe.f_now = dtab + P.fE;
@@ -920,6 +933,56 @@ class Sim : public SimBase {
     p.comp = m.C;
     kh::launch_dft<T>(p, stream);
     ++launches;
+  }
+
+  // Tensor maps over the padded layout for the TMA-staged kernel.
+  kh_status build_tma_maps() {
+    static int attr_done = -1;
+    if (attr_done != 0) attr_done = kh::prepare_tma_kernels<T>();
+    if (attr_done != 0) return fail(KH_ERR_CUDA, "cudaFuncSetAttribute on the TMA half-step kernels failed");
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult qr;
+    KH_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &qr));
+    if (!fn || qr != cudaDriverEntryPointSuccess) return fail(KH_ERR_CUDA, "cuTensorMapEncodeTiled not available");
+    auto encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    const int hx = 16 / int(sizeof(T));
+    const cuuint64_t dims[3] = {cuuint64_t(pitch_), cuuint64_t(n_[1] + 2), cuuint64_t(n_[2] + 2)};
+    const cuuint64_t strides[2] = {cuuint64_t(pitch_) * sizeof(T), cuuint64_t(plane_) * sizeof(T)};
+    const cuuint32_t box_a[3] = {cuuint32_t(kh::kTmaX + hx), cuuint32_t(kh::kTmaY + 1), 1};
+    const cuuint32_t box_o[3] = {cuuint32_t(kh::kTmaX), cuuint32_t(kh::kTmaY), 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    const CUtensorMapDataType dt = sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+    auto mk = [&](CUtensorMap* m, T* base, const cuuint32_t* box) -> kh_status {
+      // base points at element (-1,-1,-1) - XOFF + ... : the allocation start
+      CUresult r = encode(m, dt, 3, static_cast<void*>(base), dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      if (r != CUDA_SUCCESS) return fail(KH_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+      return KH_OK;
+    };
+    std::memset(&maps_h_, 0, sizeof(maps_h_));
+    std::memset(&maps_e_, 0, sizeof(maps_e_));
+    for (int c = 0; c < 3; ++c) {
+      kh_status st;
+      if ((st = mk(&maps_h_.a[c], E_[c], box_a)) != KH_OK) return st;
+      if ((st = mk(&maps_h_.o[c], H_[c], box_o)) != KH_OK) return st;
+      if (mu_[c] && (st = mk(&maps_h_.m[c], mu_[c], box_o)) != KH_OK) return st;
+      if ((st = mk(&maps_e_.a[c], H_[c], box_a)) != KH_OK) return st;
+      if ((st = mk(&maps_e_.o[c], E_[c], box_o)) != KH_OK) return st;
+      if (eps_[c] && (st = mk(&maps_e_.m[c], eps_[c], box_o)) != KH_OK) return st;
+    }
+    return KH_OK;
+  }
+
+  kh_status device_error() override { return check_device_error(); }
+
+  // A kernel whose bounded wait gave up leaves KH_ERR_TIMEOUT in err_dev_.
+  kh_status check_device_error() {
+    if (!err_dev_) return KH_OK;
+    int e = 0;
+    KH_CUDA(cudaMemcpy(&e, err_dev_, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e != 0) return fail(KH_ERR_TIMEOUT, "a half-step kernel gave up waiting on its TMA copies");
+    return KH_OK;
   }
 
   kh::SourceFixParams<T> fix_params(bool h) const {
@@ -971,6 +1034,7 @@ class Sim : public SimBase {
     p.sigma_region_mask = h ? sigmask_b_ : sigmask_d_;
     p.tile_bits = h ? tbits_h_ : tbits_e_;
     p.cell_class = cls_;
+    p.err = err_dev_;
     p.slot_off = slot_off_;
     p.ent_src = ent_src_;
     p.ent_comp = ent_comp_;
@@ -1016,6 +1080,9 @@ class Sim : public SimBase {
   bool special_in_region_[2] = {false, false};
   long long* slot_cell_ = nullptr;
   int nslots_ = 0;
+  int* err_dev_ = nullptr;
+  bool use_tma_ = true;
+  kh::TmaMaps maps_h_, maps_e_;
 
   std::vector<void*> allocs_;
   std::vector<std::pair<void*, size_t>> state_;
@@ -1125,7 +1192,7 @@ kh_status kh_sim_synchronize(kh_sim* sim) {
     sim->impl->err = cudaGetErrorString(e);
     return KH_ERR_CUDA;
   }
-  return KH_OK;
+  return sim->impl->device_error();
 }
 
 kh_status kh_sim_timestep(const kh_sim* sim, int64_t* out) {
