@@ -230,6 +230,8 @@ def run_ours(args, world, rank, local_rank):
             dist.destroy_process_group()
         return 0
     peak, peak_kind = measured_peaks()
+    simt = os.environ.get("KHRONOS_GB300_KERNEL") == "simt"
+    e_kernel = "half_step_kernel<float,E>" if simt else "half_step_tma_kernel<float,E>"
     e_launch_ms = e_ms / args.steps
     achieved = e_bytes / (e_launch_ms / 1e3) / 1e9
     line = {
@@ -239,10 +241,10 @@ def run_ours(args, world, rank, local_rank):
         "config": {"workload": WORKLOAD, "grid": list(spec.n), "cells": cells,
                    "l2": "inputs larger than L2 (fields+materials+CPML state ~0.9 GB per replica vs 129 MB L2); no flush",
                    "parallelism": f"replicas{world}" if world > 1 else "single"},
-        "roofline": {"bound": "hbm", "kernel": "half_step_kernel<float,E>", "achieved": achieved, "peak": peak,
+        "roofline": {"bound": "hbm", "kernel": e_kernel, "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "algorithmic_bytes_per_launch": e_bytes,
-                     "traffic": ncu_traffic("half_step_kernel<float,E>"),
+                     "traffic": ncu_traffic(e_kernel),
                      "h_kernel": {"achieved": h_bytes / (h_ms / args.steps / 1e3) / 1e9,
                                   "algorithmic_bytes_per_launch": h_bytes, "ms_per_launch": h_ms / args.steps},
                      "e_ms_per_launch": e_launch_ms, "dft_ms_per_step": dft_ms / args.steps,

@@ -18,7 +18,10 @@ namespace kh {
 
 constexpr int kMaxPoles = 4;
 constexpr int kBlockY = 4;      // rows per CTA
-constexpr int kPlanesPerCta = 16;
+#ifndef KH_PLANES_PER_CTA
+#define KH_PLANES_PER_CTA 16
+#endif
+constexpr int kPlanesPerCta = KH_PLANES_PER_CTA;
 // Resident CTAs per SM the half-step kernels are compiled for (caps registers
 // at 65536 / (kMinBlocks · 32 · kBlockY)).
 #ifndef KH_MIN_BLOCKS
@@ -79,6 +82,7 @@ struct HalfStepParams {
   long long pitch, plane, origin;
   int nxb;  // x tiles of 32*VN cells
   int full; // 1: cells with sources/χ3/poles/conductivity handled in-kernel (FULL variant)
+  int zplanes;  // z planes marched by one CTA of the TMA-staged kernel
   T dt, inv_d[3];
 
   const T* A[3];  // curl source field (E for the H half, H for the E half)
@@ -118,9 +122,19 @@ struct HalfStepParams {
 
 // TMA-staged half-step: tile of kTmaX × kTmaY cells per CTA (one warp per
 // row, 2 cells per lane), kTmaStages-deep shared-memory ring per CTA.
+#ifndef KH_TMA_ROWS
+#define KH_TMA_ROWS 4
+#endif
+#ifndef KH_TMA_STAGES
+#define KH_TMA_STAGES 4
+#endif
+#ifndef KH_TMA_MIN_BLOCKS
+#define KH_TMA_MIN_BLOCKS 5
+#endif
 constexpr int kTmaX = 64;
-constexpr int kTmaY = 4;
-constexpr int kTmaStages = 4;
+constexpr int kTmaY = KH_TMA_ROWS;
+constexpr int kTmaStages = KH_TMA_STAGES;
+constexpr int kTmaMinBlocks = KH_TMA_MIN_BLOCKS;
 
 // Tensor maps of one half-step over the padded layout (x = pitch, y = ny+2,
 // z = nz+2): the curl-source arrays with a box of (kTmaX + 16 bytes) ×
@@ -138,9 +152,13 @@ size_t tma_smem_bytes();
 template <typename T>
 void launch_half_step_tma(bool h_half, const HalfStepParams<T>& p, const TmaMaps& maps, void* stream);
 
-// One-time per-process kernel attribute set-up (dynamic shared memory size).
+// Kernel attribute set-up (dynamic shared memory size), once per device.
 template <typename T>
 int prepare_tma_kernels();
+
+// CTAs of the TMA-staged kernel resident on one SM (after prepare_tma_kernels).
+template <typename T>
+int tma_resident_ctas();
 
 template <typename T>
 struct DftParams {

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -28,6 +29,7 @@ using kh::Cplx;
 namespace {
 
 const char* kVersion = "khronos_gb300 1.0 (sm_103a)";
+constexpr int kMaxDevices = 64;
 
 struct SimBase {
   virtual ~SimBase() = default;
@@ -416,6 +418,7 @@ class Sim : public SimBase {
     const char* kv = std::getenv("KHRONOS_GB300_KERNEL");
     use_tma_ = !(kv && std::string(kv) == "simt");
     if (use_tma_) KH_TRY(build_tma_maps());
+    zplanes_ = choose_zplanes();
     KH_CUDA(cudaDeviceSynchronize());
     prepared_ = true;
     return KH_OK;
@@ -937,9 +940,19 @@ class Sim : public SimBase {
 
   // Tensor maps over the padded layout for the TMA-staged kernel.
   kh_status build_tma_maps() {
-    static int attr_done = -1;
-    if (attr_done != 0) attr_done = kh::prepare_tma_kernels<T>();
-    if (attr_done != 0) return fail(KH_ERR_CUDA, "cudaFuncSetAttribute on the TMA half-step kernels failed");
+    // the attribute is per device: set it once for each device a simulation runs on
+    static std::atomic<bool> attr_done[kMaxDevices];
+    int dev = 0;
+    KH_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return fail(KH_ERR_UNSUPPORTED, "device ordinal above the supported range");
+    if (!attr_done[dev]) {
+      if (kh::prepare_tma_kernels<T>() != 0)
+        return fail(KH_ERR_CUDA, "cudaFuncSetAttribute on the TMA half-step kernels failed");
+      attr_done[dev] = true;
+    }
+    int sms = 0;
+    KH_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    tma_slots_ = sms * kh::tma_resident_ctas<T>();
     void* fn = nullptr;
     cudaDriverEntryPointQueryResult qr;
     KH_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &qr));
@@ -972,6 +985,24 @@ class Sim : public SimBase {
       if (eps_[c] && (st = mk(&maps_e_.m[c], eps_[c], box_o)) != KH_OK) return st;
     }
     return KH_OK;
+  }
+
+  // z planes per CTA of the TMA-staged kernel; KHRONOS_GB300_ZPLANES overrides.
+  int choose_zplanes() const {
+    if (const char* zv = std::getenv("KHRONOS_GB300_ZPLANES")) {
+      const int z = std::atoi(zv);
+      if (z >= 1) return std::min(z, n_[2]);
+    }
+    // 10 planes: a measured optimum on 128- and 256-plane grids (one plane of
+    // curl-source halo re-read per CTA against enough CTAs to balance the
+    // SMs); shallower when the launch would not fill two rounds of resident CTAs.
+    int z = 10;
+    if (use_tma_ && tma_slots_ > 0) {
+      const long long xy = (long long)((n_[0] + kh::kTmaX - 1) / kh::kTmaX) * ((n_[1] + kh::kTmaY - 1) / kh::kTmaY);
+      const long long fill = xy * n_[2] / (2LL * tma_slots_);
+      z = int(std::max(2LL, std::min<long long>(z, fill)));
+    }
+    return std::min(z, n_[2]);
   }
 
   kh_status device_error() override { return check_device_error(); }
@@ -1014,6 +1045,7 @@ class Sim : public SimBase {
     p.plane = plane_;
     p.origin = origin_;
     p.nxb = nxb_;
+    p.zplanes = zplanes_;
     p.dt = dt_;
     for (int a = 0; a < 3; ++a) p.inv_d[a] = T(1) / delta_[a];
     for (int c = 0; c < 3; ++c) {
@@ -1082,6 +1114,8 @@ class Sim : public SimBase {
   int nslots_ = 0;
   int* err_dev_ = nullptr;
   bool use_tma_ = true;
+  int zplanes_ = 10;
+  int tma_slots_ = 0;  // SMs × resident TMA-kernel CTAs per SM
   kh::TmaMaps maps_h_, maps_e_;
 
   std::vector<void*> allocs_;

@@ -120,7 +120,7 @@ __device__ __forceinline__ void load_aux(const HalfStepParams<T>& p, AuxLoads<T>
 }  // namespace
 
 template <typename T, bool H, bool CPML, bool FULL>
-__global__ void __launch_bounds__(32 * kTmaY, sizeof(T) == 4 ? 4 : 2)
+__global__ void __launch_bounds__(32 * kTmaY, sizeof(T) == 4 ? kTmaMinBlocks : 2)
     half_step_tma_kernel(const HalfStepParams<T> p, const __grid_constant__ TmaMaps maps) {
   using G = TmaGeom<T>;
   constexpr int VN = 2;
@@ -138,8 +138,8 @@ __global__ void __launch_bounds__(32 * kTmaY, sizeof(T) == 4 ? 4 : 2)
   const bool row_ok = j < p.ny;
   const int x0 = x_tile + lane * VN;
   const bool lane_ok = row_ok && x0 < p.nx;
-  const int k0 = blockIdx.z * kPlanesPerCta;
-  const int k1 = min(k0 + kPlanesPerCta, p.nz);
+  const int k0 = blockIdx.z * p.zplanes;
+  const int k1 = min(k0 + p.zplanes, p.nz);
   const int N = k1 - k0;  // planes computed; loads n = 0..N
   const bool pervox = p.m_inv[0] != nullptr;
 
@@ -185,8 +185,11 @@ __global__ void __launch_bounds__(32 * kTmaY, sizeof(T) == 4 ? 4 : 2)
   // static per-thread data along the march
   const long long row = p.origin + (long long)j * p.pitch + x0;
   const bool fy = row_ok && (j < p.pml_lo[1] || j >= p.ny - p.pml_hi[1]);
-  const uint64_t tbits =
-      (p.tile_bits && row_ok) ? p.tile_bits[((long long)(k0 >> 6) * p.ny + j) * p.nxb + blockIdx.x] : 0ull;
+  // special-cell plane bits of this row segment for planes 64·g .. 64·g+63,
+  // re-read when the march enters the next group of 64 planes
+  const uint64_t* tb_row = (p.tile_bits && row_ok) ? p.tile_bits + (long long)j * p.nxb + blockIdx.x : nullptr;
+  const long long tb_group = (long long)p.ny * p.nxb;
+  uint64_t tbits = tb_row ? tb_row[(long long)(k0 >> 6) * tb_group] : 0ull;
   bool fxv[VN];
   AxisCoef<T> axv[VN];
   bool anyfx = false;
@@ -209,7 +212,10 @@ __global__ void __launch_bounds__(32 * kTmaY, sizeof(T) == 4 ? 4 : 2)
   bool bad = false;
   for (int c = 0; c < N; ++c) {
     const int k = k0 + c;
-    if (c + 1 < N) load_aux<T, H, FULL>(p, nxt, k + 1, row, lane_ok, fy, anyfx, tbits);
+    if (c + 1 < N) {
+      if (tb_row && ((k + 1) & 63) == 0) tbits = tb_row[(long long)((k + 1) >> 6) * tb_group];
+      load_aux<T, H, FULL>(p, nxt, k + 1, row, lane_ok, fy, anyfx, tbits);
+    }
     const int ncur = H ? c : c + 1;
     const int nnb = H ? c + 1 : c;
     bool ok = mbar_wait(&bars[ncur % kTmaStages], uint32_t((ncur / kTmaStages) & 1));
@@ -345,8 +351,7 @@ template <typename T, bool CPML, bool FULL>
 static void launch_tma_variant(bool h_half, const HalfStepParams<T>& p, const TmaMaps& maps,
                                cudaStream_t st) {
   dim3 block(32, kTmaY, 1);
-  dim3 grid((p.nx + kTmaX - 1) / kTmaX, (p.ny + kTmaY - 1) / kTmaY,
-            (p.nz + kPlanesPerCta - 1) / kPlanesPerCta);
+  dim3 grid((p.nx + kTmaX - 1) / kTmaX, (p.ny + kTmaY - 1) / kTmaY, (p.nz + p.zplanes - 1) / p.zplanes);
   const size_t smem = TmaGeom<T>::SMEM;
   if (h_half) half_step_tma_kernel<T, true, CPML, FULL><<<grid, block, smem, st>>>(p, maps);
   else half_step_tma_kernel<T, false, CPML, FULL><<<grid, block, smem, st>>>(p, maps);
@@ -384,11 +389,22 @@ int prepare_tma_kernels() {
   return e;
 }
 
+template <typename T>
+int tma_resident_ctas() {
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, half_step_tma_kernel<T, true, true, false>, 32 * kTmaY,
+                                                    TmaGeom<T>::SMEM) != cudaSuccess)
+    return 1;
+  return n > 0 ? n : 1;
+}
+
 template size_t tma_smem_bytes<float>();
 template size_t tma_smem_bytes<double>();
 template void launch_half_step_tma<float>(bool, const HalfStepParams<float>&, const TmaMaps&, void*);
 template void launch_half_step_tma<double>(bool, const HalfStepParams<double>&, const TmaMaps&, void*);
 template int prepare_tma_kernels<float>();
 template int prepare_tma_kernels<double>();
+template int tma_resident_ctas<float>();
+template int tma_resident_ctas<double>();
 
 }  // namespace kh

@@ -259,3 +259,28 @@ def test_reset_and_state_roundtrip(kh, gpu_lib):
     a.step(90)
     for comp in range(6):
         assert np.array_equal(a.field(comp), fa[comp])
+
+
+def test_z_tiling_is_invisible(kh, oracle, gpu_lib, monkeypatch):
+    """The TMA kernel's z-tile depth changes nothing: tiles that cross a
+    64-plane group of the special-cell bitmask (12, 7) give the same bits as
+    aligned tiles (16, 64), and the default matches the oracle."""
+    from khronos_gb300 import configs
+    from khronos_gb300.device import GpuSim
+
+    w = configs.waveguide(dtype="f32", scale=0.6)
+    sp = w.sim.spec()
+    assert sp.n[2] > 64
+    runs = {}
+    for zp in ("16", "12", "7", "64"):
+        monkeypatch.setenv("KHRONOS_GB300_ZPLANES", zp)
+        s = GpuSim(sp, lib=gpu_lib)
+        s.step(70)
+        runs[zp] = ([s.field(c) for c in range(6)], s.dft(0))
+        s.close()
+    for zp in ("12", "7", "64"):
+        for c in range(6):
+            assert np.array_equal(runs[zp][0][c], runs["16"][0][c]), (zp, c)
+        assert np.array_equal(runs[zp][1], runs["16"][1]), zp
+    monkeypatch.delenv("KHRONOS_GB300_ZPLANES")
+    compare(sp, 70, oracle, gpu_lib, TOL["f32"])
