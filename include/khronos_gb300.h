@@ -176,6 +176,21 @@ kh_status kh_sim_monitor_info(const kh_sim* sim, int32_t monitor_id, int32_t dim
  * device: S(f) = Σ Re(E1·H2* − E2·H1*)·dA after averaging the two normal layers. */
 kh_status kh_sim_flux(kh_sim* sim, const int32_t ids[4], int32_t normal_axis, double dA,
                       double* out);
+/* kh_sim_flux without any device allocation (no counterpart in the reference).
+ * For callers that must not allocate or free device memory while they run:
+ * a cudaFree synchronises the whole device, stalling simulations running on
+ * other streams, and a process whose device memory is fully committed to its
+ * simulations may have nothing left for even a small cudaMalloc.  The
+ * per-frequency sums go to a fixed device array inside the library instead:
+ * at most 4096 frequencies (more returns KH_ERR_INVALID; use kh_sim_flux).
+ * The first call on each device does a one-time set-up (it resolves that
+ * array's device address with the device current); make it before any
+ * stream capture begins.  The array is shared by all simulations of the
+ * process on a device and keeps the last call's values: calls that overlap
+ * on one device (from several host threads) race on it, so serialise them.
+ * Same result as kh_sim_flux. */
+kh_status kh_sim_flux_static(kh_sim* sim, const int32_t ids[4], int32_t normal_axis, double dA,
+                             double* out);
 
 /* State control. */
 kh_status kh_sim_reset(kh_sim* sim);

@@ -91,6 +91,8 @@ SIGNATURES = {
     "kh_sim_read_dft": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]),
     "kh_sim_monitor_info": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "kh_sim_flux": (C.c_int32, [C.c_void_p, C.POINTER(C.c_int32), C.c_int32, C.c_double, C.POINTER(C.c_double)]),
+    "kh_sim_flux_static": (C.c_int32, [C.c_void_p, C.POINTER(C.c_int32), C.c_int32, C.c_double,
+                                       C.POINTER(C.c_double)]),
     "kh_sim_reset": (C.c_int32, [C.c_void_p]),
     "kh_sim_state_bytes": (C.c_int32, [C.c_void_p, C.POINTER(C.c_int64)]),
     "kh_sim_export_state": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64]),

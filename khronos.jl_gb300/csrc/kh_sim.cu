@@ -16,6 +16,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -30,6 +31,43 @@ namespace {
 
 const char* kVersion = "khronos_gb300 1.0 (sm_103a)";
 constexpr int kMaxDevices = 64;
+
+// Device scratch of kh_sim_flux_static: the per-frequency flux sums of one
+// call.  Fixed size (kFluxStaticMaxFreqs doubles = 32 KB per device), shared
+// by every simulation in the process on that device; it keeps the last
+// call's values.  The flux kernel writes every entry 0..nf-1 before the copy
+// reads them, so nothing has to start at zero.
+constexpr int kFluxStaticMaxFreqs = 4096;
+static __device__ __align__(256) double g_flux_static_scratch[kFluxStaticMaxFreqs];
+
+// Device address of g_flux_static_scratch, resolved once per device with that
+// device current (the first kh_sim_flux_static call on the device).
+kh_status flux_static_scratch(double** out, std::string& err) {
+  static std::mutex mu;
+  static double* addr[kMaxDevices] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    err = std::string("cudaGetDevice: ") + cudaGetErrorString(e);
+    return KH_ERR_CUDA;
+  }
+  if (dev < 0 || dev >= kMaxDevices) {
+    err = "device ordinal above the supported range";
+    return KH_ERR_UNSUPPORTED;
+  }
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_flux_static_scratch);
+    if (e != cudaSuccess || !p) {
+      err = std::string("cudaGetSymbolAddress(flux scratch): ") + cudaGetErrorString(e);
+      return KH_ERR_CUDA;
+    }
+    addr[dev] = static_cast<double*>(p);
+  }
+  *out = addr[dev];
+  return KH_OK;
+}
 
 struct SimBase {
   virtual ~SimBase() = default;
@@ -48,6 +86,7 @@ struct SimBase {
   virtual kh_status read_dft(int id, double* out) = 0;
   virtual kh_status monitor_info(int id, int32_t* dims, int32_t* nf) const = 0;
   virtual kh_status flux(const int32_t* ids, int normal, double dA, double* out) = 0;
+  virtual kh_status flux_static(const int32_t* ids, int normal, double dA, double* out) = 0;
   virtual kh_status reset() = 0;
   virtual int64_t state_bytes() const = 0;
   virtual kh_status export_state(void* dst, int64_t bytes) = 0;
@@ -508,6 +547,35 @@ class Sim : public SimBase {
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpy(out, dout, sizeof(double) * m[0]->nf, cudaMemcpyDeviceToHost);
     cudaFree(dout);
+    if (e != cudaSuccess) return fail(KH_ERR_CUDA, cudaGetErrorString(e));
+    return KH_OK;
+  }
+
+  // flux() with the per-frequency sums in the static device scratch instead of
+  // a cudaMalloc'd buffer: no device allocation or free.
+  kh_status flux_static(const int32_t* ids, int normal, double dA, double* out) override {
+    if (!prepared_) return fail(KH_ERR_INVALID, "flux before prepare");
+    if (!ids || !out || normal < 0 || normal > 2) return fail(KH_ERR_INVALID, "bad flux arguments");
+    const Mon* m[4];
+    for (int q = 0; q < 4; ++q) {
+      if (ids[q] < 0 || ids[q] >= int(mons_.size())) return fail(KH_ERR_INVALID, "bad monitor id");
+      m[q] = &mons_[ids[q]];
+      if (m[q]->nf != m[0]->nf) return fail(KH_ERR_INVALID, "flux monitors differ in frequencies");
+    }
+    const int nf = m[0]->nf;
+    if (nf > kFluxStaticMaxFreqs)
+      return fail(KH_ERR_INVALID, "kh_sim_flux_static: " + std::to_string(nf) +
+                                      " frequencies exceed its fixed scratch of " +
+                                      std::to_string(kFluxStaticMaxFreqs) + "; use kh_sim_flux");
+    double* scratch = nullptr;
+    const kh_status st = flux_static_scratch(&scratch, err);
+    if (st != KH_OK) return st;
+    kh::launch_flux<T>(m[0]->F, m[1]->F, m[2]->F, m[3]->F, m[0]->C, m[1]->C, m[2]->C, m[3]->C,
+                       m[0]->dims, m[1]->dims, m[2]->dims, m[3]->dims, normal, nf, dA, scratch,
+                       nullptr);
+    ++launches;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(out, scratch, sizeof(double) * nf, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return fail(KH_ERR_CUDA, cudaGetErrorString(e));
     return KH_OK;
   }
@@ -1265,6 +1333,12 @@ kh_status kh_sim_monitor_info(const kh_sim* sim, int32_t monitor_id, int32_t dim
 kh_status kh_sim_flux(kh_sim* sim, const int32_t ids[4], int32_t normal_axis, double dA, double* out) {
   if (!sim) return KH_ERR_INVALID;
   return sim->impl->flux(ids, normal_axis, dA, out);
+}
+
+kh_status kh_sim_flux_static(kh_sim* sim, const int32_t ids[4], int32_t normal_axis, double dA,
+                             double* out) {
+  if (!sim) return KH_ERR_INVALID;
+  return sim->impl->flux_static(ids, normal_axis, dA, out);
 }
 
 kh_status kh_sim_reset(kh_sim* sim) {

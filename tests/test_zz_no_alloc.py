@@ -1,0 +1,105 @@
+"""kh_sim_flux_static: the flux reduction with its per-frequency sums in the
+library's fixed device array instead of a cudaMalloc'd buffer.
+
+Called through the C ABI and compared with kh_sim_flux on the same monitors.
+Both run the same FP64 kernel on the same DFT arrays, so the bar is
+bit-for-bit equality (written as rtol=0, atol=0).  The file sorts last so
+that the static array has already seen earlier tests' calls when these run,
+and the tests also pass alone.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+MAX_FREQS = 4096  # fixed scratch size of kh_sim_flux_static
+
+
+def _flux_static(gpu, monitor_indices, normal_axis, dA):
+    ids = (C.c_int32 * 4)(*[gpu.monitor_ids[i] for i in monitor_indices])
+    nf = len(gpu.spec.monitors[monitor_indices[0]].freqs)
+    out = np.full(nf, np.nan, dtype=np.float64)
+    st = gpu.lib.kh_sim_flux_static(gpu.handle, ids, int(normal_axis), float(dA),
+                                    out.ctypes.data_as(C.POINTER(C.c_double)))
+    return st, out
+
+
+def test_null_handle_rejected(kh, gpu_lib):
+    out = np.zeros(4)
+    ids = (C.c_int32 * 4)(0, 1, 2, 3)
+    st = gpu_lib.kh_sim_flux_static(None, ids, 0, 1.0, out.ctypes.data_as(C.POINTER(C.c_double)))
+    assert st != 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dtype", ["f32", "f64"])
+def test_flux_static_matches_flux(kh, gpu_lib, dtype):
+    """Two calls in a row per flux plane, planes alternating, equal kh_sim_flux."""
+    from khronos_gb300 import configs
+    from khronos_gb300.device import GpuSim
+
+    w = configs.waveguide(dtype=dtype, scale=0.25)
+    sp = w.sim.spec()
+    gpu = GpuSim(sp, lib=gpu_lib)
+    gpu.step(200)
+    planes = []
+    base = 0
+    for fm in w.flux_monitors:
+        planes.append((list(range(base, base + 4)), fm.normal_axis, fm.dA))
+        base += 4
+    ref = [gpu.flux(ids, ax, dA) for ids, ax, dA in planes]
+    assert all(np.any(r != 0) for r in ref)
+    for _ in range(2):
+        for (ids, ax, dA), r in zip(planes, ref):
+            for _call in range(2):
+                st, got = _flux_static(gpu, ids, ax, dA)
+                assert st == 0, gpu.lib.kh_last_error(gpu.handle).decode()
+                np.testing.assert_allclose(got, r, rtol=0, atol=0)
+    gpu.close()
+
+
+@pytest.mark.gpu
+def test_flux_static_shared_between_simulations(kh, gpu_lib):
+    """A call with fewer frequencies after one with more, from another
+    simulation, reads only its own sums."""
+    from khronos_gb300 import configs
+    from khronos_gb300.device import GpuSim
+
+    wa = configs.waveguide(dtype="f32", scale=0.25)      # 21 frequencies
+    wb = configs.dipole(dtype="f64", resolution=10)      # 3 frequencies
+    a, b = GpuSim(wa.sim.spec(), lib=gpu_lib), GpuSim(wb.sim.spec(), lib=gpu_lib)
+    a.step(150)
+    b.step(150)
+    fa, fb = wa.flux_monitors[0], wb.flux_monitors[0]
+    ref_a = a.flux([0, 1, 2, 3], fa.normal_axis, fa.dA)
+    ref_b = b.flux([0, 1, 2, 3], fb.normal_axis, fb.dA)
+    for _ in range(2):
+        st, got_a = _flux_static(a, [0, 1, 2, 3], fa.normal_axis, fa.dA)
+        assert st == 0
+        st, got_b = _flux_static(b, [0, 1, 2, 3], fb.normal_axis, fb.dA)
+        assert st == 0
+        assert got_b.shape == (3,)
+        np.testing.assert_allclose(got_a, ref_a, rtol=0, atol=0)
+        np.testing.assert_allclose(got_b, ref_b, rtol=0, atol=0)
+    a.close()
+    b.close()
+
+
+@pytest.mark.gpu
+def test_flux_static_rejects_too_many_frequencies(kh, gpu_lib):
+    from khronos_gb300 import configs
+    from khronos_gb300.device import GpuSim
+
+    w = configs.dipole(dtype="f32", resolution=6)
+    fm = w.flux_monitors[0]
+    fm.frequencies = list(np.linspace(0.5, 0.8, MAX_FREQS + 1))
+    sp = w.sim.spec()
+    gpu = GpuSim(sp, lib=gpu_lib)
+    gpu.step(4)
+    st, _ = _flux_static(gpu, [0, 1, 2, 3], fm.normal_axis, fm.dA)
+    assert st == 1  # KH_ERR_INVALID
+    msg = gpu.lib.kh_last_error(gpu.handle).decode()
+    assert str(MAX_FREQS) in msg
+    # the allocating entry point still serves this size
+    assert gpu.flux([0, 1, 2, 3], fm.normal_axis, fm.dA).shape == (MAX_FREQS + 1,)
+    gpu.close()
