@@ -255,12 +255,35 @@ def run_ours(args, world, rank, local_rank):
     }
     if e2e is not None:
         line["e2e"] = e2e
+    if not args.no_flux_check:
+        line["flux_error"] = flux_accuracy(w, sh)
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(spec)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def flux_accuracy(w, sh):
+    """Flux spectra of the full FP32 run against the full FP64 run of the same
+    inputs (the FP32 spec promoted; the FP64 kernels match the FP64 oracle to
+    1e-10 in the parity tests); relative L2 over the frequencies, worst plane."""
+    from khronos_gb300.device import GpuSim
+    from khronos_gb300.monitors import flux_error
+
+    fluxes = {}
+    _, spec32 = build_workload("f32", "cpml")
+    for dt, spec in (("f32", spec32), ("f64", spec32.promoted())):
+        g = GpuSim(spec)
+        g.step(w.steps, sh)
+        fluxes[dt] = [g.flux(list(range(4 * i, 4 * i + 4)), fm.normal_axis, fm.dA)
+                      for i, fm in enumerate(w.flux_monitors)]
+        g.close()
+    errs = [flux_error(a, b) for a, b in zip(fluxes["f32"], fluxes["f64"])]
+    return {"rel_l2": max(e["rel_l2"] for e in errs), "max_rel": max(e["max_rel"] for e in errs),
+            "per_plane": errs, "steps": w.steps, "frequencies": len(w.flux_monitors[0].frequencies),
+            "vs": "FP64 run of the same inputs (FP32 spec promoted) and step count"}
 
 
 def end_to_end(args, spec, w, sh, world, dist, cells):
@@ -299,6 +322,7 @@ def main(argv=None):
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--no-flux-check", action="store_true", help="skip the FP32-vs-FP64 flux leg")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3

@@ -115,3 +115,19 @@ def flux_from_dft(normal_axis: int, e1, e2, h1, h2, dA: float) -> np.ndarray:
     sl = tuple(sl)
     s = (e1[sl] * np.conj(h2[sl]) - e2[sl] * np.conj(h1[sl])).real * dA
     return s.reshape(-1, s.shape[-1]).sum(axis=0)
+
+
+def flux_error(test, ref) -> dict:
+    """Error of a flux spectrum against a reference spectrum (same frequencies):
+    relative L2 over the frequencies, and the largest per-frequency error
+    relative to the largest reference magnitude."""
+    test = np.asarray(test, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    if test.shape != ref.shape:
+        raise ValueError("flux spectra differ in shape")
+    scale = float(np.max(np.abs(ref))) if ref.size else 0.0
+    if scale == 0.0:
+        d = float(np.max(np.abs(test))) if test.size else 0.0
+        return {"rel_l2": d, "max_rel": d}
+    return {"rel_l2": float(np.linalg.norm(test - ref) / np.linalg.norm(ref)),
+            "max_rel": float(np.max(np.abs(test - ref)) / scale)}

@@ -116,6 +116,15 @@ class SimSpec:
     def cells(self) -> int:
         return int(self.n[0]) * int(self.n[1]) * int(self.n[2])
 
+    def promoted(self) -> "SimSpec":
+        """The same run (identical cell indices, monitor boxes, source
+        footprints and input values) computed in FP64: the full-FP64 run an
+        FP32 run's error is measured against.  Only the arithmetic type
+        changes; inputs already rounded to FP32 stay as they are."""
+        import dataclasses
+
+        return dataclasses.replace(self, dtype=KH_F64)
+
 
 def flat_f(a: np.ndarray) -> np.ndarray:
     """x-fastest contiguous float64 copy of a cell-indexed array."""

@@ -128,3 +128,27 @@ def test_oracle_f32_tracks_f64(kh, oracle):
     b.step(300)
     errs = field_errors([b.field(c) for c in range(6)], [a.field(c) for c in range(6)])
     assert max(errs) < 1e-4
+
+
+def test_flux_error_measure(kh):
+    from khronos_gb300.monitors import flux_error
+
+    ref = np.array([1.0, -2.0, 4.0])
+    e = flux_error(ref * (1 + 1e-5), ref)
+    assert abs(e["rel_l2"] - 1e-5) < 1e-12
+    assert abs(e["max_rel"] - 1e-5) < 1e-12
+    assert flux_error(np.zeros(2), np.zeros(2)) == {"rel_l2": 0.0, "max_rel": 0.0}
+    with pytest.raises(ValueError):
+        flux_error(np.zeros(2), np.zeros(3))
+
+
+def test_promoted_spec_keeps_inputs(kh):
+    from khronos_gb300 import configs
+    from khronos_gb300.spec import KH_F32, KH_F64
+
+    sp = configs.dipole(dtype="f32", resolution=10).sim.spec()
+    pp = sp.promoted()
+    assert sp.dtype == KH_F32 and pp.dtype == KH_F64
+    assert pp.n == sp.n and pp.dt == sp.dt and pp.delta == sp.delta
+    assert [m.start for m in pp.monitors] == [m.start for m in sp.monitors]
+    assert all(np.array_equal(a.amp, b.amp) for a, b in zip(pp.sources, sp.sources))
