@@ -314,6 +314,148 @@ def end_to_end(args, spec, w, sh, world, dist, cells):
             "scope": "GpuSim(spec) from host arrays + K steps + DFT arrays and flux read back to host"}
 
 
+def _pct(v, q):
+    import numpy as np
+
+    return float(np.percentile(np.asarray(v, dtype=np.float64), q)) if len(v) else None
+
+
+def serving_leg(n_requests, seed=2024, budget_gb=150.0, max_resident=16, quantum=64, load=1.5):
+    """The serving stream twice: one plain simulation at a time (the
+    reference's run_batch), then through the request server with Poisson
+    arrivals at `load` × the sequential throughput.  Latency = result read
+    back on the host − scheduled arrival."""
+    import threading
+
+    import numpy as np
+    import torch
+
+    from khronos_gb300 import configs
+    from khronos_gb300.device import GpuSim
+    from khronos_gb300.serve import Server
+
+    stream = configs.serving_stream(n_requests, seed)
+    work = [r.work for r in stream]
+
+    def flux_of(g, w):
+        fm = w.flux_monitors[0]
+        return g.flux([0, 1, 2, 3], fm.normal_axis, fm.dA)
+
+    # 1) sequential, back to back: per-request service time
+    torch.cuda.synchronize()
+    service, seq_flux = [], []
+    for r in stream:
+        t0 = time.perf_counter()
+        w = r.make()
+        g = GpuSim(w.sim.spec())
+        g.step(r.steps)
+        seq_flux.append(flux_of(g, w))
+        g.close()
+        service.append(time.perf_counter() - t0)
+    seq_rate = sum(work) / sum(service) / 1e9
+    gap = float(np.mean(service)) / load
+    arrivals = [r.arrival_unit * gap for r in stream]
+    # sequential latencies under the same arrivals (a FIFO single server)
+    finish, seq_lat = 0.0, []
+    for a, sv in zip(arrivals, service):
+        finish = max(finish, a) + sv
+        seq_lat.append(finish - a)
+    seq_span = finish - arrivals[0]
+
+    # 2) the request server, requests submitted at their arrival times
+    srv = Server(int(budget_gb * 1e9), max_resident=max_resident, quantum_steps=quantum)
+    srv_flux = [None] * len(stream)
+    done_at = [0.0] * len(stream)
+    t_start = time.perf_counter()
+    index = {}
+    lock = threading.Lock()
+    errors = []
+
+    def submitter():
+        try:
+            for r, a in zip(stream, arrivals):
+                delay = t_start + a - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                w = r.make()
+                req = srv.submit(w.sim.spec(), r.steps)
+                with lock:
+                    index[req.ticket] = (r.index, w)
+        except Exception as e:  # surfaced below
+            errors.append(e)
+
+    th = threading.Thread(target=submitter)
+    th.start()
+    peak_resident = 0
+    for _ in range(len(stream)):
+        req = srv.next_done(timeout=600.0)
+        if req is None:
+            raise RuntimeError("serving leg: no request finished within 600 s")
+        req.wait()
+        with lock:
+            i, w = index[req.ticket]
+        srv_flux[i] = flux_of(req.sim, w)
+        done_at[i] = time.perf_counter() - t_start
+        req.release()
+        peak_resident = max(peak_resident, srv.stats()["resident"])
+    th.join()
+    srv.close()
+    if errors:
+        raise errors[0]
+    # 3) sustained capacity: the whole stream submitted at once
+    model_bytes = 0.0
+    srv = Server(int(budget_gb * 1e9), max_resident=max_resident, quantum_steps=quantum)
+    t0 = time.perf_counter()
+    pending = []
+    for r in stream:
+        spec = r.make().sim.spec()
+        pending.append(srv.submit(spec, r.steps))
+    for _ in stream:
+        req = srv.next_done(timeout=600.0)
+        if req is None:
+            raise RuntimeError("serving leg: no request finished within 600 s")
+        req.wait()
+        model_bytes += req.sim.model_bytes_per_step() * req.steps
+        req.release()
+    sat_span = time.perf_counter() - t0
+    srv.close()
+    peak_gbs, _ = measured_peaks()
+    srv_lat = [d - a for d, a in zip(done_at, arrivals)]
+    srv_span = max(done_at) - arrivals[0]
+    diff = max(float(np.max(np.abs(a - b)) / max(float(np.max(np.abs(b))), 1e-300))
+               for a, b in zip(srv_flux, seq_flux))
+    lat = lambda v: {"p50": _pct(v, 50), "p95": _pct(v, 95), "p99": _pct(v, 99), "max": max(v)}
+    return {
+        "requests": n_requests, "seed": seed, "budget_gb": budget_gb, "max_resident": max_resident,
+        "quantum_steps": quantum, "offered_load_vs_sequential": load, "mean_interarrival_s": gap,
+        "cell_updates": int(sum(work)),
+        "server": {"gcell_per_s": sum(work) / srv_span / 1e9, "latency_s": lat(srv_lat), "makespan_s": srv_span},
+        "sequential": {"gcell_per_s": sum(work) / seq_span / 1e9, "busy_gcell_per_s": seq_rate,
+                       "latency_s": lat(seq_lat), "makespan_s": seq_span,
+                       "mean_service_s": float(np.mean(service))},
+        "saturated": {"gcell_per_s": sum(work) / sat_span / 1e9, "makespan_s": sat_span,
+                      "model_bytes": model_bytes, "achieved_gbs": model_bytes / sat_span / 1e9,
+                      "hbm_frac": model_bytes / sat_span / 1e9 / peak_gbs},
+        "speedup_aggregate": (sum(work) / srv_span) / (sum(work) / seq_span),
+        "capacity_vs_sequential": (sum(work) / sat_span) / (sum(work) / sum(service)),
+        "flux_max_rel_diff_served_vs_solo": diff,
+    }
+
+
+def run_serving(args):
+    import torch
+
+    torch.cuda.set_device(0)
+    __graft_entry__.package()
+    res = serving_leg(args.serve_requests)
+    line = {"metric": "serve p50/p95/p99 latency and aggregate Gcell-updates/s", "unit": "s",
+            "dtype": "f32", "data": "synthetic", "n_gpus": 1, "config": {"workload": "serving stream", **{
+                k: res[k] for k in ("requests", "seed", "budget_gb", "max_resident", "quantum_steps")}},
+            "serving": res}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -323,12 +465,16 @@ def main(argv=None):
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-flux-check", action="store_true", help="skip the FP32-vs-FP64 flux leg")
+    ap.add_argument("--serve-only", action="store_true", help="run only the serving-stream leg")
+    ap.add_argument("--serve-requests", type=int, default=512)
     args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3
     world, rank, local_rank = dist_env()
     if args.impl == "reference":
         return run_reference(args, world, rank)
+    if args.serve_only:
+        return run_serving(args)
     return run_ours(args, world, rank, local_rank)
 
 

@@ -162,6 +162,8 @@ kh_status kh_sim_prepare(kh_sim* sim);
 
 /* Time stepping: nsteps full steps of step!(sim) on `stream`. */
 kh_status kh_sim_step(kh_sim* sim, int64_t nsteps, void* stream);
+/* Block until the steps queued on this simulation (on any stream) have
+ * finished; KH_ERR_TIMEOUT if a kernel gave up a bounded wait. */
 kh_status kh_sim_synchronize(kh_sim* sim);
 kh_status kh_sim_timestep(const kh_sim* sim, int64_t* out);
 kh_status kh_sim_sources_active(const kh_sim* sim, int32_t* out);
@@ -192,6 +194,11 @@ kh_status kh_sim_flux(kh_sim* sim, const int32_t ids[4], int32_t normal_axis, do
 kh_status kh_sim_flux_static(kh_sim* sim, const int32_t ids[4], int32_t normal_axis, double dA,
                              double* out);
 
+/* Device memory: what kh_sim_prepare will allocate (estimate, available
+ * before prepare; estimate_memory, src/Memory.jl:120-251) and what it has
+ * allocated (0 before prepare). */
+kh_status kh_sim_memory_bytes(const kh_sim* sim, int64_t* estimate, int64_t* allocated);
+
 /* State control. */
 kh_status kh_sim_reset(kh_sim* sim);
 kh_status kh_sim_state_bytes(const kh_sim* sim, int64_t* out);
@@ -212,6 +219,65 @@ kh_status kh_sim_model_bytes_split(const kh_sim* sim, double* h_half, double* e_
  * E half-step kernels and the DFT launches of these nsteps. */
 kh_status kh_sim_step_timed(kh_sim* sim, int64_t nsteps, void* stream, double* h_ms,
                             double* e_ms, double* dft_ms);
+
+/* ---------------------------------------------------------------------------
+ * Request server (continuous batching of independent simulations on one GPU).
+ * Replaces run_batch / run_batch_concurrent / plan_batch (src/Batch.jl:21-263)
+ * and the admission estimate of estimate_memory (src/Memory.jl:120-251):
+ * requests are admitted in arrival order whenever the device-memory budget and
+ * a resident slot allow, prepared on an admission thread while other requests
+ * step, and stepped in quanta on per-slot streams so their kernels overlap.
+ *
+ * Ownership: kh_server_submit takes a created, configured, NOT prepared
+ * kh_sim; from then on the server owns it.  When kh_server_wait reports the
+ * request finished, its results are read with the kh_sim_* calls on the same
+ * handle; kh_server_release then destroys it and frees its budget.  Requests
+ * that are never released keep their memory (and budget) until
+ * kh_server_destroy.
+ * ------------------------------------------------------------------------- */
+typedef struct kh_server kh_server;
+
+enum {
+  KH_REQ_QUEUED = 0,    /* submitted, waiting for budget or a slot */
+  KH_REQ_ADMITTED = 1,  /* being prepared / waiting for the stepping thread */
+  KH_REQ_RUNNING = 2,
+  KH_REQ_DONE = 3,
+  KH_REQ_FAILED = 4,
+  KH_REQ_RELEASED = 5
+};
+
+typedef struct {
+  int64_t budget_bytes;  /* device bytes the admitted, unreleased requests may hold */
+  int32_t max_resident;  /* requests prepared and stepping at once (0: 16) */
+  int32_t quantum_steps; /* steps issued per request per scheduling round (0: 64) */
+} kh_server_desc;
+
+typedef struct {
+  int32_t state;   /* KH_REQ_* */
+  int32_t status;  /* kh_status of a finished request */
+  int64_t steps;   /* steps requested */
+  int64_t bytes;   /* device bytes: estimate until admitted, then allocated */
+  double t_submit, t_admit, t_start, t_done; /* seconds since kh_server_create; -1 = not yet */
+} kh_request_info;
+
+kh_status kh_server_create(const kh_server_desc* desc, kh_server** out);
+/* Queue `sim` for nsteps steps; returns its ticket.  KH_ERR_OOM if its
+ * estimated bytes exceed the whole budget. */
+kh_status kh_server_submit(kh_server* s, kh_sim* sim, int64_t nsteps, int64_t* ticket);
+/* Wait until the request finished (timeout_s < 0: no limit); returns the
+ * request's status, or KH_ERR_TIMEOUT if it is still running. */
+kh_status kh_server_wait(kh_server* s, int64_t ticket, double timeout_s);
+/* Completion queue: the ticket of a finished request not reported before
+ * (each finished request is reported once); KH_ERR_TIMEOUT if none finishes
+ * within timeout_s (< 0: no limit). */
+kh_status kh_server_wait_any(kh_server* s, double timeout_s, int64_t* ticket);
+kh_status kh_server_info(kh_server* s, int64_t ticket, kh_request_info* out);
+kh_status kh_server_release(kh_server* s, int64_t ticket);
+kh_status kh_server_stats(kh_server* s, int64_t* queued, int64_t* resident, int64_t* budget_used);
+const char* kh_server_last_error(const kh_server* s);
+/* Stops admitting and issuing, waits for the work in flight, destroys every
+ * request's simulation that was not released. */
+void kh_server_destroy(kh_server* s);
 
 #ifdef __cplusplus
 }

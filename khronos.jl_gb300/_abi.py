@@ -15,6 +15,7 @@ KH_F32, KH_F64 = 0, 1
 KH_MAT_EPS_INV, KH_MAT_MU_INV, KH_MAT_SIGMA_D, KH_MAT_SIGMA_B, KH_MAT_CHI3 = range(5)
 KH_TIME_GAUSSIAN, KH_TIME_CW, KH_TIME_TABLE = range(3)
 KH_SEM_REFERENCE_CPU, KH_SEM_CPML = 0, 1
+KH_REQ_QUEUED, KH_REQ_ADMITTED, KH_REQ_RUNNING, KH_REQ_DONE, KH_REQ_FAILED, KH_REQ_RELEASED = range(6)
 
 STATUS_NAMES = {
     0: "KH_OK", 1: "KH_ERR_INVALID", 2: "KH_ERR_OOM", 3: "KH_ERR_CUDA",
@@ -69,6 +70,27 @@ class SourceDesc(C.Structure):
     ]
 
 
+class ServerDesc(C.Structure):
+    _fields_ = [
+        ("budget_bytes", C.c_int64),
+        ("max_resident", C.c_int32),
+        ("quantum_steps", C.c_int32),
+    ]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [
+        ("state", C.c_int32),
+        ("status", C.c_int32),
+        ("steps", C.c_int64),
+        ("bytes", C.c_int64),
+        ("t_submit", C.c_double),
+        ("t_admit", C.c_double),
+        ("t_start", C.c_double),
+        ("t_done", C.c_double),
+    ]
+
+
 # Every exported symbol with its ctypes signature: (restype, argtypes).
 SIGNATURES = {
     "kh_version": (C.c_char_p, []),
@@ -100,6 +122,16 @@ SIGNATURES = {
     "kh_sim_model_bytes_per_step": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double)]),
     "kh_sim_model_bytes_split": (C.c_int32, [C.c_void_p] + [C.POINTER(C.c_double)] * 3),
     "kh_sim_step_timed": (C.c_int32, [C.c_void_p, C.c_int64, C.c_void_p] + [C.POINTER(C.c_double)] * 3),
+    "kh_sim_memory_bytes": (C.c_int32, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "kh_server_create": (C.c_int32, [C.POINTER(ServerDesc), C.POINTER(C.c_void_p)]),
+    "kh_server_submit": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
+    "kh_server_wait": (C.c_int32, [C.c_void_p, C.c_int64, C.c_double]),
+    "kh_server_wait_any": (C.c_int32, [C.c_void_p, C.c_double, C.POINTER(C.c_int64)]),
+    "kh_server_info": (C.c_int32, [C.c_void_p, C.c_int64, C.POINTER(RequestInfo)]),
+    "kh_server_release": (C.c_int32, [C.c_void_p, C.c_int64]),
+    "kh_server_stats": (C.c_int32, [C.c_void_p] + [C.POINTER(C.c_int64)] * 3),
+    "kh_server_last_error": (C.c_char_p, [C.c_void_p]),
+    "kh_server_destroy": (None, [C.c_void_p]),
 }
 
 _lib = None

@@ -1,6 +1,6 @@
 """Build recipe for libkhronos_gb300.so (sm_103a, in-tree).
 
-Two translation units are compiled in parallel with nvcc and linked into
+The translation units are compiled in parallel with nvcc and linked into
 ``khronos.jl_gb300/libkhronos_gb300.so``.  No torch extension machinery is
 involved: the product is a plain C-ABI shared library.
 """
@@ -18,7 +18,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = ROOT / "_build" / "khronos_gb300"
 LIB = PKG / "libkhronos_gb300.so"
-SOURCES = ["kh_kernels.cu", "kh_tma.cu", "kh_sim.cu"]
+SOURCES = ["kh_kernels.cu", "kh_tma.cu", "kh_sim.cu", "kh_serve.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -33,7 +33,7 @@ def _stale() -> bool:
     if not LIB.exists():
         return True
     t = LIB.stat().st_mtime
-    deps = [CSRC / s for s in SOURCES] + [CSRC / "kh_kernels.cuh", CSRC / "kh_cell.cuh", ROOT / "include" / "khronos_gb300.h"]
+    deps = [CSRC / s for s in SOURCES] + [CSRC / h for h in ("kh_kernels.cuh", "kh_cell.cuh", "kh_simbase.h")] + [ROOT / "include" / "khronos_gb300.h"]
     return any(d.stat().st_mtime > t for d in deps)
 
 

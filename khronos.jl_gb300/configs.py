@@ -12,6 +12,10 @@ All inputs are synthetic and seeded (no dataset exists for these runs):
 * ``dispersive`` — 256³, 12-cell CPML, ε 2.25 slab with χ3 = 1e-3, 4 Lorentz +
                    4 Drude spheres (seed 42), Ez plane source, 6-face box flux at
                    11 frequencies, 3000 steps.
+* ``serving_stream`` — request stream (seed 2024): grids from {64³, 96³, 128³,
+                   160×160×96, 256×128×64} with a 10-cell CPML, 1–20 spheres,
+                   Ez dipole, 5-frequency flux plane, U(500, 4000) steps,
+                   Poisson arrivals.
 
 ``scale`` shrinks the cell counts (same physical layout, coarser or smaller
 grid) so the CPU oracle can run the same layout in seconds.
@@ -179,6 +183,75 @@ def dispersive(dtype="f32", steps=3000, scale=1.0, seed=42) -> Workload:
                      monitors=fms, dtype=dtype, eps_inv=eps_c, chi3=chi3, poles=poles)
     return Workload("dispersive", sim, steps, fms,
                     f"{sim.n[0]}^3, chi3 slab, 4 Lorentz + 4 Drude spheres, PML 12 cells")
+
+
+SERVING_GRIDS = [(64, 64, 64), (96, 96, 96), (128, 128, 128), (160, 160, 96), (256, 128, 64)]
+
+
+@dataclass
+class ServingRequest:
+    index: int
+    grid: tuple
+    steps: int
+    arrival_unit: float   # arrival time in units of the mean inter-arrival time
+    work: int             # cell-updates
+    make: object = None   # () -> Workload (built on demand)
+
+
+def serving_request(index: int, grid, steps: int, seed: int, dtype="f32") -> Workload:
+    """One request of the serving stream: `grid` cells at 20 cells/µm with a
+    10-cell CPML, 1–20 dielectric spheres (ε ~ U(2, 12), radius 3–15 cells),
+    an Ez Gaussian-pulse dipole at a random interior point and one x-normal
+    5-frequency flux plane."""
+    res = 20
+    pml = 10 / res
+    size = tuple(n / res for n in grid)
+    rng = np.random.default_rng(seed)
+    nsph = int(rng.integers(1, 21))
+    eps = np.ones(grid)
+    lo = [int(res * pml)] * 3
+    hi = [grid[a] - lo[a] for a in range(3)]
+    for _ in range(nsph):
+        r = float(rng.uniform(3, 15))
+        c = [float(rng.uniform(lo[a], hi[a])) for a in range(3)]
+        e = float(rng.uniform(2, 12))
+        b0 = [max(0, int(math.floor(c[a] - r))) for a in range(3)]
+        b1 = [min(grid[a], int(math.ceil(c[a] + r)) + 1) for a in range(3)]
+        ii, jj, kk = np.meshgrid(*[np.arange(b0[a], b1[a]) + 0.5 for a in range(3)], indexing="ij")
+        m = (ii - c[0]) ** 2 + (jj - c[1]) ** 2 + (kk - c[2]) ** 2 <= r * r
+        sub = eps[b0[0]:b1[0], b0[1]:b1[1], b0[2]:b1[2]]
+        sub[m & (sub == 1.0)] = e  # first sphere wins
+    einv = 1.0 / eps
+    margin = 2
+    pos = [float(rng.uniform(lo[a] + margin, hi[a] - margin)) / res - size[a] / 2 for a in range(3)]
+    src = UniformSource(time_profile=GaussianPulseSource(fcen=FCEN, fwidth=0.2 * FCEN), component=G.EZ,
+                        center=tuple(pos), size=(0.0, 0.0, 0.0))
+    inner = [size[a] - 2 * pml for a in range(3)]
+    fm = FluxMonitor(center=(0.3 * inner[0], 0.0, 0.0), size=(0.0, 0.9 * inner[1], 0.9 * inner[2]),
+                     frequencies=_freqs(5, 0.8 * FCEN, 1.2 * FCEN))
+    sim = Simulation(cell_size=size, resolution=res, sources=[src], boundaries=[[pml, pml]] * 3,
+                     monitors=[fm], dtype=dtype, eps_inv=[einv, einv, einv])
+    assert tuple(sim.n) == tuple(grid), (sim.n, grid)
+    return Workload(f"serve{index}", sim, steps, [fm],
+                    f"{grid[0]}x{grid[1]}x{grid[2]}, {nsph} spheres, Ez dipole, {steps} steps")
+
+
+def serving_stream(n_requests: int = 512, seed: int = 2024, dtype="f32") -> List[ServingRequest]:
+    """The request stream: grids uniformly from SERVING_GRIDS, steps
+    ~ U(500, 4000), Poisson arrivals (exponential gaps of unit mean; scale by
+    the chosen mean inter-arrival time)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    t = 0.0
+    for i in range(n_requests):
+        grid = SERVING_GRIDS[int(rng.integers(0, len(SERVING_GRIDS)))]
+        steps = int(rng.integers(500, 4001))
+        t += float(rng.exponential(1.0))
+        sub_seed = int(rng.integers(0, 2 ** 31 - 1))
+        cells = grid[0] * grid[1] * grid[2]
+        out.append(ServingRequest(i, grid, steps, t, cells * steps,
+                                  make=(lambda i=i, g=grid, n=steps, s=sub_seed: serving_request(i, g, n, s, dtype))))
+    return out
 
 
 BUILDERS = {"dipole": dipole, "waveguide": waveguide, "dispersive": dispersive}

@@ -22,6 +22,7 @@
 
 #include "../../include/khronos_gb300.h"
 #include "kh_kernels.cuh"
+#include "kh_simbase.h"
 
 #include <cudaTypedefs.h>
 
@@ -69,34 +70,7 @@ kh_status flux_static_scratch(double** out, std::string& err) {
   return KH_OK;
 }
 
-struct SimBase {
-  virtual ~SimBase() = default;
-  std::string err;
-  int64_t launches = 0;
-  virtual kh_status set_material(int kind, int comp, const double* v) = 0;
-  virtual kh_status add_pole(const kh_pole_coeffs& c, const double* s) = 0;
-  virtual kh_status add_source(const kh_source_desc& s) = 0;
-  virtual kh_status add_monitor(int comp, const int32_t* st, const int32_t* dm, int nf,
-                                const double* f, int dec, int32_t* id) = 0;
-  virtual kh_status prepare() = 0;
-  virtual kh_status step(int64_t n, cudaStream_t s) = 0;
-  virtual int64_t timestep() const = 0;
-  virtual int sources_active() const = 0;
-  virtual kh_status get_field(int comp, double* out) = 0;
-  virtual kh_status read_dft(int id, double* out) = 0;
-  virtual kh_status monitor_info(int id, int32_t* dims, int32_t* nf) const = 0;
-  virtual kh_status flux(const int32_t* ids, int normal, double dA, double* out) = 0;
-  virtual kh_status flux_static(const int32_t* ids, int normal, double dA, double* out) = 0;
-  virtual kh_status reset() = 0;
-  virtual int64_t state_bytes() const = 0;
-  virtual kh_status export_state(void* dst, int64_t bytes) = 0;
-  virtual kh_status import_state(const void* src, int64_t bytes) = 0;
-  virtual double model_bytes_per_step() const = 0;
-  virtual kh_status device_error() = 0;
-  virtual void model_split(double& h, double& e, double& dft) const = 0;
-  virtual kh_status step_timed(int64_t n, cudaStream_t s, double* h_ms, double* e_ms,
-                               double* dft_ms) = 0;
-};
+using kh_host::SimBase;
 
 #define KH_CUDA(call)                                                          \
   do {                                                                         \
@@ -133,8 +107,10 @@ class Sim : public SimBase {
 
   ~Sim() override {
     for (void* p : allocs_) cudaFree(p);
-    if (pinned_) cudaFreeHost(pinned_);
-    if (copy_done_) cudaEventDestroy(copy_done_);
+    for (int b = 0; b < 2; ++b) {
+      if (pinned_[b]) cudaFreeHost(pinned_[b]);
+      if (copy_ev_[b]) cudaEventDestroy(copy_ev_[b]);
+    }
     if (batch_done_) cudaEventDestroy(batch_done_);
     for (cudaEvent_t ev : events_) cudaEventDestroy(ev);
   }
@@ -449,7 +425,15 @@ class Sim : public SimBase {
       if (s.d.time_kind == KH_TIME_CW) has_cw_ = true;
       else last_time_ = std::max(last_time_, double(T(s.d.cutoff)));
     }
-    KH_CUDA(cudaEventCreateWithFlags(&copy_done_, cudaEventDisableTiming));
+    // Per-batch time-factor/phase tables: two device buffers and two pinned
+    // staging buffers (batch b uses buffer b % 2), sized for the largest batch
+    // so stepping never allocates.
+    tab_cap_ = table_capacity() * sizeof(Cplx<T>);
+    for (int b = 0; b < 2; ++b) {
+      KH_TRY(alloc_raw(tab_cap_, &tab_dev_[b], false));
+      KH_CUDA(cudaMallocHost(&pinned_[b], tab_cap_));
+      KH_CUDA(cudaEventCreateWithFlags(&copy_ev_[b], cudaEventDisableTiming));
+    }
     KH_CUDA(cudaEventCreateWithFlags(&batch_done_, cudaEventDisableTiming));
     KH_TRY(alloc_raw(sizeof(int), (void**)&err_dev_, false));
     // Half-step kernel: TMA-staged unless KHRONOS_GB300_KERNEL=simt selects the
@@ -458,7 +442,9 @@ class Sim : public SimBase {
     use_tma_ = !(kv && std::string(kv) == "simt");
     if (use_tma_) KH_TRY(build_tma_maps());
     zplanes_ = choose_zplanes();
-    KH_CUDA(cudaDeviceSynchronize());
+    // the zeroing and uploads above ran on the legacy default stream; wait for
+    // them only (work of other simulations on non-blocking streams goes on)
+    KH_CUDA(cudaStreamSynchronize(cudaStreamLegacy));
     prepared_ = true;
     return KH_OK;
 #undef KH_TRY
@@ -480,14 +466,69 @@ class Sim : public SimBase {
 
   int64_t timestep() const override { return timestep_; }
   int sources_active() const override { return sources_active_ ? 1 : 0; }
+  bool is_prepared() const override { return prepared_; }
+  int64_t cells() const override { return int64_t(n_[0]) * n_[1] * n_[2]; }
+  int64_t device_bytes() const override { return device_bytes_; }
+
+  kh_status wait_idle() override {
+    if (batch_recorded_) KH_CUDA(cudaEventSynchronize(batch_done_));
+    return check_device_error();
+  }
+
+  // The allocations prepare() makes, from the same decisions (an upper bound
+  // where a decision depends on cell classification).
+  int64_t estimate_bytes() const override {
+    const int64_t field = total_ * int64_t(sizeof(T));
+    bool any_pml = false, pml[3];
+    for (int a = 0; a < 3; ++a) {
+      pml[a] = d_.pml_lo[a] > 0 || d_.pml_hi[a] > 0;
+      any_pml |= pml[a];
+    }
+    bool src_e = false, src_h = false;
+    int64_t src_cells = 0;
+    for (auto& sr : srcs_) {
+      (sr.d.component < 3 ? src_e : src_h) = true;
+      src_cells += int64_t(sr.d.dims[0]) * sr.d.dims[1] * sr.d.dims[2];
+    }
+    const bool spec_e = src_e || !chi3_h_.empty() || !poles_.empty();
+    const bool msb = !msigb_h_[0].empty() || !msigb_h_[1].empty() || !msigb_h_[2].empty();
+    const bool msd = !msigd_h_[0].empty() || !msigd_h_[1].empty() || !msigd_h_[2].empty();
+    int64_t b = 6 * field;
+    for (int c = 0; c < 3; ++c) {
+      const int nx = (c + 1) % 3, pv = (c + 2) % 3;
+      if (any_pml || src_h) b += field;
+      if (any_pml || spec_e) b += field;
+      if (pml[nx]) b += 2 * field;
+      if (pml[c]) b += 2 * field;
+      if (msb && (pml[nx] || pml[pv])) b += field;
+      if (msd && (pml[nx] || pml[pv])) b += field;
+      if (!eps_h_[c].empty()) b += field;
+      if (!mu_h_[c].empty()) b += field;
+      if (!msigd_h_[c].empty()) b += field;
+      if (!msigb_h_[c].empty()) b += field;
+    }
+    if (!chi3_h_.empty()) b += field;
+    b += int64_t(poles_.size()) * 7 * field;
+    for (int a = 0; a < 3; ++a) b += 2 * int64_t(n_[a]) * int64_t(sizeof(kh::AxisCoef<T>));
+    if (spec_e || src_h) {
+      b += total_ * 4;
+      b += 2 * int64_t((n_[2] + 63) / 64) * n_[1] * nxb_ * 8;
+    }
+    b += src_cells * int64_t(4 + 4 + sizeof(Cplx<T>) + 8) + 4 * (src_cells + 1);
+    for (auto& m : mons_) {
+      const int64_t cnt = int64_t(m.dims[0]) * m.dims[1] * m.dims[2] * m.nf * int64_t(sizeof(Cplx<T>));
+      b += cnt * (sizeof(T) == 4 ? 2 : 1);
+    }
+    b += 2 * int64_t(table_capacity() * sizeof(Cplx<T>)) + int64_t(sizeof(int));
+    return b;
+  }
 
   // ---------------- results ----------------
   kh_status get_field(int comp, double* out) override {
     if (!prepared_) return fail(KH_ERR_INVALID, "get_field before prepare");
     if (comp < 0 || comp > 5 || !out) return fail(KH_ERR_INVALID, "bad get_field arguments");
     std::vector<T> h(static_cast<size_t>(total_));
-    KH_CUDA(cudaDeviceSynchronize());
-    if (kh_status es = check_device_error(); es != KH_OK) return es;
+    if (kh_status es = wait_idle(); es != KH_OK) return es;
     KH_CUDA(cudaMemcpy(h.data(), comp < 3 ? E_[comp] : H_[comp - 3], total_ * sizeof(T),
                        cudaMemcpyDeviceToHost));
     static const int add[6][3] = {{0, 1, 1}, {1, 0, 1}, {1, 1, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
@@ -506,8 +547,7 @@ class Sim : public SimBase {
     const Mon& m = mons_[id];
     const size_t cnt = size_t(m.ncell) * m.nf;
     std::vector<Cplx<T>> F(cnt), C;
-    KH_CUDA(cudaDeviceSynchronize());
-    if (kh_status es = check_device_error(); es != KH_OK) return es;
+    if (kh_status es = wait_idle(); es != KH_OK) return es;
     KH_CUDA(cudaMemcpy(F.data(), m.F, cnt * sizeof(Cplx<T>), cudaMemcpyDeviceToHost));
     if (m.C) {
       C.resize(cnt);
@@ -538,6 +578,7 @@ class Sim : public SimBase {
       m[q] = &mons_[ids[q]];
       if (m[q]->nf != m[0]->nf) return fail(KH_ERR_INVALID, "flux monitors differ in frequencies");
     }
+    if (kh_status es = wait_idle(); es != KH_OK) return es;
     double* dout = nullptr;
     KH_CUDA(cudaMalloc(&dout, sizeof(double) * m[0]->nf));
     kh::launch_flux<T>(m[0]->F, m[1]->F, m[2]->F, m[3]->F, m[0]->C, m[1]->C, m[2]->C, m[3]->C,
@@ -567,6 +608,7 @@ class Sim : public SimBase {
       return fail(KH_ERR_INVALID, "kh_sim_flux_static: " + std::to_string(nf) +
                                       " frequencies exceed its fixed scratch of " +
                                       std::to_string(kFluxStaticMaxFreqs) + "; use kh_sim_flux");
+    if (kh_status es = wait_idle(); es != KH_OK) return es;
     double* scratch = nullptr;
     const kh_status st = flux_static_scratch(&scratch, err);
     if (st != KH_OK) return st;
@@ -582,8 +624,9 @@ class Sim : public SimBase {
 
   kh_status reset() override {
     if (!prepared_) return fail(KH_ERR_INVALID, "reset before prepare");
-    KH_CUDA(cudaDeviceSynchronize());
+    if (kh_status es = wait_idle(); es != KH_OK) return es;
     for (auto& s : state_) KH_CUDA(cudaMemset(s.first, 0, s.second));
+    KH_CUDA(cudaStreamSynchronize(cudaStreamLegacy));
     timestep_ = 0;
     sources_active_ = true;
     return KH_OK;
@@ -597,7 +640,7 @@ class Sim : public SimBase {
 
   kh_status export_state(void* dst, int64_t bytes) override {
     if (!prepared_ || !dst || bytes != state_bytes()) return fail(KH_ERR_INVALID, "bad export buffer");
-    KH_CUDA(cudaDeviceSynchronize());
+    if (kh_status es = wait_idle(); es != KH_OK) return es;
     char* p = static_cast<char*>(dst);
     int64_t hdr[2] = {timestep_, sources_active_ ? 1 : 0};
     std::memcpy(p, hdr, 16);
@@ -611,7 +654,7 @@ class Sim : public SimBase {
 
   kh_status import_state(const void* src, int64_t bytes) override {
     if (!prepared_ || !src || bytes != state_bytes()) return fail(KH_ERR_INVALID, "bad import buffer");
-    KH_CUDA(cudaDeviceSynchronize());
+    if (kh_status es = wait_idle(); es != KH_OK) return es;
     const char* p = static_cast<const char*>(src);
     int64_t hdr[2];
     std::memcpy(hdr, p, 16);
@@ -709,6 +752,17 @@ class Sim : public SimBase {
  private:
   static constexpr int kBatch = 512;
 
+  // Entries of the largest per-batch table: both halves' source factors on
+  // every step, plus each monitor's phases on its decimation steps.
+  size_t table_capacity() const {
+    size_t n = size_t(kBatch) * 2 * srcs_.size();
+    for (auto& m : mons_) {
+      const int dec = m.dec < 1 ? 1 : m.dec;
+      n += size_t(m.nf) * size_t((kBatch + dec - 1) / dec + 1);
+    }
+    return std::max<size_t>(n, 1);
+  }
+
   struct Timing {
     double h = 0, e = 0, dft = 0;
   };
@@ -784,6 +838,7 @@ class Sim : public SimBase {
     void* p = nullptr;
     KH_CUDA(cudaMalloc(&p, bytes));
     allocs_.push_back(p);
+    device_bytes_ += int64_t(bytes);
     KH_CUDA(cudaMemset(p, 0, bytes));
     if (is_state) state_.push_back({p, bytes});
     *out = p;
@@ -794,6 +849,7 @@ class Sim : public SimBase {
   kh_status upload_raw(const void* h, size_t bytes, void** out) {
     KH_CUDA(cudaMalloc(out, bytes));
     allocs_.push_back(*out);
+    device_bytes_ += int64_t(bytes);
     KH_CUDA(cudaMemcpy(*out, h, bytes, cudaMemcpyHostToDevice));
     return KH_OK;
   }
@@ -890,28 +946,23 @@ class Sim : public SimBase {
         (hm ? P.dftH : P.dftE).push_back({mi, off});
       }
     }
-    // Upload the table (pinned staging, one copy per batch).
-    const size_t bytes = std::max<size_t>(tab.size(), 1) * sizeof(Cplx<T>);
-    if (bytes > tab_cap_) {
-      KH_CUDA(cudaStreamSynchronize(stream));
-      if (tab_dev_) cudaFree(tab_dev_);
-      if (pinned_) cudaFreeHost(pinned_);
-      tab_dev_ = nullptr;
-      pinned_ = nullptr;
-      KH_CUDA(cudaMalloc(&tab_dev_, bytes * 2));
-      KH_CUDA(cudaMallocHost(&pinned_, bytes * 2));
-      tab_cap_ = bytes * 2;
-    } else if (pending_copy_) {
-      KH_CUDA(cudaEventSynchronize(copy_done_));
+    // Upload the table: staging buffer b was last copied from two batches ago;
+    // wait for that copy before overwriting it.
+    const int b = tab_par_;
+    tab_par_ ^= 1;
+    const size_t bytes = tab.size() * sizeof(Cplx<T>);
+    if (bytes > tab_cap_) return fail(KH_ERR_INVALID, "time-factor table exceeds its capacity");
+    if (copy_pending_[b]) {
+      KH_CUDA(cudaEventSynchronize(copy_ev_[b]));
+      copy_pending_[b] = false;
     }
     if (!tab.empty()) {
-      std::memcpy(pinned_, tab.data(), tab.size() * sizeof(Cplx<T>));
-      KH_CUDA(cudaMemcpyAsync(tab_dev_, pinned_, tab.size() * sizeof(Cplx<T>),
-                              cudaMemcpyHostToDevice, stream));
-      KH_CUDA(cudaEventRecord(copy_done_, stream));
-      pending_copy_ = true;
+      std::memcpy(pinned_[b], tab.data(), bytes);
+      KH_CUDA(cudaMemcpyAsync(tab_dev_[b], pinned_[b], bytes, cudaMemcpyHostToDevice, stream));
+      KH_CUDA(cudaEventRecord(copy_ev_[b], stream));
+      copy_pending_[b] = true;
     }
-    const Cplx<T>* dtab = static_cast<const Cplx<T>*>(tab_dev_);
+    const Cplx<T>* dtab = static_cast<const Cplx<T>*>(tab_dev_[b]);
 
     // Timed runs bracket every launch group with events: 5 per step.
     if (timing) {
@@ -969,6 +1020,7 @@ class Sim : public SimBase {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(KH_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
     KH_CUDA(cudaEventRecord(batch_done_, stream));
+    batch_recorded_ = true;
     last_stream_ = stream;
     timestep_ += nb;
     if (timing) {
@@ -1197,12 +1249,15 @@ class Sim : public SimBase {
   int *slot_off_ = nullptr, *ent_src_ = nullptr, *ent_comp_ = nullptr;
   Cplx<T>* ent_amp_ = nullptr;
 
-  void* tab_dev_ = nullptr;
-  void* pinned_ = nullptr;
-  size_t tab_cap_ = 0;
-  bool pending_copy_ = false;
-  cudaEvent_t copy_done_ = nullptr;
+  void* tab_dev_[2] = {nullptr, nullptr};
+  void* pinned_[2] = {nullptr, nullptr};
+  size_t tab_cap_ = 0;  // bytes per buffer
+  int tab_par_ = 0;
+  bool copy_pending_[2] = {false, false};
+  cudaEvent_t copy_ev_[2] = {nullptr, nullptr};
   cudaEvent_t batch_done_ = nullptr;
+  bool batch_recorded_ = false;
+  int64_t device_bytes_ = 0;
   cudaStream_t last_stream_ = nullptr;
   std::vector<cudaEvent_t> events_;
 
@@ -1212,11 +1267,6 @@ class Sim : public SimBase {
 };
 
 }  // namespace
-
-struct kh_sim {
-  std::unique_ptr<SimBase> impl;
-  std::string err;
-};
 
 extern "C" {
 
@@ -1289,12 +1339,8 @@ kh_status kh_sim_step(kh_sim* sim, int64_t nsteps, void* stream) {
 
 kh_status kh_sim_synchronize(kh_sim* sim) {
   if (!sim) return KH_ERR_INVALID;
-  cudaError_t e = cudaDeviceSynchronize();
-  if (e != cudaSuccess) {
-    sim->impl->err = cudaGetErrorString(e);
-    return KH_ERR_CUDA;
-  }
-  return sim->impl->device_error();
+  if (!sim->impl->is_prepared()) return KH_OK;
+  return sim->impl->wait_idle();
 }
 
 kh_status kh_sim_timestep(const kh_sim* sim, int64_t* out) {
@@ -1339,6 +1385,13 @@ kh_status kh_sim_flux_static(kh_sim* sim, const int32_t ids[4], int32_t normal_a
                              double* out) {
   if (!sim) return KH_ERR_INVALID;
   return sim->impl->flux_static(ids, normal_axis, dA, out);
+}
+
+kh_status kh_sim_memory_bytes(const kh_sim* sim, int64_t* estimate, int64_t* allocated) {
+  if (!sim) return KH_ERR_INVALID;
+  if (estimate) *estimate = sim->impl->estimate_bytes();
+  if (allocated) *allocated = sim->impl->device_bytes();
+  return KH_OK;
 }
 
 kh_status kh_sim_reset(kh_sim* sim) {

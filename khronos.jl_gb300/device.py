@@ -18,7 +18,7 @@ def _dptr(a: np.ndarray):
 class GpuSim:
     """Device-resident simulation driven through the C ABI."""
 
-    def __init__(self, spec: SimSpec, lib=None):
+    def __init__(self, spec: SimSpec, lib=None, prepare: bool = True):
         self.spec = spec
         self.lib = lib or _abi.load()
         self.handle = C.c_void_p()
@@ -74,7 +74,8 @@ class GpuSim:
                 self._check(self.lib.kh_sim_add_dft_monitor(self.handle, m.component, st, dm, len(fr),
                                                             _dptr(fr), int(m.decimation), C.byref(mid)))
                 self.monitor_ids.append(mid.value)
-            self._check(self.lib.kh_sim_prepare(self.handle))
+            if prepare:
+                self._check(self.lib.kh_sim_prepare(self.handle))
         except Exception:
             self.close()
             raise
@@ -85,8 +86,14 @@ class GpuSim:
 
     def close(self):
         if self.handle:
-            self.lib.kh_sim_destroy(self.handle)
+            if not getattr(self, "_detached", False):
+                self.lib.kh_sim_destroy(self.handle)
             self.handle = C.c_void_p()
+
+    def detach(self):
+        """Hand the handle's ownership to another owner (a request server):
+        close() no longer destroys it."""
+        self._detached = True
 
     def __del__(self):
         try:
