@@ -456,6 +456,89 @@ def run_serving(args):
     return 0
 
 
+def adjoint_leg(steps=6000, fd_voxels=0, scale=1.0, fp64=True):
+    """Waveguide-bend inverse design (400×400×128, 120×120×22 design voxels,
+    5 frequencies): FP32 objective + adjoint gradient wall time through the
+    public API; optionally the FP64 gradient of the same inputs (error of the
+    FP32 gradient) and central finite differences (δρ = 1e-3, FP64) on
+    `fd_voxels` seeded design voxels."""
+    import numpy as np
+    import torch
+
+    from khronos_gb300 import configs
+    from khronos_gb300.adjoint import bend_problem, reference_fields
+
+    out = {"steps": steps, "scale": scale}
+    w = configs.bend(dtype="f32", steps=steps, scale=scale)
+    cells = int(np.prod(w.sim.n))
+    out["grid"] = list(w.sim.n)
+    out["design_dims"] = list(w.design_dims)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e_ref = reference_fields(w)
+    t_ref = time.perf_counter() - t0
+    opt = bend_problem(w, e_ref)
+    opt(w.rho0, need_gradient=False)  # creates both simulations (set-up, uploads)
+    t0 = time.perf_counter()
+    opt.update_design(w.rho0)
+    f0 = opt.forward_run()
+    t_fwd = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    g32 = opt.adjoint_run().copy()
+    t_adj = time.perf_counter() - t0
+    if opt.gradient_per_freq is None:  # windowed mode: one adjoint run for all frequencies
+        n_adj = 1
+    else:
+        n_adj = int(np.count_nonzero(np.any(opt.gradient_per_freq != 0, axis=(1, 2, 3))))
+    launches = opt._fwd.launches + opt._adj.launches
+    opt.close()
+    out.update({
+        "mode": opt.mode, "history_gb": opt.history_bytes() / 1e9,
+        "f0_fp32": f0, "straight_ref_s": t_ref, "forward_s": t_fwd, "adjoint_s": t_adj,
+        "adjoint_runs": n_adj, "gradient_s": t_fwd + t_adj,
+        "gcell_per_s": cells * steps * (1 + n_adj) / (t_fwd + t_adj) / 1e9,
+        "gpu_launches_fwd_adj": launches,
+    })
+    if fp64:
+        # the FP64 run of the same inputs (FP32 specs promoted)
+        o64 = bend_problem(w, reference_fields(w, promote=True), promote=True)
+        t0 = time.perf_counter()
+        f64, g64 = o64(w.rho0)
+        g64 = g64.copy()
+        out["fp64_gradient_s"] = time.perf_counter() - t0
+        out["f0_fp64"] = f64
+        out["f0_rel_err_fp32"] = abs(f0 - f64) / abs(f64)
+        out["gradient_rel_l2_fp32_vs_fp64"] = float(np.linalg.norm(g32 - g64) / np.linalg.norm(g64))
+        if fd_voxels:
+            rng = np.random.default_rng(99)
+            idx = [tuple(int(rng.integers(0, d)) for d in w.design_dims) for _ in range(fd_voxels)]
+            t0 = time.perf_counter()
+            fd = o64.calculate_fd_gradient(w.rho0, idx, db=1e-3)
+            rel = [abs(g64[i] - f) / abs(f) for i, f in zip(idx, fd)]
+            rel32 = [abs(g32[i] - f) / abs(f) for i, f in zip(idx, fd)]
+            out["fd"] = {"voxels": [list(i) for i in idx], "fd": fd.tolist(),
+                         "adjoint_fp64": [float(g64[i]) for i in idx],
+                         "adjoint_fp32": [float(g32[i]) for i in idx],
+                         "rel_err_fp64_max": max(rel), "rel_err_fp32_max": max(rel32),
+                         "seconds": time.perf_counter() - t0, "db": 1e-3}
+        o64.close()
+    return out
+
+
+def run_adjoint(args):
+    import torch
+
+    torch.cuda.set_device(0)
+    __graft_entry__.package()
+    res = adjoint_leg(args.adjoint_steps, args.adjoint_fd, args.adjoint_scale, not args.adjoint_no_fp64)
+    line = {"metric": "adjoint gradient of the waveguide-bend objective (wall time, s)", "unit": "s",
+            "value": res["gradient_s"], "higher_is_better": False, "dtype": "f32", "data": "synthetic",
+            "n_gpus": 1, "config": {"workload": "waveguide bend inverse design 400x400x128 (scaled by "
+                                                f"{args.adjoint_scale}), 5 frequencies"}, "adjoint": res}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -467,6 +550,11 @@ def main(argv=None):
     ap.add_argument("--no-flux-check", action="store_true", help="skip the FP32-vs-FP64 flux leg")
     ap.add_argument("--serve-only", action="store_true", help="run only the serving-stream leg")
     ap.add_argument("--serve-requests", type=int, default=512)
+    ap.add_argument("--adjoint-only", action="store_true", help="run only the waveguide-bend adjoint leg")
+    ap.add_argument("--adjoint-steps", type=int, default=6000)
+    ap.add_argument("--adjoint-scale", type=float, default=1.0)
+    ap.add_argument("--adjoint-fd", type=int, default=0, help="finite-difference voxels (FP64)")
+    ap.add_argument("--adjoint-no-fp64", action="store_true")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3
@@ -475,6 +563,8 @@ def main(argv=None):
         return run_reference(args, world, rank)
     if args.serve_only:
         return run_serving(args)
+    if args.adjoint_only:
+        return run_adjoint(args)
     return run_ours(args, world, rank, local_rank)
 
 

@@ -194,6 +194,94 @@ kh_status kh_sim_flux(kh_sim* sim, const int32_t ids[4], int32_t normal_axis, do
 kh_status kh_sim_flux_static(kh_sim* sim, const int32_t ids[4], int32_t normal_axis, double dA,
                              double* out);
 
+/* ---------------------------------------------------------------------------
+ * Adjoint (inverse design) support.  Replaces the reference's host-side
+ * adjoint machinery (src/Adjoint/*.jl) behind its OptimizationProblem /
+ * ChainRules rrule:
+ *
+ *   kh_sim_update_material_box   update_design! + reset_fields! per new design
+ *                                (src/Adjoint/DesignRegion.jl, OptimizationProblem.jl:87-93)
+ *   kh_sim_update_source         swapping in the adjoint sources of
+ *                                adjoint_run! (OptimizationProblem.jl:237-277,
+ *                                place_adjoint_source ObjectiveQuantities.jl:290-345)
+ *   kh_sim_dft_overlap           evaluate(::FourierFieldsObjective) and the
+ *                                objective's field overlap (ObjectiveQuantities.jl:282-288)
+ *   kh_adjoint_accumulate        calculate_gradient! (src/Adjoint/GradientKernel.jl:35-109)
+ *
+ * The adjoint run is a forward run of the same kernels with sources on the
+ * objective monitor's cells (Yee-scheme reciprocity: the transfer from a
+ * current source at a to the E field at b equals that from b to a), so no
+ * time history is stored: the gradient needs only the forward and adjoint DFT
+ * fields on the design voxels.
+ * ------------------------------------------------------------------------- */
+
+/* Overwrite per-voxel ε⁻¹ (kind KH_MAT_EPS_INV) or μ⁻¹ (KH_MAT_MU_INV) of one
+ * component in the cell box start..start+dims-1 after kh_sim_prepare; values
+ * x fastest over the box.  The array must have been set with
+ * kh_sim_set_material before prepare.  Waits for this simulation's queued
+ * steps.  Pair it with kh_sim_reset for a new design. */
+kh_status kh_sim_update_material_box(kh_sim* sim, int32_t kind, int32_t comp, const int32_t start[3],
+                                     const int32_t dims[3], const double* values);
+
+/* Replace, after kh_sim_prepare, the amplitudes of source `index` (the order
+ * of kh_sim_add_source; complex interleaved over its dims, NULL = keep) and,
+ * for a KH_TIME_TABLE source, its table (table_len steps, layout of
+ * kh_source_desc.table; NULL = keep) and end time `cutoff`.  The cells a
+ * source injects into are fixed at prepare (its nonzero amplitudes): a
+ * nonzero amplitude elsewhere returns KH_ERR_INVALID.  Waits for this
+ * simulation's queued steps.  The sources-active flag is not touched: call
+ * kh_sim_reset before running the new sources from t = 0. */
+kh_status kh_sim_update_source(kh_sim* sim, int32_t index, const double* amp, int64_t table_len,
+                               const double* table, double cutoff);
+
+/* out[f] = Σ_cells weights[cell, f] · F[cell, f] over DFT monitor
+ * `monitor_id`, FP64 on the device (fixed reduction order).  weights and out
+ * are complex interleaved host arrays; weights has the monitor's layout
+ * (cell x fastest over its box, frequency slowest; dims × nfreq values), out
+ * nfreq values. */
+kh_status kh_sim_dft_overlap(kh_sim* sim, int32_t monitor_id, const double* weights, double* out);
+
+/* Adjoint gradient reduction, FP64 on the device, accumulated into the host
+ * array grad (one double per design voxel, x fastest over the design box):
+ *   grad[v] += Re(coef · Σ_{c=x,y,z} F_c[v, fwd_freq] · A_c[v, adj_freq])
+ * F_c: the forward run's DFT monitors fwd_ids[c] of E_c over the design box;
+ * A_c: the adjoint run's monitors adj_ids[c] over the same box.  With coef =
+ * −2·conj(∂J/∂Y)/Ŝ (Ŝ the adjoint source's DFT at that frequency) each call
+ * adds one frequency's ∂J/∂ε per voxel (summed over the three components of
+ * an isotropic voxel).  Both simulations must have the same precision. */
+kh_status kh_adjoint_accumulate(kh_sim* fwd, const int32_t fwd_ids[3], int32_t fwd_freq, kh_sim* adj,
+                                const int32_t adj_ids[3], int32_t adj_freq, double coef_re,
+                                double coef_im, double* grad);
+
+/* History monitor: records `component` over the cell box start..start+dims-1
+ * after its half-step of every step n < capacity_steps, into a device buffer
+ * of capacity_steps × box cells (values of the run's precision).  Before
+ * kh_sim_prepare.  No counterpart in the reference, which keeps only DFT
+ * monitors; it is the forward/adjoint field record of the windowed adjoint
+ * (kh_history_correlate).  kh_sim_reset restarts recording at step 0. */
+kh_status kh_sim_add_history_monitor(kh_sim* sim, int32_t component, const int32_t start[3],
+                                     const int32_t dims[3], int64_t capacity_steps, int32_t* out_id);
+/* One recorded step of a history monitor (box cells, x fastest) as doubles. */
+kh_status kh_sim_read_history(kh_sim* sim, int32_t history_id, int64_t step, double* out);
+
+/* Windowed adjoint reduction, FP64 on the device, accumulated into the host
+ * array grad (one double per box cell, x fastest):
+ *   grad[v] += coef · Σ_{c=x,y,z} Σ_{m<nsteps} F_c[m, v] · A_c[nsteps−1−m, v]
+ * F_c: the forward run's history monitors fwd_ids[c] (E_c over the design
+ * box); A_c: the adjoint run's history monitors over the same box, the
+ * adjoint being driven by the time-reversed objective weights.  Exact for a
+ * finite run (the DFT form of kh_adjoint_accumulate needs decayed fields).
+ * Replaces calculate_gradient! (src/Adjoint/GradientKernel.jl:35-109) for
+ * that case.  Both histories must hold at least nsteps steps. */
+kh_status kh_history_correlate(kh_sim* fwd, const int32_t fwd_ids[3], kh_sim* adj, const int32_t adj_ids[3],
+                               int64_t nsteps, double coef, double* grad);
+
+/* Squared L2 norms Σ E_c² (out[0..2]) and Σ H_c² (out[3..5]) over the grid,
+ * FP64 on the device: the field decay that stop_when_dft_decayed
+ * (src/Simulation.jl:411-485) tracks through DFT norms, and a finiteness
+ * check (a non-finite field gives a non-finite norm). */
+kh_status kh_sim_field_sq_norms(kh_sim* sim, double out[6]);
+
 /* Device memory: what kh_sim_prepare will allocate (estimate, available
  * before prepare; estimate_memory, src/Memory.jl:120-251) and what it has
  * allocated (0 before prepare). */

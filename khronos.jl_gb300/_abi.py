@@ -123,6 +123,20 @@ SIGNATURES = {
     "kh_sim_model_bytes_split": (C.c_int32, [C.c_void_p] + [C.POINTER(C.c_double)] * 3),
     "kh_sim_step_timed": (C.c_int32, [C.c_void_p, C.c_int64, C.c_void_p] + [C.POINTER(C.c_double)] * 3),
     "kh_sim_memory_bytes": (C.c_int32, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "kh_sim_update_material_box": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_int32),
+                                               C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
+    "kh_sim_update_source": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.c_int64,
+                                         C.POINTER(C.c_double), C.c_double]),
+    "kh_sim_dft_overlap": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "kh_adjoint_accumulate": (C.c_int32, [C.c_void_p, C.POINTER(C.c_int32), C.c_int32, C.c_void_p,
+                                          C.POINTER(C.c_int32), C.c_int32, C.c_double, C.c_double,
+                                          C.POINTER(C.c_double)]),
+    "kh_sim_add_history_monitor": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                               C.c_int64, C.POINTER(C.c_int32)]),
+    "kh_sim_read_history": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int64, C.POINTER(C.c_double)]),
+    "kh_history_correlate": (C.c_int32, [C.c_void_p, C.POINTER(C.c_int32), C.c_void_p, C.POINTER(C.c_int32),
+                                         C.c_int64, C.c_double, C.POINTER(C.c_double)]),
+    "kh_sim_field_sq_norms": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double)]),
     "kh_server_create": (C.c_int32, [C.POINTER(ServerDesc), C.POINTER(C.c_void_p)]),
     "kh_server_submit": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
     "kh_server_wait": (C.c_int32, [C.c_void_p, C.c_int64, C.c_double]),

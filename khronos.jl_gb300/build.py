@@ -18,7 +18,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = ROOT / "_build" / "khronos_gb300"
 LIB = PKG / "libkhronos_gb300.so"
-SOURCES = ["kh_kernels.cu", "kh_tma.cu", "kh_sim.cu", "kh_serve.cu"]
+SOURCES = ["kh_kernels.cu", "kh_tma.cu", "kh_sim.cu", "kh_serve.cu", "kh_adjoint.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

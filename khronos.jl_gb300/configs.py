@@ -185,6 +185,83 @@ def dispersive(dtype="f32", steps=3000, scale=1.0, seed=42) -> Workload:
                     f"{sim.n[0]}^3, chi3 slab, 4 Lorentz + 4 Drude spheres, PML 12 cells")
 
 
+@dataclass
+class BendWorkload:
+    """Inverse-design workload: forward and straight-reference simulations,
+    the design box and the output plane (see ``bend``)."""
+
+    sim: Simulation                 # the bend with the initial design
+    straight: Simulation            # straight strip along +y (E_ref run)
+    design_start: tuple
+    design_dims: tuple
+    rho0: np.ndarray                # initial density over the design box
+    eps_min: float
+    eps_max: float
+    plane: list                     # [(component, start, dims)] of Ex, Ey, Ez on the output plane
+    frequencies: list
+    steps: int
+    description: str = ""
+
+
+def bend(dtype="f32", steps=6000, scale=1.0, seed=7) -> BendWorkload:
+    """3-D waveguide-bend inverse design: 400×400×128 cells at 25 cells/µm
+    (16 × 16 × 5.12 µm) with a 12-cell CPML, ε = 2.085 cladding.  Input strip
+    along +x and output strip along +y (ε 12.25, 0.5 × 0.22 µm) meet a centred
+    120×120×22-voxel design box (4.8 × 4.8 × 0.88 µm) with ρ ~ U(0, 1) (seed 7)
+    and ε = 2.085 + ρ·(12.25 − 2.085) on all three components of each voxel.
+    Source: Ey current plane at x = −6 µm with a Gaussian transverse profile
+    (waist 0.4 µm), Gaussian pulse fcen = 1/1.55, fwidth = 0.25·fcen.
+    Objective plane: y = +6 µm, 2 × 1.2 µm across the output strip, Ex/Ey/Ez at
+    5 frequencies fcen·(0.9 … 1.1).  The straight run (strip along +y, Ex
+    plane source at y = −6 µm) gives E_ref on the same plane.  ``scale``
+    shrinks the resolution (same physical layout)."""
+    res = 25 * scale
+    L, H = 16.0, 5.12
+    pml = 12 / 25
+    e_clad, e_core = 2.085, 12.25
+    g = G.Grid.build((L, L, H), (0, 0, 0), res, dtype)
+    di = max(2, int(round(120 * scale)))
+    dk = max(2, int(round(22 * scale)))
+    dstart = tuple((g.n[a] - d) // 2 for a, d in enumerate((di, di, dk)))
+    ddims = (di, di, dk)
+    rng = np.random.default_rng(seed)
+    rho0 = rng.uniform(0.0, 1.0, size=ddims)
+
+    def eps_arrays(kind: str):
+        out = []
+        for comp in (G.EX, G.EY, G.EZ):
+            xs, ys, zs = yee_coords(g, comp)
+            e = np.full(g.n, e_clad)
+            if kind == "bend":
+                inp = _box_mask(xs, ys, zs, (-L / 4, 0.0, 0.0), (L / 2, 0.5, 0.22))
+                outp = _box_mask(xs, ys, zs, (0.0, L / 4, 0.0), (0.5, L / 2, 0.22))
+                e[inp | outp] = e_core
+                sl = tuple(slice(dstart[a], dstart[a] + ddims[a]) for a in range(3))
+                e[sl] = e_clad + rho0 * (e_core - e_clad)
+            else:
+                e[_box_mask(xs, ys, zs, (0.0, 0.0, 0.0), (0.5, 1e9, 0.22))] = e_core
+            out.append(1.0 / e)
+        return out
+
+    fw = 0.25 * FCEN
+    prof = lambda x, y, z: math.exp(-((y ** 2 + z ** 2) / 0.4 ** 2))
+    src = ProfileSource(time_profile=GaussianPulseSource(fcen=FCEN, fwidth=fw), component=G.EY,
+                        center=(-6.0, 0.0, 0.0), size=(0.0, 2.0, 1.2), profile_func=prof)
+    prof_s = lambda x, y, z: math.exp(-((x ** 2 + z ** 2) / 0.4 ** 2))
+    src_s = ProfileSource(time_profile=GaussianPulseSource(fcen=FCEN, fwidth=fw), component=G.EX,
+                          center=(0.0, -6.0, 0.0), size=(2.0, 0.0, 1.2), profile_func=prof_s)
+    kw = dict(cell_size=(L, L, H), resolution=res, boundaries=[[pml, pml]] * 3, dtype=dtype)
+    sim = Simulation(sources=[src], eps_inv=eps_arrays("bend"), **kw)
+    straight = Simulation(sources=[src_s], eps_inv=eps_arrays("straight"), **kw)
+    plane = []
+    for comp in (G.EX, G.EY, G.EZ):
+        gv = g.grid_volume((0.0, 6.0, 0.0), (2.0, 0.0, 1.2), comp)
+        plane.append((comp, gv.start0, gv.dims))
+    freqs = list(np.linspace(0.9 * FCEN, 1.1 * FCEN, 5))
+    return BendWorkload(sim, straight, dstart, ddims, rho0, e_clad, e_core, plane, freqs, steps,
+                        f"{g.n[0]}x{g.n[1]}x{g.n[2]} bend, design {di}x{di}x{dk}, PML 12 cells")
+
+
 SERVING_GRIDS = [(64, 64, 64), (96, 96, 96), (128, 128, 128), (160, 160, 96), (256, 128, 64)]
 
 

@@ -404,6 +404,30 @@ void launch_dft(const DftParams<T>& p, void* stream) {
 }
 
 // ---------------------------------------------------------------------------
+// History recording: one thread per x-row segment element, rows of the box
+// laid out x fastest in the destination slot.
+template <typename T>
+__global__ void record_kernel(const RecordParams<T> p) {
+  const int rows = p.dims[1] * p.dims[2];
+  for (int r = blockIdx.y; r < rows; r += gridDim.y) {
+    const int jj = r % p.dims[1], kk = r / p.dims[1];
+    const T* src = p.field + p.origin + (long long)(p.start[2] + kk) * p.plane +
+                   (long long)(p.start[1] + jj) * p.pitch + p.start[0];
+    T* dst = p.dst + (long long)r * p.dims[0];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.dims[0]; i += gridDim.x * blockDim.x)
+      dst[i] = src[i];
+  }
+}
+
+template <typename T>
+void launch_record(const RecordParams<T>& p, void* stream) {
+  const int rows = p.dims[1] * p.dims[2];
+  const int tx = p.dims[0] >= 128 ? 128 : 64;
+  dim3 grid((p.dims[0] + tx - 1) / tx, rows < 65535 ? rows : 65535);
+  record_kernel<T><<<grid, tx, 0, static_cast<cudaStream_t>(stream)>>>(p);
+}
+
+// ---------------------------------------------------------------------------
 // Flux (get_flux, FluxMonitor.jl:92-156) in FP64: one block per frequency,
 // fixed-order tree reduction so the result is reproducible.
 template <typename T>
@@ -504,6 +528,8 @@ template void launch_half_step<float>(bool, const HalfStepParams<float>&, void*)
 template void launch_half_step<double>(bool, const HalfStepParams<double>&, void*);
 template void launch_source_fix<float>(const SourceFixParams<float>&, void*);
 template void launch_source_fix<double>(const SourceFixParams<double>&, void*);
+template void launch_record<float>(const RecordParams<float>&, void*);
+template void launch_record<double>(const RecordParams<double>&, void*);
 template void launch_dft<float>(const DftParams<float>&, void*);
 template void launch_dft<double>(const DftParams<double>&, void*);
 template void launch_flux<float>(const Cplx<float>*, const Cplx<float>*, const Cplx<float>*,

@@ -160,6 +160,19 @@ int prepare_tma_kernels();
 template <typename T>
 int tma_resident_ctas();
 
+// History recording: copy one component over a cell box (x fastest) into a
+// contiguous slot of a history buffer.
+template <typename T>
+struct RecordParams {
+  const T* field;
+  long long pitch, plane, origin;
+  int start[3], dims[3];
+  T* dst;
+};
+
+template <typename T>
+void launch_record(const RecordParams<T>& p, void* stream);
+
 template <typename T>
 struct DftParams {
   const T* field;

@@ -192,6 +192,39 @@ class Sim : public SimBase {
     return KH_OK;
   }
 
+  kh_status add_history(int comp, const int32_t* st, const int32_t* dm, int64_t cap,
+                        int32_t* id) override {
+    if (prepared_) return fail(KH_ERR_INVALID, "add_history_monitor after prepare");
+    if (comp < 0 || comp > 5 || !st || !dm || !id || cap <= 0)
+      return fail(KH_ERR_INVALID, "bad history monitor arguments");
+    Hist h;
+    h.comp = comp;
+    for (int a = 0; a < 3; ++a) {
+      h.start[a] = st[a];
+      h.dims[a] = dm[a];
+      if (dm[a] <= 0 || st[a] < 0 || st[a] + dm[a] > n_[a] + 1)
+        return fail(KH_ERR_INVALID, "history box outside the grid");
+    }
+    h.cap = cap;
+    h.ncell = (long long)dm[0] * dm[1] * dm[2];
+    hists_.push_back(h);
+    *id = int32_t(hists_.size() - 1);
+    return KH_OK;
+  }
+
+  kh_status history_view(int id, kh_host::HistoryView* out) override {
+    if (!prepared_) return fail(KH_ERR_INVALID, "history read before prepare");
+    if (id < 0 || id >= int(hists_.size()) || !out) return fail(KH_ERR_INVALID, "bad history monitor id");
+    const Hist& h = hists_[id];
+    out->buf = h.buf;
+    for (int a = 0; a < 3; ++a) out->dims[a] = h.dims[a];
+    out->ncell = h.ncell;
+    out->capacity = h.cap;
+    out->recorded = std::min<int64_t>(timestep_, h.cap);
+    out->dtype = sizeof(T) == 4 ? KH_F32 : KH_F64;
+    return KH_OK;
+  }
+
   kh_status prepare() override {
     if (prepared_) return KH_OK;
     for (int a = 0; a < 3; ++a) {
@@ -275,7 +308,7 @@ class Sim : public SimBase {
         }
     // Sparse source table: entries per cell in injection order
     // (components Ex..Hz, then sources in order; Kernels.jl:455-463, Sources.jl:330-340).
-    struct Ent { long long cell; int src, comp; std::complex<double> amp; int i, j, k; };
+    struct Ent { long long cell; int src, comp; std::complex<double> amp; int i, j, k; long long q; };
     std::vector<Ent> ents;
     for (int comp = 0; comp < 6; ++comp)
       for (size_t si = 0; si < srcs_.size(); ++si) {
@@ -287,15 +320,17 @@ class Sim : public SimBase {
               const int gi = s.d.start[0] + i, gj = s.d.start[1] + j, gk = s.d.start[2] + k;
               // cells outside the updated range are never consumed by the reference
               if (gi < 0 || gj < 0 || gk < 0 || gi >= n_[0] || gj >= n_[1] || gk >= n_[2]) continue;
-              const std::complex<double> a = s.amp[(size_t(k) * s.d.dims[1] + j) * s.d.dims[0] + i];
+              const long long q = ((long long)k * s.d.dims[1] + j) * s.d.dims[0] + i;
+              const std::complex<double> a = s.amp[size_t(q)];
               const std::complex<T> aT(T(a.real()), T(a.imag()));
               if (aT.real() == T(0) && aT.imag() == T(0)) continue;
-              ents.push_back({cidx(gi, gj, gk), int(si), comp, std::complex<double>(aT.real(), aT.imag()), gi, gj, gk});
+              ents.push_back({cidx(gi, gj, gk), int(si), comp, std::complex<double>(aT.real(), aT.imag()), gi, gj, gk, q});
               mark(gi, gj, gk, comp < 3 ? (kh::kSpecialE | kh::kHasSrcE) : (kh::kSpecialH | kh::kHasSrcH));
               if (comp < 3) anySpecialE = true; else anySpecialH = true;
             }
       }
     std::stable_sort(ents.begin(), ents.end(), [](const Ent& a, const Ent& b) { return a.cell < b.cell; });
+    src_ent_.assign(srcs_.size(), {});
     std::vector<int> slot_off(1, 0), ent_src, ent_comp;
     std::vector<long long> slot_cell;
     std::vector<Cplx<T>> ent_amp;
@@ -304,6 +339,7 @@ class Sim : public SimBase {
       const int slot = int(slot_off.size() - 1);
       if (slot >= (1 << 24)) return fail(KH_ERR_UNSUPPORTED, "too many source cells");
       while (e2 < ents.size() && ents[e2].cell == ents[e].cell) {
+        src_ent_[ents[e2].src].push_back({ents[e2].q, int(ent_src.size())});
         ent_src.push_back(ents[e2].src);
         ent_comp.push_back(ents[e2].comp);
         ent_amp.push_back({T(ents[e2].amp.real()), T(ents[e2].amp.imag())});
@@ -408,6 +444,7 @@ class Sim : public SimBase {
       KH_TRY(upload_raw(ent_src.data(), ent_src.size() * sizeof(int), (void**)&ent_src_));
       KH_TRY(upload_raw(ent_comp.data(), ent_comp.size() * sizeof(int), (void**)&ent_comp_));
       KH_TRY(upload_raw(ent_amp.data(), ent_amp.size() * sizeof(Cplx<T>), (void**)&ent_amp_));
+      ent_amp_h_ = ent_amp;
       KH_TRY(upload_raw(slot_cell.data(), slot_cell.size() * sizeof(long long), (void**)&slot_cell_));
       nslots_ = int(slot_cell.size());
     }
@@ -418,6 +455,8 @@ class Sim : public SimBase {
       KH_TRY(alloc_raw(bytes, (void**)&m.F, true));
       if (sizeof(T) == 4) KH_TRY(alloc_raw(bytes, (void**)&m.C, true));
     }
+    for (auto& h : hists_)
+      KH_TRY(alloc_raw(size_t(h.ncell) * size_t(h.cap) * sizeof(T), (void**)&h.buf, false));
     // last_source_time (TimeSources.jl:40-47); a CW source never cuts off.
     has_cw_ = false;
     last_time_ = -INFINITY;
@@ -520,6 +559,7 @@ class Sim : public SimBase {
       b += cnt * (sizeof(T) == 4 ? 2 : 1);
     }
     b += 2 * int64_t(table_capacity() * sizeof(Cplx<T>)) + int64_t(sizeof(int));
+    for (auto& h : hists_) b += h.ncell * h.cap * int64_t(sizeof(T));
     return b;
   }
 
@@ -619,6 +659,108 @@ class Sim : public SimBase {
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpy(out, scratch, sizeof(double) * nf, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return fail(KH_ERR_CUDA, cudaGetErrorString(e));
+    return KH_OK;
+  }
+
+  // Design update: per-voxel ε⁻¹ (or μ⁻¹) of one component in a cell box,
+  // values x fastest over the box.  Cell classes do not depend on these
+  // values, so nothing else is rebuilt.
+  kh_status update_material_box(int kind, int comp, const int32_t* st, const int32_t* dm,
+                                const double* v) override {
+    if (!prepared_) return fail(KH_ERR_INVALID, "update_material_box before prepare");
+    if (!st || !dm || !v) return fail(KH_ERR_INVALID, "null update_material_box argument");
+    if (comp < 0 || comp > 2) return fail(KH_ERR_INVALID, "material component must be 0..2");
+    T* dst = nullptr;
+    std::vector<T>* host = nullptr;
+    if (kind == KH_MAT_EPS_INV) { dst = eps_[comp]; host = &eps_h_[comp]; }
+    else if (kind == KH_MAT_MU_INV) { dst = mu_[comp]; host = &mu_h_[comp]; }
+    else return fail(KH_ERR_UNSUPPORTED, "only ε⁻¹ and μ⁻¹ can be updated after prepare");
+    if (!dst) return fail(KH_ERR_INVALID, "no per-voxel array of this kind was set before prepare");
+    for (int a = 0; a < 3; ++a)
+      if (dm[a] <= 0 || st[a] < 0 || st[a] + dm[a] > n_[a]) return fail(KH_ERR_INVALID, "box outside the grid");
+    if (kh_status es = wait_idle(); es != KH_OK) return es;
+    std::vector<T> plane(size_t(dm[0]) * dm[1]);
+    for (int k = 0; k < dm[2]; ++k) {
+      for (int j = 0; j < dm[1]; ++j)
+        for (int i = 0; i < dm[0]; ++i) {
+          const T val = T(v[(size_t(k) * dm[1] + j) * dm[0] + i]);
+          plane[size_t(j) * dm[0] + i] = val;
+          (*host)[(size_t(st[2] + k) * n_[1] + (st[1] + j)) * n_[0] + (st[0] + i)] = val;
+        }
+      T* row0 = dst + origin_ + (long long)(st[2] + k) * plane_ + (long long)st[1] * pitch_ + st[0];
+      KH_CUDA(cudaMemcpy2D(row0, size_t(pitch_) * sizeof(T), plane.data(), size_t(dm[0]) * sizeof(T),
+                           size_t(dm[0]) * sizeof(T), size_t(dm[1]), cudaMemcpyHostToDevice));
+    }
+    return KH_OK;
+  }
+
+  // Replace source `index`'s amplitudes (the cells it injects into stay the
+  // same: an element that was zero at prepare must stay zero) and, for a
+  // KH_TIME_TABLE source, its table and end time.
+  kh_status update_source(int index, const double* amp, int64_t table_len, const double* table,
+                          double cutoff) override {
+    if (!prepared_) return fail(KH_ERR_INVALID, "update_source before prepare");
+    if (index < 0 || index >= int(srcs_.size())) return fail(KH_ERR_INVALID, "bad source index");
+    SrcH& s = srcs_[index];
+    if (table && s.d.time_kind != KH_TIME_TABLE)
+      return fail(KH_ERR_INVALID, "a time table can only replace a KH_TIME_TABLE profile");
+    if (table && table_len < 0) return fail(KH_ERR_INVALID, "negative table length");
+    const size_t cnt = size_t(s.d.dims[0]) * s.d.dims[1] * s.d.dims[2];
+    std::vector<Cplx<T>> amp_new = ent_amp_h_;
+    if (amp) {
+      std::vector<int> where(cnt, -1);
+      for (auto& pe : src_ent_[index]) where[size_t(pe.first)] = pe.second;
+      for (size_t q = 0; q < cnt; ++q) {
+        const Cplx<T> a{T(amp[2 * q]), T(amp[2 * q + 1])};
+        if (where[q] >= 0) amp_new[size_t(where[q])] = a;
+        else if (a.re != T(0) || a.im != T(0))
+          return fail(KH_ERR_INVALID, "update_source: nonzero amplitude outside the source's prepared cells");
+      }
+    }
+    if (kh_status es = wait_idle(); es != KH_OK) return es;
+    if (amp) {
+      for (size_t q = 0; q < cnt; ++q) s.amp[q] = std::complex<double>(amp[2 * q], amp[2 * q + 1]);
+      if (!amp_new.empty())
+        KH_CUDA(cudaMemcpy(ent_amp_, amp_new.data(), amp_new.size() * sizeof(Cplx<T>), cudaMemcpyHostToDevice));
+      ent_amp_h_.swap(amp_new);
+    }
+    if (table) {
+      s.table.assign(size_t(2 * table_len), std::complex<T>(T(0), T(0)));
+      for (int64_t q = 0; q < 2 * table_len; ++q)
+        s.table[size_t(q)] = std::complex<T>(T(table[2 * q]), T(table[2 * q + 1]));
+      s.d.table_len = table_len;
+      s.d.cutoff = cutoff;
+      has_cw_ = false;
+      last_time_ = -INFINITY;
+      for (auto& x : srcs_) {
+        if (x.d.time_kind == KH_TIME_CW) has_cw_ = true;
+        else last_time_ = std::max(last_time_, double(T(x.d.cutoff)));
+      }
+    }
+    return KH_OK;
+  }
+
+  kh_status monitor_view(int id, kh_host::MonitorView* out) override {
+    if (!prepared_) return fail(KH_ERR_INVALID, "monitor read before prepare");
+    if (id < 0 || id >= int(mons_.size()) || !out) return fail(KH_ERR_INVALID, "bad monitor id");
+    const Mon& m = mons_[id];
+    out->F = m.F;
+    out->C = m.C;
+    for (int a = 0; a < 3; ++a) out->dims[a] = m.dims[a];
+    out->nf = m.nf;
+    out->dtype = sizeof(T) == 4 ? KH_F32 : KH_F64;
+    return KH_OK;
+  }
+
+  int dtype() const override { return sizeof(T) == 4 ? KH_F32 : KH_F64; }
+
+  kh_status field_arrays(const void* out[6], long long* count) override {
+    if (!prepared_) return fail(KH_ERR_INVALID, "field read before prepare");
+    for (int c = 0; c < 3; ++c) {
+      out[c] = E_[c];
+      out[3 + c] = H_[c];
+    }
+    *count = total_;
     return KH_OK;
   }
 
@@ -780,6 +922,12 @@ class Sim : public SimBase {
     kh_source_desc d;
     std::vector<std::complex<double>> amp;
     std::vector<std::complex<T>> table;
+  };
+  struct Hist {
+    int comp, start[3], dims[3];
+    long long ncell = 0;
+    int64_t cap = 0;
+    T* buf = nullptr;
   };
   struct Mon {
     int comp, start[3], dims[3], nf, dec;
@@ -1000,6 +1148,7 @@ class Sim : public SimBase {
       }
       mark(s, 1);
       for (auto& dm : P.dftH) launch_dft_for(dm.first, dtab + dm.second, stream);
+      record_histories(true, timestep_ + s, stream);
       mark(s, 2);
       pe.sources_active = P.sa ? 1 : 0;
       pe.f_now = dtab + P.fE;
@@ -1015,6 +1164,7 @@ class Sim : public SimBase {
       }
       mark(s, 3);
       for (auto& dm : P.dftE) launch_dft_for(dm.first, dtab + dm.second, stream);
+      record_histories(false, timestep_ + s, stream);
       mark(s, 4);
     }
     cudaError_t e = cudaGetLastError();
@@ -1037,6 +1187,26 @@ class Sim : public SimBase {
       }
     }
     return KH_OK;
+  }
+
+  // History monitors of one half: the component values after that half-step
+  // of step `ts` go to slot ts (steps past the capacity are not recorded).
+  void record_histories(bool h_half, int64_t ts, cudaStream_t stream) {
+    for (auto& h : hists_) {
+      if ((h.comp >= 3) != h_half || ts >= h.cap) continue;
+      kh::RecordParams<T> p;
+      p.field = h.comp < 3 ? E_[h.comp] : H_[h.comp - 3];
+      p.pitch = pitch_;
+      p.plane = plane_;
+      p.origin = origin_;
+      for (int a = 0; a < 3; ++a) {
+        p.start[a] = h.start[a];
+        p.dims[a] = h.dims[a];
+      }
+      p.dst = h.buf + ts * h.ncell;
+      kh::launch_record<T>(p, stream);
+      ++launches;
+    }
   }
 
   void launch_dft_for(int mi, const Cplx<T>* phase, cudaStream_t stream) {
@@ -1226,6 +1396,7 @@ class Sim : public SimBase {
   std::vector<PoleD> poles_d_;
   std::vector<SrcH> srcs_;
   std::vector<Mon> mons_;
+  std::vector<Hist> hists_;
   int nsrc_ = 0;
   bool has_src_[2] = {false, false};         // [E half, H half]
   bool src_fix_ok_[2] = {true, true};
@@ -1248,6 +1419,9 @@ class Sim : public SimBase {
   uint64_t *tbits_e_ = nullptr, *tbits_h_ = nullptr;
   int *slot_off_ = nullptr, *ent_src_ = nullptr, *ent_comp_ = nullptr;
   Cplx<T>* ent_amp_ = nullptr;
+  std::vector<Cplx<T>> ent_amp_h_;  // host copy of ent_amp_
+  // per source: (amplitude element index, entry index) of every injected cell
+  std::vector<std::vector<std::pair<long long, int>>> src_ent_;
 
   void* tab_dev_[2] = {nullptr, nullptr};
   void* pinned_[2] = {nullptr, nullptr};
@@ -1431,6 +1605,24 @@ kh_status kh_sim_model_bytes_per_step(const kh_sim* sim, double* out) {
   if (!sim || !out) return KH_ERR_INVALID;
   *out = sim->impl->model_bytes_per_step();
   return KH_OK;
+}
+
+kh_status kh_sim_add_history_monitor(kh_sim* sim, int32_t component, const int32_t start[3],
+                                     const int32_t dims[3], int64_t capacity_steps, int32_t* out_id) {
+  if (!sim) return KH_ERR_INVALID;
+  return sim->impl->add_history(component, start, dims, capacity_steps, out_id);
+}
+
+kh_status kh_sim_update_material_box(kh_sim* sim, int32_t kind, int32_t comp, const int32_t start[3],
+                                     const int32_t dims[3], const double* values) {
+  if (!sim) return KH_ERR_INVALID;
+  return sim->impl->update_material_box(kind, comp, start, dims, values);
+}
+
+kh_status kh_sim_update_source(kh_sim* sim, int32_t index, const double* amp, int64_t table_len,
+                               const double* table, double cutoff) {
+  if (!sim) return KH_ERR_INVALID;
+  return sim->impl->update_source(index, amp, table_len, table, cutoff);
 }
 
 }  // extern "C"

@@ -12,6 +12,29 @@
 
 namespace kh_host {
 
+// Device view of one DFT monitor: accumulators F[f·ncell + cell] (cell x
+// fastest over the monitor box) and, for FP32 runs, the Kahan compensation
+// C (value = F − C); C is null in FP64 runs.
+struct MonitorView {
+  const void* F = nullptr;
+  const void* C = nullptr;
+  int dims[3] = {0, 0, 0};
+  int nf = 0;
+  int dtype = KH_F32;
+  long long ncell() const { return (long long)dims[0] * dims[1] * dims[2]; }
+};
+
+// Device view of one history monitor: field values of one component over a
+// cell box at every step, buf[step·ncell + cell] (cell x fastest), `recorded`
+// steps valid (0 ≤ step < recorded).
+struct HistoryView {
+  const void* buf = nullptr;
+  int dims[3] = {0, 0, 0};
+  long long ncell = 0;
+  int64_t capacity = 0, recorded = 0;
+  int dtype = KH_F32;
+};
+
 struct SimBase {
   virtual ~SimBase() = default;
   std::string err;
@@ -46,6 +69,21 @@ struct SimBase {
   virtual void model_split(double& h, double& e, double& dft) const = 0;
   virtual kh_status step_timed(int64_t n, cudaStream_t s, double* h_ms, double* e_ms,
                                double* dft_ms) = 0;
+  // After prepare: overwrite per-voxel ε⁻¹/μ⁻¹ in a cell box; replace one
+  // source's amplitudes (same footprint) and time table.
+  virtual kh_status update_material_box(int kind, int comp, const int32_t* st, const int32_t* dm,
+                                        const double* v) = 0;
+  virtual kh_status update_source(int index, const double* amp, int64_t table_len,
+                                  const double* table, double cutoff) = 0;
+  // Device arrays of a monitor, valid once this simulation's queued work is done.
+  virtual kh_status monitor_view(int id, MonitorView* out) = 0;
+  virtual int dtype() const = 0;
+  // Device arrays of E_x..E_z, H_x..H_z (padded layout, `count` elements each,
+  // zero outside the grid), valid once this simulation's queued work is done.
+  virtual kh_status field_arrays(const void* out[6], long long* count) = 0;
+  virtual kh_status add_history(int comp, const int32_t* st, const int32_t* dm, int64_t capacity,
+                                int32_t* id) = 0;
+  virtual kh_status history_view(int id, HistoryView* out) = 0;
 };
 
 }  // namespace kh_host

@@ -74,6 +74,14 @@ class GpuSim:
                 self._check(self.lib.kh_sim_add_dft_monitor(self.handle, m.component, st, dm, len(fr),
                                                             _dptr(fr), int(m.decimation), C.byref(mid)))
                 self.monitor_ids.append(mid.value)
+            self.history_ids: List[int] = []
+            for h in spec.histories:
+                st = (C.c_int32 * 3)(*h.start)
+                dm = (C.c_int32 * 3)(*h.dims)
+                hid = C.c_int32()
+                self._check(self.lib.kh_sim_add_history_monitor(self.handle, h.component, st, dm,
+                                                                int(h.capacity), C.byref(hid)))
+                self.history_ids.append(hid.value)
             if prepare:
                 self._check(self.lib.kh_sim_prepare(self.handle))
         except Exception:
@@ -167,6 +175,72 @@ class GpuSim:
         self._check(self.lib.kh_sim_step_timed(self.handle, int(nsteps), C.c_void_p(stream) if stream else None,
                                                C.byref(h), C.byref(e), C.byref(d)))
         return h.value, e.value, d.value
+
+    def field_sq_norms(self) -> np.ndarray:
+        """Σ E_c², Σ H_c² over the grid (6 values, FP64 on the device)."""
+        out = np.zeros(6)
+        self._check(self.lib.kh_sim_field_sq_norms(self.handle, _dptr(out)))
+        return out
+
+    # -- adjoint support -------------------------------------------------------
+    def update_material_box(self, kind: int, comp: int, start, values: np.ndarray):
+        """Overwrite per-voxel ε⁻¹/μ⁻¹ of one component over the cell box
+        start..start+values.shape-1 (values indexed [i, j, k])."""
+        v = flat_f(values)
+        st = (C.c_int32 * 3)(*[int(s) for s in start])
+        dm = (C.c_int32 * 3)(*[int(d) for d in np.shape(values)])
+        self._check(self.lib.kh_sim_update_material_box(self.handle, int(kind), int(comp), st, dm, _dptr(v)))
+
+    def update_source(self, index: int, amp: Optional[np.ndarray] = None, table: Optional[np.ndarray] = None,
+                      cutoff: float = 0.0):
+        """Replace source ``index``'s amplitude array (same footprint) and/or
+        its time table ((steps, 2) complex: f(nΔt), f(nΔt + Δt/2))."""
+        a = flat_complex(amp) if amp is not None else None
+        t = flat_complex(np.asarray(table).reshape(-1)) if table is not None else None
+        n = int(np.asarray(table).shape[0]) if table is not None else 0
+        self._check(self.lib.kh_sim_update_source(self.handle, int(index), _dptr(a) if a is not None else None,
+                                                  n, _dptr(t) if t is not None else None, float(cutoff)))
+
+    def dft_overlap(self, monitor_index: int, weights: np.ndarray) -> np.ndarray:
+        """Σ_cells weights·F per frequency, FP64 on the device; weights has the
+        monitor's DFT shape (Nx, Ny, Nz, Nf)."""
+        m = self.spec.monitors[monitor_index]
+        shape = tuple(m.dims) + (len(m.freqs),)
+        w = np.asarray(weights, dtype=np.complex128)
+        if w.shape != shape:
+            raise ValueError(f"weights shape {w.shape} != monitor shape {shape}")
+        wf = flat_complex(w)
+        out = np.zeros(2 * len(m.freqs))
+        self._check(self.lib.kh_sim_dft_overlap(self.handle, self.monitor_ids[monitor_index], _dptr(wf), _dptr(out)))
+        return out[0::2] + 1j * out[1::2]
+
+    def adjoint_accumulate(self, fwd_monitors, fwd_freq: int, adj: "GpuSim", adj_monitors, adj_freq: int,
+                           coef: complex, grad: np.ndarray):
+        """grad += Re(coef·Σ_c F_c·A_c) per design voxel (FP64 on the device);
+        grad is a float64 array over the design box, indexed [i, j, k]."""
+        fi = (C.c_int32 * 3)(*[self.monitor_ids[i] for i in fwd_monitors])
+        ai = (C.c_int32 * 3)(*[adj.monitor_ids[i] for i in adj_monitors])
+        flat = np.ascontiguousarray(grad.ravel(order="F"))
+        self._check(self.lib.kh_adjoint_accumulate(self.handle, fi, int(fwd_freq), adj.handle, ai, int(adj_freq),
+                                                   float(np.real(coef)), float(np.imag(coef)), _dptr(flat)))
+        grad[...] = flat.reshape(grad.shape, order="F")
+
+    def history(self, index: int, step: int) -> np.ndarray:
+        """Recorded values of history monitor ``index`` at ``step``, indexed [i, j, k]."""
+        h = self.spec.histories[index]
+        out = np.zeros(int(np.prod(h.dims)))
+        self._check(self.lib.kh_sim_read_history(self.handle, self.history_ids[index], int(step), _dptr(out)))
+        return out.reshape(tuple(h.dims), order="F")
+
+    def history_correlate(self, fwd_histories, adj: "GpuSim", adj_histories, nsteps: int, coef: float,
+                          grad: np.ndarray):
+        """grad += coef·Σ_c Σ_m F_c[m]·A_c[N−1−m] per box cell (FP64 on the device)."""
+        fi = (C.c_int32 * 3)(*[self.history_ids[i] for i in fwd_histories])
+        ai = (C.c_int32 * 3)(*[adj.history_ids[i] for i in adj_histories])
+        flat = np.ascontiguousarray(grad.ravel(order="F"))
+        self._check(self.lib.kh_history_correlate(self.handle, fi, adj.handle, ai, int(nsteps), float(coef),
+                                                  _dptr(flat)))
+        grad[...] = flat.reshape(grad.shape, order="F")
 
     # -- state ----------------------------------------------------------------
     def reset(self):

@@ -85,6 +85,16 @@ class MonitorSpec:
 
 
 @dataclass
+class HistorySpec:
+    """A history monitor: ``component`` over a cell box at every step < capacity."""
+
+    component: int
+    start: Tuple[int, int, int]
+    dims: Tuple[int, int, int]
+    capacity: int
+
+
+@dataclass
 class PoleSpec:
     coeffs: dict
     sigma: np.ndarray               # (nx, ny, nz) oscillator strength per voxel
@@ -107,6 +117,7 @@ class SimSpec:
     poles: List[PoleSpec] = field(default_factory=list)
     sources: List[SourceSpec] = field(default_factory=list)
     monitors: List[MonitorSpec] = field(default_factory=list)
+    histories: List[HistorySpec] = field(default_factory=list)
 
     @property
     def np_dtype(self):

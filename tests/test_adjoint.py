@@ -1,0 +1,345 @@
+"""Adjoint gradients: host logic and the method on the CPU oracle; the CUDA
+path (design/source updates, FP64 overlap and gradient reductions, the
+OptimizationProblem driver, the autograd rrule) on the GPU.
+
+Bars written in the tests:
+* adjoint gradient vs central finite differences (δρ = 1e-3, FP64): 1e-3
+  relative per voxel;
+* CUDA FP64 gradient vs the oracle restatement of the same method: 1e-9
+  relative to the largest gradient entry;
+* updated design / sources vs a freshly built simulation: bit-for-bit;
+* FP32 gradient vs FP64 gradient: relative L2 reported and held under 1e-3.
+"""
+import copy
+import math
+
+import numpy as np
+import pytest
+
+from adjoint_case import make_problem
+
+FD_TOL = 1e-3
+
+
+# ---------------------------------------------------------------- host logic
+@pytest.mark.parametrize("T", [np.float32, np.float64])
+def test_quadrature_table_is_exact_at_its_frequency(kh, T):
+    """Re(a·(g + iq)) carries the complex amplitude a exactly at ω: the DFT of
+    q is −i times the DFT of g there (with the device's phase factors)."""
+    from khronos_gb300.adjoint import adjoint_time_table
+
+    f, dt, steps = 0.62, 0.0333, 2000
+    tab, cutoff, S_hat = adjoint_time_table(f, dt, steps, T)
+    g, q = tab[:, 1].real, tab[:, 1].imag
+    assert np.all(tab[:, 0] == 0)
+    Tt = np.dtype(T).type
+    t = np.array([Tt(Tt(k) * Tt(dt)) for k in range(steps)], dtype=np.float64) + float(Tt(dt) / Tt(2))
+    ph = np.exp(1j * 2 * math.pi * float(Tt(f)) * t) * float(Tt(dt))
+    G, Q = np.sum(ph * g), np.sum(ph * q)
+    tol = 1e-10 if T is np.float64 else 1e-5
+    assert abs(Q + 1j * G) <= tol * abs(G)
+    assert abs(S_hat - G) <= (1e-12 if T is np.float64 else 1e-6) * abs(G)
+    assert cutoff > 0 and np.max(np.abs(g[t > cutoff])) == 0
+
+
+def test_wirtinger_under_no_grad(kh):
+    """Inside an autograd.Function forward grad mode is off; the exact
+    autograd derivative must still be used."""
+    torch = pytest.importorskip("torch")
+    from khronos_gb300.adjoint import power_overlap, wirtinger
+
+    Y = [np.array([1 + 2j, -0.5 + 0.25j])]
+    with torch.no_grad():
+        _, G = wirtinger(power_overlap, Y)
+    assert np.array_equal(G[0], 2 * Y[0])
+
+
+def test_wirtinger_torch_matches_numeric(kh):
+    pytest.importorskip("torch")
+    from khronos_gb300.adjoint import power_overlap, wirtinger
+
+    Y = [np.array([1 + 2j, -0.5 + 0.25j]), np.array([3 - 1j])]
+    J, G = wirtinger(power_overlap, Y)
+    assert J == pytest.approx(5 + 0.3125 + 10)
+    np.testing.assert_allclose(G[0], 2 * Y[0])
+    np.testing.assert_allclose(G[1], 2 * Y[1])
+
+    def cubic(y):
+        return (y.real ** 3 - 2 * y.imag * y.real).sum()
+
+    Jn, Gn = wirtinger(lambda y: np.real(cubic(np.asarray(y))), [Y[0]])
+    Jt, Gt = wirtinger(cubic, [Y[0]])
+    assert Jn == pytest.approx(Jt)
+    np.testing.assert_allclose(Gn[0], Gt[0], rtol=1e-6)
+
+
+@pytest.mark.parametrize("mode", ["time", "dft"])
+def test_problem_specs(kh, mode):
+    """Forward spec gains decimation-1 objective monitors and design-box
+    monitors (history monitors in "time" mode, DFT monitors in "dft" mode);
+    the adjoint spec keeps the materials, drops the forward sources and
+    places table sources on the objective cells (one per component and
+    frequency in "time" mode, one per component in "dft" mode)."""
+    from khronos_gb300.spec import TIME_TABLE
+
+    opt, _ = make_problem("f64", 100, 3, small=True, mode=mode)
+    fs, as_ = opt.fwd_spec, opt.adj_spec
+    assert len(fs.sources) == len(opt.base.sources) > 0
+    assert all(m.decimation == 1 for m in fs.monitors)
+    nsrc = 9 if mode == "time" else 3
+    assert len(as_.sources) == nsrc and all(s.time_kind == TIME_TABLE for s in as_.sources)
+    assert sorted({s.component for s in as_.sources}) == [0, 1, 2]
+    assert as_.materials is opt.base.materials
+    if mode == "time":
+        assert len(fs.monitors) == 3 and len(fs.histories) == 3 and len(as_.histories) == 3
+        assert all(h.capacity == 100 and h.dims == opt.design_region.dims for h in fs.histories)
+        assert opt.history_bytes() == 2 * 3 * 48 * 100 * 8
+    else:
+        assert len(fs.monitors) == 6 and len(as_.monitors) == 3 and not fs.histories
+        assert [fs.monitors[i].dims for i in opt._fwd_design] == [opt.design_region.dims] * 3
+
+
+@pytest.mark.parametrize("mode,steps", [("time", 700), ("dft", 3500)])
+def test_adjoint_method_on_the_oracle(kh, oracle, mode, steps):
+    """The reciprocity adjoint restated on the CPU oracle (FP64) equals central
+    finite differences of the oracle's own forward runs: "time" mode on a
+    700-step run whose fields have not decayed, "dft" mode once they have."""
+    import oracle.adjoint as oadj
+
+    opt, rho = make_problem("f64", steps, 2, small=True, mode=mode)
+    g, per = oadj.gradient(opt, rho)
+    if per is not None:
+        assert np.allclose(per.sum(axis=0), g)
+    idx = [(0, 0, 0), (2, 3, 1), (3, 3, 2)]
+    fd = oadj.fd_gradient(opt, rho, idx)
+    for i, f in zip(idx, fd):
+        assert abs(g[i] - f) <= FD_TOL * abs(f), (i, g[i], f)
+
+
+# ------------------------------------------------------------------- GPU path
+def _fresh_fields(spec, steps, lib):
+    from khronos_gb300.device import GpuSim
+
+    s = GpuSim(spec, lib=lib)
+    s.step(steps)
+    out = [s.field(c) for c in range(6)], [s.dft(m) for m in range(len(spec.monitors))]
+    s.close()
+    return out
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dtype", ["f32", "f64"])
+def test_update_material_box_matches_fresh(kh, gpu_lib, dtype):
+    import oracle.adjoint as oadj
+    from khronos_gb300.device import GpuSim
+    from khronos_gb300.spec import MAT_EPS_INV
+
+    opt, rho = make_problem(dtype, 300, 2, small=True)
+    ref_f, ref_d = _fresh_fields(oadj._with_design(opt.fwd_spec, opt, rho), 300, gpu_lib)
+    s = GpuSim(oadj._with_design(opt.fwd_spec, opt, np.full_like(rho, 0.5)), lib=gpu_lib)
+    s.step(57)
+    einv = opt.design_region.eps_inv(rho)
+    for c in range(3):
+        s.update_material_box(MAT_EPS_INV, c, opt.design_region.start, einv)
+    s.reset()
+    s.step(300)
+    for c in range(6):
+        assert np.array_equal(s.field(c), ref_f[c])
+    for m in range(len(ref_d)):
+        assert np.array_equal(s.dft(m), ref_d[m])
+    with pytest.raises(Exception, match="outside"):
+        s.update_material_box(MAT_EPS_INV, 0, (1000, 0, 0), einv)
+    s.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dtype", ["f32", "f64"])
+def test_update_source_matches_fresh(kh, gpu_lib, dtype):
+    from khronos_gb300.adjoint import adjoint_time_table
+    from khronos_gb300.device import GpuSim
+
+    opt, rho = make_problem(dtype, 400, 2, small=True)
+    tab, cutoff, _ = adjoint_time_table(opt.frequencies[1], float(opt.base.dt), 400, opt._np_T())
+    rng = np.random.default_rng(11)
+    spec = copy.copy(opt.adj_spec)
+    spec.sources = [copy.copy(s) for s in opt.adj_spec.sources]
+    amps = []
+    for s in spec.sources:
+        a = rng.normal(size=s.dims) + 1j * rng.normal(size=s.dims)
+        a[0, 0, 0] = 0  # a zero inside the footprint is allowed
+        amps.append(a)
+        s.amp, s.table, s.cutoff = a, tab, cutoff
+    ref_f, ref_d = _fresh_fields(spec, 400, gpu_lib)
+    g = GpuSim(opt.adj_spec, lib=gpu_lib)
+    g.step(10)
+    for i, a in enumerate(amps):
+        g.update_source(i, amp=a, table=tab, cutoff=cutoff)
+    g.reset()
+    g.step(400)
+    for c in range(6):
+        assert np.array_equal(g.field(c), ref_f[c])
+    for m in range(len(ref_d)):
+        assert np.array_equal(g.dft(m), ref_d[m])
+    g.close()
+    # the footprint is fixed at prepare: a source prepared with a zero cell
+    # rejects a nonzero amplitude there
+    h = GpuSim(spec, lib=gpu_lib)
+    with pytest.raises(Exception, match="outside the source"):
+        h.update_source(0, amp=np.ones(spec.sources[0].dims, dtype=np.complex128))
+    h.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dtype", ["f32", "f64"])
+def test_dft_overlap_matches_host(kh, gpu_lib, dtype):
+    from khronos_gb300.device import GpuSim
+
+    opt, _ = make_problem(dtype, 200, 3)
+    s = GpuSim(opt.fwd_spec, lib=gpu_lib)
+    s.step(200)
+    rng = np.random.default_rng(5)
+    for mid in opt._obj_ids[0] + opt._fwd_design:
+        F = s.dft(mid)
+        w = rng.normal(size=F.shape) + 1j * rng.normal(size=F.shape)
+        got = s.dft_overlap(mid, w)
+        ref = np.einsum("xyzf,xyzf->f", F, w)
+        np.testing.assert_allclose(got, ref, rtol=1e-11, atol=1e-11 * np.max(np.abs(ref)))
+    with pytest.raises(ValueError):
+        s.dft_overlap(opt._fwd_design[0], np.zeros((1, 1, 1, 3)))
+    s.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dtype", ["f32", "f64"])
+def test_history_monitor_records_fields(kh, gpu_lib, dtype):
+    """A history slot holds the component over its box right after that
+    step, bit for bit; reset restarts recording at step 0."""
+    from khronos_gb300.device import GpuSim
+
+    opt, rho = make_problem(dtype, 30, 2, small=True)
+    sp = opt.fwd_spec
+    s = GpuSim(sp, lib=gpu_lib)
+    dr = opt.design_region
+    sl = tuple(slice(dr.start[a], dr.start[a] + dr.dims[a]) for a in range(3))
+    snaps = []
+    for n in range(30):
+        s.step(1)
+        snaps.append([s.field(c)[sl] for c in range(3)])
+    for n in (0, 7, 29):
+        for c in range(3):
+            assert np.array_equal(s.history(c, n), snaps[n][c])
+    with pytest.raises(Exception, match="not recorded"):
+        s.history(0, 30)
+    s.reset()
+    s.step(5)
+    assert np.array_equal(s.history(1, 4), snaps[4][1])
+    with pytest.raises(Exception, match="not recorded"):
+        s.history(1, 5)
+    s.close()
+
+
+@pytest.mark.gpu
+def test_history_correlate_matches_host(kh, gpu_lib):
+    from khronos_gb300.device import GpuSim
+
+    opt, rho = make_problem("f64", 40, 2, small=True)
+    a = GpuSim(opt.fwd_spec, lib=gpu_lib)
+    b = GpuSim(opt.fwd_spec, lib=gpu_lib)
+    a.step(40)
+    b.step(25)
+    b.reset()
+    b.step(33)  # a second, different-length record
+    N = 33
+    g = np.full(opt.design_region.dims, 0.5)
+    a.history_correlate([0, 1, 2], b, [0, 1, 2], N, -2.0, g)
+    ref = np.full(opt.design_region.dims, 0.5)
+    for c in range(3):
+        for m in range(N):
+            ref += -2.0 * a.history(c, m) * b.history(c, N - 1 - m)
+    np.testing.assert_allclose(g, ref, rtol=1e-12, atol=1e-12 * np.max(np.abs(ref)))
+    with pytest.raises(Exception, match="fewer steps"):
+        a.history_correlate([0, 1, 2], b, [0, 1, 2], 34, 1.0, g)
+    a.close()
+    b.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode,steps", [("time", 600), ("dft", 1500)])
+def test_adjoint_gradient_matches_oracle(kh, oracle, gpu_lib, mode, steps):
+    """CUDA FP64 adjoint gradient == the oracle restatement (same method)."""
+    import oracle.adjoint as oadj
+
+    opt, rho = make_problem("f64", steps, 3, lib=gpu_lib, small=True, mode=mode)
+    f0, g = opt(rho)
+    f_ref = oadj.objective(opt, rho)
+    g_ref, _ = oadj.gradient(opt, rho)
+    assert abs(f0 - f_ref) <= 1e-10 * abs(f_ref)
+    assert np.max(np.abs(g - g_ref)) <= 1e-9 * np.max(np.abs(g_ref))
+    assert opt.current_state == "ADJ"
+    opt.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode,steps", [("time", 1500), ("dft", 6000)])
+def test_adjoint_gradient_vs_finite_differences(kh, gpu_lib, mode, steps):
+    """FP64 CUDA adjoint vs central FD of the CUDA forward run, 6 voxels
+    ("time" mode on a run whose fields have not decayed)."""
+    opt, rho = make_problem("f64", steps, 3, lib=gpu_lib, mode=mode)
+    _, g = opt(rho)
+    g = g.copy()
+    rng = np.random.default_rng(99)
+    idx = [tuple(int(rng.integers(0, d)) for d in opt.design_region.dims) for _ in range(6)]
+    fd = opt.calculate_fd_gradient(rho, idx)
+    for i, f in zip(idx, fd):
+        assert abs(g[i] - f) <= FD_TOL * abs(f), (i, g[i], f)
+    opt.close()
+
+
+@pytest.mark.gpu
+def test_adjoint_f32_against_f64(kh, gpu_lib):
+    """FP32 bulk + Kahan DFT gradient against the FP64 gradient of the same inputs."""
+    o64, rho = make_problem("f64", 2000, 3, lib=gpu_lib)
+    o32, _ = make_problem("f32", 2000, 3, lib=gpu_lib)
+    f64, g64 = o64(rho)
+    f32, g32 = o32(rho)
+    rel = np.linalg.norm(g32 - g64) / np.linalg.norm(g64)
+    assert abs(f32 - f64) <= 1e-4 * abs(f64)
+    assert rel <= 1e-3, rel
+    o64.close()
+    o32.close()
+
+
+@pytest.mark.gpu
+def test_simulate_rrule(kh, gpu_lib):
+    """torch autograd through simulate() runs the adjoint in the backward pass."""
+    torch = pytest.importorskip("torch")
+    from khronos_gb300.adjoint import simulate
+
+    opt, rho = make_problem("f64", 600, 2, lib=gpu_lib, small=True)
+    r = torch.tensor(rho, dtype=torch.float64, requires_grad=True)
+    J = simulate(opt, r)
+    (2.0 * J).backward()
+    f0, g = opt(rho)
+    assert float(J.detach()) == pytest.approx(f0, rel=1e-12)
+    np.testing.assert_allclose(r.grad.numpy(), 2.0 * g, rtol=1e-12, atol=1e-12 * np.max(np.abs(g)))
+    opt.close()
+
+
+@pytest.mark.gpu
+def test_bend_workload_small(kh, gpu_lib):
+    """The waveguide-bend workload at reduced resolution: E_ref from the
+    straight run, FP64 windowed adjoint vs finite differences on 3 voxels."""
+    from khronos_gb300 import configs
+    from khronos_gb300.adjoint import bend_problem
+
+    w = configs.bend(dtype="f64", steps=2500, scale=0.25)
+    opt = bend_problem(w, lib=gpu_lib)
+    f0, g = opt(w.rho0)
+    g = g.copy()
+    assert f0 > 0 and np.all(np.isfinite(g))
+    rng = np.random.default_rng(99)
+    idx = [tuple(int(rng.integers(0, d)) for d in w.design_dims) for _ in range(3)]
+    fd = opt.calculate_fd_gradient(w.rho0, idx)
+    for i, f in zip(idx, fd):
+        assert abs(g[i] - f) <= FD_TOL * abs(f), (i, g[i], f)
+    opt.close()
