@@ -119,11 +119,20 @@ def ncu_traffic(kernel: str):
     return None if v is None else float(v)
 
 
+WORKLOADS = {
+    "waveguide": WORKLOAD,
+    "dispersive": ("dispersive 256^3 FP32, 12-cell CPML (CUDA-path semantics), eps 2.25 slab with chi3=1e-3, "
+                   "4 Lorentz (eps_inf 2, sigma 1, f0 1, gamma 0.05) + 4 Drude (eps_inf 1, wp 5, gamma 0.1) "
+                   "spheres (seed 42), Ez Gaussian plane source, 6-face box flux x 11 freqs, Kahan FP32 DFT"),
+}
+_workload_name = "waveguide"
+
+
 def build_workload(dtype="f32", semantics="cpml"):
     __graft_entry__.package()
     from khronos_gb300 import configs
 
-    w = configs.waveguide(dtype=dtype)
+    w = configs.BUILDERS[_workload_name](dtype=dtype)
     w.sim.semantics = semantics
     return w, w.sim.spec()
 
@@ -166,7 +175,8 @@ def run_reference(args, world, rank):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": k, "warmup": args.warmup, "ms_per_step": dt / k * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD.replace("CUDA-path semantics", "reference CPU-path semantics"),
+        "config": {"workload": WORKLOADS[_workload_name].replace("CUDA-path semantics",
+                                                                  "reference CPU-path semantics"),
                    "grid": list(spec.n), "note": "reference is Julia (absent); timed: its CPU step loop "
                                                  "restated in C++ (oracle/), all host threads"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": orc.num_threads(), "kind": "port",
@@ -238,13 +248,13 @@ def run_ours(args, world, rank, local_rank):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "grid": list(spec.n), "cells": cells,
+        "config": {"workload": WORKLOADS[_workload_name], "grid": list(spec.n), "cells": cells,
                    "l2": "inputs larger than L2 (fields+materials+CPML state ~0.9 GB per replica vs 129 MB L2); no flush",
                    "parallelism": f"replicas{world}" if world > 1 else "single"},
         "roofline": {"bound": "hbm", "kernel": e_kernel, "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "algorithmic_bytes_per_launch": e_bytes,
-                     "traffic": ncu_traffic(e_kernel),
+                     "traffic": ncu_traffic(e_kernel) if _workload_name == "waveguide" else None,
                      "h_kernel": {"achieved": h_bytes / (h_ms / args.steps / 1e3) / 1e9,
                                   "algorithmic_bytes_per_launch": h_bytes, "ms_per_launch": h_ms / args.steps},
                      "e_ms_per_launch": e_launch_ms, "dft_ms_per_step": dft_ms / args.steps,
@@ -555,7 +565,11 @@ def main(argv=None):
     ap.add_argument("--adjoint-scale", type=float, default=1.0)
     ap.add_argument("--adjoint-fd", type=int, default=0, help="finite-difference voxels (FP64)")
     ap.add_argument("--adjoint-no-fp64", action="store_true")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="waveguide",
+                    help="waveguide: the 320x192x128 heterogeneous grid (default); dispersive: 256^3 ADE + chi3")
     args = ap.parse_args(argv)
+    global _workload_name
+    _workload_name = args.workload
     if args.warmup < 3:
         args.warmup = 3
     world, rank, local_rank = dist_env()

@@ -84,6 +84,7 @@ struct HalfStepParams {
   int full; // 1: cells with sources/χ3/poles/conductivity handled in-kernel (FULL variant)
   int zplanes;  // z planes marched by one CTA of the TMA-staged kernel
   T dt, inv_d[3];
+  T cd[3];  // Δt·(1/Δ_a): curl coefficients of the TMA-staged kernel
 
   const T* A[3];  // curl source field (E for the H half, H for the E half)
   T* O[3];        // updated field (H or E)

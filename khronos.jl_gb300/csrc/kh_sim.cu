@@ -1337,7 +1337,10 @@ class Sim : public SimBase {
     p.nxb = nxb_;
     p.zplanes = zplanes_;
     p.dt = dt_;
-    for (int a = 0; a < 3; ++a) p.inv_d[a] = T(1) / delta_[a];
+    for (int a = 0; a < 3; ++a) {
+      p.inv_d[a] = T(1) / delta_[a];
+      p.cd[a] = dt_ * p.inv_d[a];
+    }
     for (int c = 0; c < 3; ++c) {
       p.A[c] = h ? E_[c] : H_[c];
       p.O[c] = h ? H_[c] : E_[c];

@@ -119,8 +119,16 @@ __device__ __forceinline__ void load_aux(const HalfStepParams<T>& p, AuxLoads<T>
 
 }  // namespace
 
+// Resident CTAs per SM each variant is compiled for: the FULL variants
+// (sources, χ3, poles, conductivity in-kernel) need more registers than the
+// LEAN ones and would spill under the LEAN cap.
+template <typename T, bool FULL>
+constexpr int tma_min_blocks() {
+  return sizeof(T) == 4 ? (FULL ? kTmaMinBlocks - 1 : kTmaMinBlocks) : 2;
+}
+
 template <typename T, bool H, bool CPML, bool FULL>
-__global__ void __launch_bounds__(32 * kTmaY, sizeof(T) == 4 ? kTmaMinBlocks : 2)
+__global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
     half_step_tma_kernel(const HalfStepParams<T> p, const __grid_constant__ TmaMaps maps) {
   using G = TmaGeom<T>;
   constexpr int VN = 2;
@@ -206,10 +214,11 @@ __global__ void __launch_bounds__(32 * kTmaY, sizeof(T) == 4 ? kTmaMinBlocks : 2
   const int by = H ? wy : wy + 1;
   const int ob = wy * kTmaX + lane * VN;
 
-  AuxLoads<T> cur, nxt;
+  AuxLoads<T> cur;
   load_aux<T, H, FULL>(p, cur, k0, row, lane_ok, fy, anyfx, tbits);
 
   bool bad = false;
+  AuxLoads<T> nxt;
   for (int c = 0; c < N; ++c) {
     const int k = k0 + c;
     if (c + 1 < N) {
@@ -225,6 +234,7 @@ __global__ void __launch_bounds__(32 * kTmaY, sizeof(T) == 4 ? kTmaMinBlocks : 2
       if (p.err) atomicExch(p.err, KH_ERR_TIMEOUT);
     }
     if (!bad && lane_ok) {
+      using V2 = typename VT<T, 2>::V;
       const T* Sc = stages + (ncur % kTmaStages) * G::STAGE;
       const T* Sn = stages + (nnb % kTmaStages) * G::STAGE;
       const T* A0 = Sc;
@@ -235,29 +245,55 @@ __global__ void __launch_bounds__(32 * kTmaY, sizeof(T) == 4 ? kTmaMinBlocks : 2
       const T* Os = Sc + 3 * G::A_ELEMS;
       const T* Ms = Sc + 3 * G::A_ELEMS + 3 * G::O_ELEMS;
       const long long q = row + (long long)k * p.plane;
+      // Both cells of the thread in one 8/16-byte shared load per array (a
+      // is even and every tile row starts 16-byte aligned); the x neighbour
+      // of one cell is the other cell of the pair, the other one a scalar load.
+      const int a = by * G::AX + bx;
+      const V2 c0 = *reinterpret_cast<const V2*>(A0 + a);
+      const V2 c1 = *reinterpret_cast<const V2*>(A1 + a);
+      const V2 c2 = *reinterpret_cast<const V2*>(A2 + a);
+      const V2 n0 = *reinterpret_cast<const V2*>(B0 + a);
+      const V2 n1 = *reinterpret_cast<const V2*>(B1 + a);
+      const V2 y0 = *reinterpret_cast<const V2*>(A0 + a + s * G::AX);
+      const V2 y2 = *reinterpret_cast<const V2*>(A2 + a + s * G::AX);
+      T x1[VN], x2[VN];
+      if constexpr (H) {  // forward difference: cell v reads x + 1
+        x1[0] = c1.y; x2[0] = c2.y;
+        x1[1] = A1[a + 2]; x2[1] = A2[a + 2];
+      } else {            // backward difference: cell v reads x - 1
+        x1[0] = A1[a - 1]; x2[0] = A2[a - 1];
+        x1[1] = c1.x; x2[1] = c2.x;
+      }
+      const T cur0[VN] = {c0.x, c0.y}, cur1[VN] = {c1.x, c1.y}, cur2[VN] = {c2.x, c2.y};
+      const T nb0[VN] = {n0.x, n0.y}, nb1[VN] = {n1.x, n1.y};
+      const T yy0[VN] = {y0.x, y0.y}, yy2[VN] = {y2.x, y2.y};
       T K[3][VN], O[3][VN], m[3][VN];
 #pragma unroll
       for (int v = 0; v < VN; ++v) {
-        const int a = by * G::AX + bx + v;
-        const T cur0 = A0[a], cur1 = A1[a], a2 = A2[a];
-        const T nb0 = B0[a], nb1 = B1[a];
-        const T y0 = A0[a + s * G::AX], y2 = A2[a + s * G::AX];
-        const T x1 = A1[a + s], x2 = A2[a + s];
-        K[0][v] = p.dt * (p.inv_d[2] * (nb1 - cur1) - p.inv_d[1] * (y2 - a2));
-        K[1][v] = p.dt * (p.inv_d[0] * (x2 - a2) - p.inv_d[2] * (nb0 - cur0));
-        K[2][v] = p.dt * (p.inv_d[1] * (y0 - cur0) - p.inv_d[0] * (x1 - cur1));
+        K[0][v] = p.cd[2] * (nb1[v] - cur1[v]) - p.cd[1] * (yy2[v] - cur2[v]);
+        K[1][v] = p.cd[0] * (x2[v] - cur2[v]) - p.cd[2] * (nb0[v] - cur0[v]);
+        K[2][v] = p.cd[1] * (yy0[v] - cur0[v]) - p.cd[0] * (x1[v] - cur1[v]);
+      }
 #pragma unroll
-        for (int cc = 0; cc < 3; ++cc) {
-          O[cc][v] = Os[cc * G::O_ELEMS + ob + v];
-          m[cc][v] = pervox ? Ms[cc * G::O_ELEMS + ob + v] : p.m_scalar;
+      for (int cc = 0; cc < 3; ++cc) {
+        const V2 o = *reinterpret_cast<const V2*>(Os + cc * G::O_ELEMS + ob);
+        O[cc][0] = o.x;
+        O[cc][1] = o.y;
+        if (pervox) {
+          const V2 mm = *reinterpret_cast<const V2*>(Ms + cc * G::O_ELEMS + ob);
+          m[cc][0] = mm.x;
+          m[cc][1] = mm.y;
+        } else {
+          m[cc][0] = m[cc][1] = p.m_scalar;
         }
       }
       const bool fz = k < p.pml_lo[2] || k >= p.nz - p.pml_hi[2];
-      const bool anyRegion = fy || fz || anyfx;
-      bool anySpecial = false;
+      // this thread's two cells have no CPML flag and no special class
+      // (measured faster than a warp-uniform decision per row segment)
+      bool plain = !(anyfx || fy || fz);
 #pragma unroll
-      for (int v = 0; v < VN; ++v) anySpecial |= (cur.cls[v] & (H ? kSpecialH : kSpecialE)) != 0;
-      if (!anyRegion && !anySpecial) {
+      for (int v = 0; v < VN; ++v) plain = plain && !(cur.cls[v] & (H ? kSpecialH : kSpecialE));
+      if (plain) {
 #pragma unroll
         for (int cc = 0; cc < 3; ++cc)
 #pragma unroll
@@ -283,8 +319,24 @@ __global__ void __launch_bounds__(32 * kTmaY, sizeof(T) == 4 ? kTmaMinBlocks : 2
           T uc[3] = {cur.u[0][v], cur.u[1][v], cur.u[2][v]};
           T wc[3] = {cur.w[0][v], cur.w[1][v], cur.w[2][v]};
           if constexpr (FULL) {
-            general_cell<T, H>(p, q + v, i, j, k, fc, ac, cur.cls[v], special, Kc, mc, Oc, tc, uc, wc,
-                               cur.c3[v]);
+            if (!H && cur.cls[v] == (kSpecialE | kHasChi3) && !(fc[0] || fc[1] || fc[2])) {
+              // χ3-only cell outside CPML: D += curl; E = ε⁻¹D; Kerr correction
+              // (step_curl_and_update! + step_chi3_correction!, Dispersive.jl:127-147)
+#pragma unroll
+              for (int cc = 0; cc < 3; ++cc) {
+                tc[cc] = tc[cc] + Kc[cc];
+                Oc[cc] = mc[cc] * tc[cc];
+              }
+              if (cur.c3[v] != T(0)) {
+                const T esq = (Oc[0] * Oc[0] + Oc[1] * Oc[1]) + Oc[2] * Oc[2];
+                const T corr = T(1) / (T(1) + cur.c3[v] * esq);
+#pragma unroll
+                for (int cc = 0; cc < 3; ++cc) Oc[cc] = Oc[cc] * corr;
+              }
+            } else {
+              general_cell<T, H>(p, q + v, i, j, k, fc, ac, cur.cls[v], special, Kc, mc, Oc, tc, uc, wc,
+                                 cur.c3[v]);
+            }
           } else {
             if (fc[0] || fc[1] || fc[2]) {
               pml_cell<T, CPML>(fc, ac, Kc, mc, Oc, tc, uc, wc);
@@ -304,12 +356,18 @@ __global__ void __launch_bounds__(32 * kTmaY, sizeof(T) == 4 ? kTmaMinBlocks : 2
             cur.w[cc][v] = wc[cc];
           }
         }
-        const bool axis_any[3] = {anyfx, fy, fz};
+        const bool anyRegion = fy || fz || anyfx;
+        bool anySpecial = false;
 #pragma unroll
-        for (int cc = 0; cc < 3; ++cc) {
-          if (p.Ts[cc]) vst(p.Ts[cc] + q, cur.t[cc]);
-          if (p.U[cc] && axis_any[(cc + 1) % 3]) vst(p.U[cc] + q, cur.u[cc]);
-          if (p.W[cc] && axis_any[cc]) vst(p.W[cc] + q, cur.w[cc]);
+        for (int v = 0; v < VN; ++v) anySpecial |= (cur.cls[v] & (H ? kSpecialH : kSpecialE)) != 0;
+        if (anyRegion || anySpecial) {
+          const bool axis_any[3] = {anyfx, fy, fz};
+#pragma unroll
+          for (int cc = 0; cc < 3; ++cc) {
+            if (p.Ts[cc]) vst(p.Ts[cc] + q, cur.t[cc]);
+            if (p.U[cc] && axis_any[(cc + 1) % 3]) vst(p.U[cc] + q, cur.u[cc]);
+            if (p.W[cc] && axis_any[cc]) vst(p.W[cc] + q, cur.w[cc]);
+          }
         }
       }
       if (x0 + VN <= p.nx) {
