@@ -3,7 +3,8 @@
 Host mirror of the reference's adjoint stack (src/Adjoint/*.jl):
 
 * ``DesignRegion``            DesignRegion.jl (per-voxel density ρ, linear ε(ρ))
-* ``FieldOverlap``            FourierFieldsObjective (ObjectiveQuantities.jl:252-345)
+* ``FourierFields``           FourierFieldsObjective (ObjectiveQuantities.jl:252-345)
+* ``FieldOverlap``            its DFT contracted with fixed weights (mode-overlap objectives)
 * ``OptimizationProblem``     OptimizationProblem.jl:21-320 — ``opt(rho)`` returns
                               ``(f0, gradient)``; INIT → FWD → ADJ state machine
 * ``calculate_gradient``      calculate_gradient! (GradientKernel.jl:35-109)
@@ -82,12 +83,50 @@ class FieldOverlap:
     """Y_f = Σ_c Σ_cells weights[c][cell, f] · Ê_c(cell, f) over E-component DFT
     monitors, one cell box per component: the FourierFieldsObjective DFT
     (ObjectiveQuantities.jl:252-288) contracted with fixed weights, e.g.
-    conj(E_ref) for a mode-overlap objective |∫E·E_ref*|²."""
+    conj(E_ref) for a mode-overlap objective |∫E·E_ref*|².  The contraction
+    runs in FP64 on the device (kh_sim_dft_overlap)."""
 
     components: Sequence[int]          # subset of EX, EY, EZ
     starts: Sequence[tuple]
     dims: Sequence[tuple]
     weights: Sequence[np.ndarray]      # complex (dims + (nf,)) per component
+
+    def value_from_dfts(self, dfts: Sequence[np.ndarray]) -> np.ndarray:
+        return sum(np.einsum("xyzf,xyzf->f", d, w) for d, w in zip(dfts, self.weights))
+
+    def pattern(self, G: np.ndarray, part: int, k: int) -> np.ndarray:
+        """Adjoint-source amplitudes on part `part`'s cells at frequency k:
+        conj(G_k)·w (dJ = Re Σ_k conj(G_k)·dY_k)."""
+        return np.conj(G[k]) * self.weights[part][..., k]
+
+
+@dataclass
+class FourierFields:
+    """FourierFieldsObjective (ObjectiveQuantities.jl:252-288): the DFT of one
+    E component over a cell box; the objective function receives the complex
+    array itself, shape (Nx, Ny, Nz, Nf)."""
+
+    component: int
+    start: tuple
+    dim: tuple
+
+    @property
+    def components(self):
+        return [self.component]
+
+    @property
+    def starts(self):
+        return [tuple(self.start)]
+
+    @property
+    def dims(self):
+        return [tuple(self.dim)]
+
+    def value_from_dfts(self, dfts: Sequence[np.ndarray]) -> np.ndarray:
+        return np.array(dfts[0], dtype=np.complex128)
+
+    def pattern(self, G: np.ndarray, part: int, k: int) -> np.ndarray:
+        return np.conj(G[..., k])
 
 
 def adjoint_time_table(freq: float, dt: float, steps: int, T, bandwidth: float = 0.5):
@@ -197,7 +236,7 @@ class OptimizationProblem:
         ``steps``, no time history.
     """
 
-    def __init__(self, spec: SimSpec, objective_function: Callable, objective_arguments: Sequence[FieldOverlap],
+    def __init__(self, spec: SimSpec, objective_function: Callable, objective_arguments: Sequence,
                  design_region: DesignRegion, frequencies: Sequence[float], steps: int,
                  adjoint_bandwidth: float = 0.5, mode: str = "time", lib=None):
         if mode not in ("time", "dft"):
@@ -314,9 +353,12 @@ class OptimizationProblem:
         fwd.step(self.steps)
         Ys = []
         for oq, ids in zip(self.objective_arguments, self._obj_ids):
-            Y = np.zeros(len(self.frequencies), dtype=np.complex128)
-            for w, mid in zip(oq.weights, ids):
-                Y += fwd.dft_overlap(mid, w)
+            if isinstance(oq, FieldOverlap):  # contracted on the device
+                Y = np.zeros(len(self.frequencies), dtype=np.complex128)
+                for w, mid in zip(oq.weights, ids):
+                    Y += fwd.dft_overlap(mid, w)
+            else:
+                Y = oq.value_from_dfts([fwd.dft(mid) for mid in ids])
             Ys.append(Y)
         self.results_list = Ys
         self.f0, self._G = wirtinger(self.objective_function, Ys)
@@ -344,7 +386,7 @@ class OptimizationProblem:
         for (m, ci, k, si) in self._adj_src:
             tab = np.zeros((N, 2), dtype=np.complex128)
             tab[:, 1] = phases[k][::-1]
-            amp = np.conj(self._G[m][k]) * self.objective_arguments[m].weights[ci][..., k]
+            amp = self.objective_arguments[m].pattern(self._G[m], ci, k)
             adj.update_source(si, amp=amp, table=tab, cutoff=end)
         adj.reset()
         adj.step(N)
@@ -360,12 +402,11 @@ class OptimizationProblem:
         nf = len(self.frequencies)
         self.gradient_per_freq = np.zeros((nf,) + tuple(dr.dims))
         for k, f in enumerate(self.frequencies):
-            if all(abs(G[k]) == 0 for G in self._G):
+            if all(not np.any(np.asarray(G)[..., k] != 0) for G in self._G):
                 continue
             tab, cutoff, S_hat = adjoint_time_table(f, float(self.base.dt), self.steps, T, self.adjoint_bandwidth)
             for (m, ci, _, si) in self._adj_src:
-                oq = self.objective_arguments[m]
-                amp = np.conj(self._G[m][k]) * oq.weights[ci][..., k]
+                amp = self.objective_arguments[m].pattern(self._G[m], ci, k)
                 adj.update_source(si, amp=amp, table=tab, cutoff=cutoff)
             adj.reset()
             adj.step(self.steps)

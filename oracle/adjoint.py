@@ -52,10 +52,7 @@ def objective(opt, rho, want_fields=False):
     o.step(opt.steps)
     Ys = []
     for oq, ids in zip(opt.objective_arguments, opt._obj_ids):
-        Y = np.zeros(len(opt.frequencies), dtype=np.complex128)
-        for w, mid in zip(oq.weights, ids):
-            Y += np.einsum("xyzf,xyzf->f", o.dft(mid), w)
-        Ys.append(Y)
+        Ys.append(oq.value_from_dfts([o.dft(mid) for mid in ids]))
     J, G = wirtinger(opt.objective_function, Ys)
     if not want_fields:
         o.close()
@@ -94,10 +91,7 @@ def _gradient_time(opt, rho):
     hist_f = _record(o, opt, N)
     Ys = []
     for oq, ids in zip(opt.objective_arguments, opt._obj_ids):
-        Y = np.zeros(len(opt.frequencies), dtype=np.complex128)
-        for w, mid in zip(oq.weights, ids):
-            Y += np.einsum("xyzf,xyzf->f", o.dft(mid), w)
-        Ys.append(Y)
+        Ys.append(oq.value_from_dfts([o.dft(mid) for mid in ids]))
     o.close()
     _, G = wirtinger(opt.objective_function, Ys)
     sp = _with_design(opt.adj_spec, opt, rho)
@@ -106,7 +100,7 @@ def _gradient_time(opt, rho):
         s = sp.sources[si]
         tab = np.zeros((N, 2), dtype=np.complex128)
         tab[:, 1] = dft_phases(opt.frequencies[k], float(opt.base.dt), N, T)[::-1]
-        s.amp = np.conj(G[m][k]) * opt.objective_arguments[m].weights[ci][..., k]
+        s.amp = opt.objective_arguments[m].pattern(G[m], ci, k)
         s.table = tab
         s.cutoff = 1e300
     oa = OracleSim(sp)
@@ -123,14 +117,14 @@ def _gradient_dft(opt, rho):
     J, G, fwd = objective(opt, rho, want_fields=True)
     per = np.zeros((len(opt.frequencies),) + tuple(dr.dims))
     for k, f in enumerate(opt.frequencies):
-        if all(abs(g[k]) == 0 for g in G):
+        if all(not np.any(np.asarray(g)[..., k] != 0) for g in G):
             continue
         tab, cutoff, S_hat = adjoint_time_table(f, float(opt.base.dt), opt.steps, T, opt.adjoint_bandwidth)
         sp = _with_design(opt.adj_spec, opt, rho)
         sp.sources = [copy.copy(s) for s in opt.adj_spec.sources]
         for (m, ci, _, si) in opt._adj_src:
             s = sp.sources[si]
-            s.amp = np.conj(G[m][k]) * opt.objective_arguments[m].weights[ci][..., k]
+            s.amp = opt.objective_arguments[m].pattern(G[m], ci, k)
             s.table = tab
             s.cutoff = cutoff
         o = OracleSim(sp)

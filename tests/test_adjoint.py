@@ -343,3 +343,57 @@ def test_bend_workload_small(kh, gpu_lib):
     for i, f in zip(idx, fd):
         assert abs(g[i] - f) <= FD_TOL * abs(f), (i, g[i], f)
     opt.close()
+
+
+def test_reference_adjoint_procedure_on_the_oracle(kh, oracle):
+    """The reference's own single-frequency adjoint (GradientKernel.jl,
+    place_adjoint_source, adj_src_scale, _compute_jacobian), restated on the
+    oracle, against central finite differences: as written it is not the
+    gradient; with the adjoint amplitude conjugated it is the gradient times
+    cos(ωΔt/2)/(2π).  The library's gradient matches the differences."""
+    import oracle.adjoint as oadj
+    from oracle.reference_adjoint import reference_gradient
+    from adjoint_case import LAYOUTS
+    from khronos_gb300 import grid as G
+    from khronos_gb300.adjoint import FourierFields, OptimizationProblem
+
+    base, rho = make_problem("f64", 3500, 1, small=True)
+    _, _, ps, pd = LAYOUTS[10]
+    opt = OptimizationProblem(base.base, lambda Y: (Y.real ** 2 + Y.imag ** 2).sum(),
+                              [FourierFields(G.EZ, ps, pd)], base.design_region, base.frequencies, 3500)
+    ours, _ = oadj.gradient(opt, rho)
+    as_written = reference_gradient(opt, rho)
+    conjugated = reference_gradient(opt, rho, conjugate_amplitude=True)
+    idx = [(0, 0, 0), (2, 3, 1), (3, 3, 2)]
+    fd = oadj.fd_gradient(opt, rho, idx)
+    for i, f in zip(idx, fd):
+        assert abs(ours[i] - f) <= FD_TOL * abs(f)
+    corr = lambda a, b: float(np.corrcoef(a.ravel(), b.ravel())[0, 1])
+    assert corr(as_written, ours) < 0.9
+    assert corr(conjugated, ours) > 0.99999
+    w = 2 * math.pi * opt.frequencies[0] * float(opt.base.dt)
+    factor = math.cos(w / 2) / (2 * math.pi)
+    ratio = float(np.sum(conjugated * ours) / np.sum(ours * ours))
+    assert abs(ratio / factor - 1) < 2e-3, (ratio, factor)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode,steps", [("time", 600), ("dft", 1500)])
+def test_fourier_fields_objective_matches_oracle(kh, oracle, gpu_lib, mode, steps):
+    """A FourierFields objective (the DFT array itself, J = Σ|Ez|²) through the
+    CUDA path equals the oracle restatement."""
+    import oracle.adjoint as oadj
+    from adjoint_case import LAYOUTS
+    from khronos_gb300 import grid as G
+    from khronos_gb300.adjoint import FourierFields, OptimizationProblem
+
+    base, rho = make_problem("f64", steps, 2, small=True)
+    _, _, ps, pd = LAYOUTS[10]
+    opt = OptimizationProblem(base.base, lambda Y: (Y.real ** 2 + Y.imag ** 2).sum(),
+                              [FourierFields(G.EZ, ps, pd)], base.design_region, base.frequencies, steps,
+                              mode=mode, lib=gpu_lib)
+    f0, g = opt(rho)
+    g_ref, _ = oadj.gradient(opt, rho)
+    assert abs(f0 - oadj.objective(opt, rho)) <= 1e-10 * abs(f0)
+    assert np.max(np.abs(g - g_ref)) <= 1e-9 * np.max(np.abs(g_ref))
+    opt.close()
