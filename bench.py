@@ -223,12 +223,11 @@ def run_ours(args, world, rank, local_rank):
         dist.barrier()
     ms = start.elapsed_time(end)
     launches = gpu.launches - launches0
-    t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t.item())
+    from khronos_gb300.replicas import aggregate_rate, max_over_ranks
+
+    ms_max = max_over_ranks(ms, dist, device="cuda")
     cells = spec.cells
-    value = world * cells * args.steps / (ms_max / 1e3) / 1e9
+    value = aggregate_rate(cells * args.steps, ms_max / 1e3, world) / 1e9
     gpu.close()
 
     # ---- end to end through the C ABI with host buffers ------------------------
@@ -316,10 +315,10 @@ def end_to_end(args, spec, w, sh, world, dist, cells):
     h2d += sum(s.amp.size * 16 for s in spec.sources) + sum(x.size * 8 for x in spec.sigma_b + spec.sigma_d
                                                             if x is not None)
     d2h = sum(d.size * 16 for d in dft_host) + sum(f.size * 8 for f in fluxes)
-    t2 = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-    if dist:
-        dist.all_reduce(t2, op=dist.ReduceOp.MAX)
-    return {"value": world * cells * args.steps / float(t2.item()) / 1e9, "unit": UNIT,
+    from khronos_gb300.replicas import aggregate_rate, max_over_ranks
+
+    e2e_max = max_over_ranks(e2e_s, dist, device="cuda")
+    return {"value": aggregate_rate(cells * args.steps, e2e_max, world) / 1e9, "unit": UNIT,
             "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
             "scope": "GpuSim(spec) from host arrays + K steps + DFT arrays and flux read back to host"}
 
@@ -330,7 +329,7 @@ def _pct(v, q):
     return float(np.percentile(np.asarray(v, dtype=np.float64), q)) if len(v) else None
 
 
-def serving_leg(n_requests, seed=2024, budget_gb=150.0, max_resident=16, quantum=64, load=1.5):
+def serving_leg(n_requests, seed=2024, budget_gb=150.0, max_resident=16, quantum=64, load=1.5, world=1, rank=0):
     """The serving stream twice: one plain simulation at a time (the
     reference's run_batch), then through the request server with Poisson
     arrivals at `load` × the sequential throughput.  Latency = result read
@@ -345,6 +344,11 @@ def serving_leg(n_requests, seed=2024, budget_gb=150.0, max_resident=16, quantum
     from khronos_gb300.serve import Server
 
     stream = configs.serving_stream(n_requests, seed)
+    if world > 1:  # replicas: this rank serves its share of the independent requests
+        from khronos_gb300.replicas import shard
+
+        mine = set(shard([r.work for r in stream], world, rank))
+        stream = [r for i, r in enumerate(stream) if i in mine]
     work = [r.work for r in stream]
 
     def flux_of(g, w):
@@ -436,7 +440,7 @@ def serving_leg(n_requests, seed=2024, budget_gb=150.0, max_resident=16, quantum
                for a, b in zip(srv_flux, seq_flux))
     lat = lambda v: {"p50": _pct(v, 50), "p95": _pct(v, 95), "p99": _pct(v, 99), "max": max(v)}
     return {
-        "requests": n_requests, "seed": seed, "budget_gb": budget_gb, "max_resident": max_resident,
+        "requests": len(stream), "seed": seed, "budget_gb": budget_gb, "max_resident": max_resident,
         "quantum_steps": quantum, "offered_load_vs_sequential": load, "mean_interarrival_s": gap,
         "cell_updates": int(sum(work)),
         "server": {"gcell_per_s": sum(work) / srv_span / 1e9, "latency_s": lat(srv_lat), "makespan_s": srv_span},
@@ -452,14 +456,36 @@ def serving_leg(n_requests, seed=2024, budget_gb=150.0, max_resident=16, quantum
     }
 
 
-def run_serving(args):
+def run_serving(args, world=1, rank=0, local_rank=0):
+    """The serving stream on one GPU, or sharded over `world` replicas (one
+    server per GPU, requests split by shard(); the only collectives are the
+    host-side (gloo) reductions of the legs' rates and makespans)."""
     import torch
 
-    torch.cuda.set_device(0)
+    torch.cuda.set_device(local_rank)
     __graft_entry__.package()
-    res = serving_leg(args.serve_requests)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+
+        dist_mod.init_process_group("gloo")
+        dist = dist_mod
+    res = serving_leg(args.serve_requests, world=world, rank=rank)
+    if dist is not None:
+        from khronos_gb300.replicas import max_over_ranks
+
+        total = {}
+        for leg in ("server", "sequential", "saturated"):
+            span = max_over_ranks(res[leg]["makespan_s"], dist)
+            t = torch.tensor([float(res["cell_updates"])], dtype=torch.float64)
+            dist.all_reduce(t)
+            total[leg] = float(t.item()) / span / 1e9
+        res["replicas"] = {"world": world, "aggregate_gcell_per_s": total}
+        dist.destroy_process_group()
+        if rank != 0:
+            return 0
     line = {"metric": "serve p50/p95/p99 latency and aggregate Gcell-updates/s", "unit": "s",
-            "dtype": "f32", "data": "synthetic", "n_gpus": 1, "config": {"workload": "serving stream", **{
+            "dtype": "f32", "data": "synthetic", "n_gpus": world, "config": {"workload": "serving stream", **{
                 k: res[k] for k in ("requests", "seed", "budget_gb", "max_resident", "quantum_steps")}},
             "serving": res}
     print(json.dumps(line), flush=True)
@@ -576,7 +602,7 @@ def main(argv=None):
     if args.impl == "reference":
         return run_reference(args, world, rank)
     if args.serve_only:
-        return run_serving(args)
+        return run_serving(args, world, rank, local_rank)
     if args.adjoint_only:
         return run_adjoint(args)
     return run_ours(args, world, rank, local_rank)
