@@ -169,6 +169,14 @@ kh_status kh_sim_timestep(const kh_sim* sim, int64_t* out);
 kh_status kh_sim_sources_active(const kh_sim* sim, int32_t* out);
 /* Kernel launches issued since creation (fused half-step + DFT launches). */
 kh_status kh_sim_launch_count(const kh_sim* sim, int64_t* out);
+/* Step batches issued by replaying a captured CUDA graph
+ * (_try_capture_graphs!, src/Kernels/Kernels.jl:99-145).  kh_sim_step issues
+ * its steps in batches whose boundaries sit on multiples of the monitors'
+ * decimation; each batch is captured once per distinct launch sequence
+ * (sources on/off, DFT steps, table buffer) and replayed afterwards.
+ * KHRONOS_GB300_GRAPHS=0 in the environment at prepare turns this off;
+ * timed steps and steps that record history monitors are never captured. */
+kh_status kh_sim_graph_replays(const kh_sim* sim, int64_t* out);
 
 /* Results. */
 kh_status kh_sim_get_field(kh_sim* sim, int32_t component, double* out);

@@ -109,6 +109,7 @@ SIGNATURES = {
     "kh_sim_timestep": (C.c_int32, [C.c_void_p, C.POINTER(C.c_int64)]),
     "kh_sim_sources_active": (C.c_int32, [C.c_void_p, C.POINTER(C.c_int32)]),
     "kh_sim_launch_count": (C.c_int32, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "kh_sim_graph_replays": (C.c_int32, [C.c_void_p, C.POINTER(C.c_int64)]),
     "kh_sim_get_field": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]),
     "kh_sim_read_dft": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]),
     "kh_sim_monitor_info": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),

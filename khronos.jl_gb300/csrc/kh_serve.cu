@@ -145,7 +145,11 @@ struct kh_server {
             cudaEventCreateWithFlags(&r->ev[0], cudaEventDisableTiming);
             cudaEventCreateWithFlags(&r->ev[1], cudaEventDisableTiming);
           }
-          const int64_t q = std::min<int64_t>(desc.quantum_steps, r->nsteps - r->issued);
+          // quanta are whole multiples of the request's step alignment, so its
+          // batches repeat and replay captured step graphs
+          const int64_t al = std::max(1, r->sim->impl->step_alignment());
+          const int64_t quantum = std::max<int64_t>(al, (desc.quantum_steps + al - 1) / al * al);
+          const int64_t q = std::min<int64_t>(quantum, r->nsteps - r->issued);
           if (r->t_start < 0) {
             std::lock_guard<std::mutex> g(mu);
             r->t_start = now();

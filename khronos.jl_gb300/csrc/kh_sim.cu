@@ -113,6 +113,10 @@ class Sim : public SimBase {
     }
     if (batch_done_) cudaEventDestroy(batch_done_);
     for (cudaEvent_t ev : events_) cudaEventDestroy(ev);
+    for (auto& g : graphs_) cudaGraphExecDestroy(g.exec);
+    if (ev_in_) cudaEventDestroy(ev_in_);
+    if (ev_out_) cudaEventDestroy(ev_out_);
+    if (gstream_) cudaStreamDestroy(gstream_);
   }
 
   // ---------------- set-up ----------------
@@ -457,6 +461,19 @@ class Sim : public SimBase {
     }
     for (auto& h : hists_)
       KH_TRY(alloc_raw(size_t(h.ncell) * size_t(h.cap) * sizeof(T), (void**)&h.buf, false));
+    // Step alignment: lcm of the monitors' decimations (1 if above a batch).
+    {
+      long long l = 1;
+      for (auto& m : mons_)
+        if (m.dec > 1) {
+          long long a = l, b2 = m.dec;
+          while (b2) { const long long t2 = a % b2; a = b2; b2 = t2; }
+          l = l / a * m.dec;
+          if (l > kBatch) break;
+        }
+      align_ = l > kBatch ? 1 : int(l);
+      batch_len_ = (kBatch / align_) * align_;
+    }
     // last_source_time (TimeSources.jl:40-47); a CW source never cuts off.
     has_cw_ = false;
     last_time_ = -INFINITY;
@@ -474,6 +491,14 @@ class Sim : public SimBase {
       KH_CUDA(cudaEventCreateWithFlags(&copy_ev_[b], cudaEventDisableTiming));
     }
     KH_CUDA(cudaEventCreateWithFlags(&batch_done_, cudaEventDisableTiming));
+    // Step graphs (KHRONOS_GB300_GRAPHS=0 turns them off)
+    const char* gv = std::getenv("KHRONOS_GB300_GRAPHS");
+    graphs_on_ = !(gv && std::string(gv) == "0");
+    if (graphs_on_) {
+      KH_CUDA(cudaStreamCreateWithFlags(&gstream_, cudaStreamNonBlocking));
+      KH_CUDA(cudaEventCreateWithFlags(&ev_in_, cudaEventDisableTiming));
+      KH_CUDA(cudaEventCreateWithFlags(&ev_out_, cudaEventDisableTiming));
+    }
     KH_TRY(alloc_raw(sizeof(int), (void**)&err_dev_, false));
     // Half-step kernel: TMA-staged unless KHRONOS_GB300_KERNEL=simt selects the
     // register-pipelined one.
@@ -493,15 +518,22 @@ class Sim : public SimBase {
   kh_status step(int64_t nsteps, cudaStream_t stream) override {
     if (!prepared_) return fail(KH_ERR_INVALID, "step before prepare");
     if (nsteps < 0) return fail(KH_ERR_INVALID, "negative step count");
+    // Batches end on multiples of batch_len_ (a multiple of every monitor's
+    // decimation), so steady-state batches repeat their launch sequence and
+    // replay one captured graph.
     int64_t done = 0;
     while (done < nsteps) {
-      const int nb = int(std::min<int64_t>(kBatch, nsteps - done));
+      const int64_t to_edge = batch_len_ - timestep_ % batch_len_;
+      const int nb = int(std::min<int64_t>(to_edge, nsteps - done));
       kh_status st = run_batch(nb, stream);
       if (st != KH_OK) return st;
       done += nb;
     }
     return KH_OK;
   }
+
+  int step_alignment() const override { return align_; }
+  int64_t graph_replays() const override { return graph_replays_; }
 
   int64_t timestep() const override { return timestep_; }
   int sources_active() const override { return sources_active_ ? 1 : 0; }
@@ -923,6 +955,13 @@ class Sim : public SimBase {
     std::vector<std::complex<double>> amp;
     std::vector<std::complex<T>> table;
   };
+  struct GraphEntry {
+    std::vector<int64_t> sig;
+    cudaGraphExec_t exec;
+    int64_t nlaunch;
+    uint64_t last_use;
+  };
+  static constexpr size_t kMaxGraphs = 24;
   struct Hist {
     int comp, start[3], dims[3];
     long long ncell = 0;
@@ -1042,6 +1081,20 @@ class Sim : public SimBase {
     // A batch on a new stream waits for the previous batch, whose kernels read
     // the shared time-factor table this batch is about to overwrite.
     if (last_stream_ != stream && batch_done_) KH_CUDA(cudaStreamWaitEvent(stream, batch_done_, 0));
+    // Graph replay (the steady-state step graphs of _try_capture_graphs!,
+    // Kernels.jl:99-145): the batch runs on the simulation's own stream, which
+    // waits for the caller's stream and is waited on by it afterwards.  Not
+    // for timed batches (events around every launch) nor while a history
+    // monitor records (its destination moves every step).
+    bool use_graph = graphs_on_ && !timing;
+    for (auto& h : hists_)
+      if (timestep_ < h.cap) use_graph = false;
+    cudaStream_t ws = stream;  // stream the batch's work is issued on
+    if (use_graph) {
+      KH_CUDA(cudaEventRecord(ev_in_, stream));
+      KH_CUDA(cudaStreamWaitEvent(gstream_, ev_in_, 0));
+      ws = gstream_;
+    }
     // Host pass: source activity, time factors and DFT phases for nb steps.
     struct StepPlan {
       bool sa;
@@ -1106,8 +1159,8 @@ class Sim : public SimBase {
     }
     if (!tab.empty()) {
       std::memcpy(pinned_[b], tab.data(), bytes);
-      KH_CUDA(cudaMemcpyAsync(tab_dev_[b], pinned_[b], bytes, cudaMemcpyHostToDevice, stream));
-      KH_CUDA(cudaEventRecord(copy_ev_[b], stream));
+      KH_CUDA(cudaMemcpyAsync(tab_dev_[b], pinned_[b], bytes, cudaMemcpyHostToDevice, ws));
+      KH_CUDA(cudaEventRecord(copy_ev_[b], ws));
       copy_pending_[b] = true;
     }
     const Cplx<T>* dtab = static_cast<const Cplx<T>*>(tab_dev_[b]);
@@ -1131,6 +1184,7 @@ class Sim : public SimBase {
     const bool full_h_base = msb || (ref_cpu && special_in_region_[1]);
     const bool full_e_base = msd || chi3_ != nullptr || !poles_d_.empty() || (ref_cpu && special_in_region_[0]);
     kh::SourceFixParams<T> fh = fix_params(true), fe = fix_params(false);
+    auto issue_all = [&](cudaStream_t st) {
     for (int s = 0; s < nb; ++s) {
       const StepPlan& P = plan[s];
       ph.sources_active = P.sa ? 1 : 0;
@@ -1138,34 +1192,88 @@ class Sim : public SimBase {
       const bool src_h = P.sa && has_src_[1];
       ph.full = (full_h_base || (src_h && !src_fix_ok_[1])) ? 1 : 0;
       mark(s, 0);
-      if (use_tma_) kh::launch_half_step_tma<T>(true, ph, maps_h_, stream);
-      else kh::launch_half_step<T>(true, ph, stream);
+      if (use_tma_) kh::launch_half_step_tma<T>(true, ph, maps_h_, st);
+      else kh::launch_half_step<T>(true, ph, st);
       ++launches;
       if (src_h && !ph.full) {
         fh.f_now = dtab + P.fH;
-        kh::launch_source_fix<T>(fh, stream);
+        kh::launch_source_fix<T>(fh, st);
         ++launches;
       }
       mark(s, 1);
-      for (auto& dm : P.dftH) launch_dft_for(dm.first, dtab + dm.second, stream);
-      record_histories(true, timestep_ + s, stream);
+      for (auto& dm : P.dftH) launch_dft_for(dm.first, dtab + dm.second, st);
+      record_histories(true, timestep_ + s, st);
       mark(s, 2);
       pe.sources_active = P.sa ? 1 : 0;
       pe.f_now = dtab + P.fE;
       const bool src_e = P.sa && has_src_[0];
       pe.full = (full_e_base || (src_e && !src_fix_ok_[0])) ? 1 : 0;
-      if (use_tma_) kh::launch_half_step_tma<T>(false, pe, maps_e_, stream);
-      else kh::launch_half_step<T>(false, pe, stream);
+      if (use_tma_) kh::launch_half_step_tma<T>(false, pe, maps_e_, st);
+      else kh::launch_half_step<T>(false, pe, st);
       ++launches;
       if (src_e && !pe.full) {
         fe.f_now = dtab + P.fE;
-        kh::launch_source_fix<T>(fe, stream);
+        kh::launch_source_fix<T>(fe, st);
         ++launches;
       }
       mark(s, 3);
-      for (auto& dm : P.dftE) launch_dft_for(dm.first, dtab + dm.second, stream);
-      record_histories(false, timestep_ + s, stream);
+      for (auto& dm : P.dftE) launch_dft_for(dm.first, dtab + dm.second, st);
+      record_histories(false, timestep_ + s, st);
       mark(s, 4);
+    }
+    };
+    if (!use_graph) {
+      issue_all(stream);
+    } else {
+      // signature of the batch's launch sequence: equal signatures issue the
+      // same kernels with the same arguments (only the table contents differ)
+      std::vector<int64_t> sig;
+      sig.reserve(size_t(nb) * 8 + 4);
+      sig.push_back(nb);
+      sig.push_back(b);
+      for (int q = 0; q < nb; ++q) {
+        const StepPlan& P = plan[q];
+        sig.push_back(P.sa ? 1 : 0);
+        sig.push_back(int64_t(P.fH));
+        sig.push_back(int64_t(P.fE));
+        for (auto& dm : P.dftH) { sig.push_back(-1 - dm.first); sig.push_back(int64_t(dm.second)); }
+        for (auto& dm : P.dftE) { sig.push_back(-1000000 - dm.first); sig.push_back(int64_t(dm.second)); }
+      }
+      GraphEntry* g = nullptr;
+      for (auto& ge : graphs_)
+        if (ge.sig == sig) { g = &ge; break; }
+      if (g) ++graph_hits_;
+      else ++graph_misses_;
+      if (!g) {
+        if (graphs_.size() >= kMaxGraphs) {  // evict the least recently used
+          size_t lru = 0;
+          for (size_t q = 1; q < graphs_.size(); ++q)
+            if (graphs_[q].last_use < graphs_[lru].last_use) lru = q;
+          cudaGraphExecDestroy(graphs_[lru].exec);
+          graphs_.erase(graphs_.begin() + long(lru));
+        }
+        const int64_t l0 = launches;
+        KH_CUDA(cudaStreamBeginCapture(ws, cudaStreamCaptureModeThreadLocal));
+        issue_all(ws);
+        cudaGraph_t graph = nullptr;
+        cudaError_t ce = cudaStreamEndCapture(ws, &graph);
+        cudaGraphExec_t exec = nullptr;
+        if (ce == cudaSuccess) ce = cudaGraphInstantiate(&exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (ce != cudaSuccess) return fail(KH_ERR_CUDA, std::string("step graph capture: ") + cudaGetErrorString(ce));
+        graphs_.push_back({std::move(sig), exec, launches - l0, 0});
+        launches = l0;
+        g = &graphs_.back();
+      }
+      g->last_use = ++graph_clock_;
+      KH_CUDA(cudaGraphLaunch(g->exec, ws));
+      launches += g->nlaunch;
+      ++graph_replays_;
+      KH_CUDA(cudaEventRecord(ev_out_, ws));
+      KH_CUDA(cudaStreamWaitEvent(stream, ev_out_, 0));
+      // batches that rarely repeat (irregular step counts) capture more than
+      // they replay: issue directly from then on
+      if (graph_misses_ > 16 && graph_hits_ < graph_misses_) graphs_on_ = false;
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(KH_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
@@ -1400,6 +1508,14 @@ class Sim : public SimBase {
   std::vector<SrcH> srcs_;
   std::vector<Mon> mons_;
   std::vector<Hist> hists_;
+  bool graphs_on_ = false;
+  int align_ = 1, batch_len_ = 512;
+  int64_t graph_misses_ = 0, graph_hits_ = 0;
+  cudaStream_t gstream_ = nullptr;
+  cudaEvent_t ev_in_ = nullptr, ev_out_ = nullptr;
+  std::vector<GraphEntry> graphs_;
+  uint64_t graph_clock_ = 0;
+  int64_t graph_replays_ = 0;
   int nsrc_ = 0;
   bool has_src_[2] = {false, false};         // [E half, H half]
   bool src_fix_ok_[2] = {true, true};
@@ -1607,6 +1723,12 @@ kh_status kh_sim_step_timed(kh_sim* sim, int64_t nsteps, void* stream, double* h
 kh_status kh_sim_model_bytes_per_step(const kh_sim* sim, double* out) {
   if (!sim || !out) return KH_ERR_INVALID;
   *out = sim->impl->model_bytes_per_step();
+  return KH_OK;
+}
+
+kh_status kh_sim_graph_replays(const kh_sim* sim, int64_t* out) {
+  if (!sim || !out) return KH_ERR_INVALID;
+  *out = sim->impl->graph_replays();
   return KH_OK;
 }
 

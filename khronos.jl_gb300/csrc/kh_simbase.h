@@ -84,6 +84,10 @@ struct SimBase {
   virtual kh_status add_history(int comp, const int32_t* st, const int32_t* dm, int64_t capacity,
                                 int32_t* id) = 0;
   virtual kh_status history_view(int id, HistoryView* out) = 0;
+  // Step counts that keep batch boundaries aligned with the DFT decimation
+  // (their multiples replay captured step graphs).
+  virtual int step_alignment() const = 0;
+  virtual int64_t graph_replays() const = 0;
 };
 
 }  // namespace kh_host

@@ -134,6 +134,12 @@ class GpuSim:
         self._check(self.lib.kh_sim_launch_count(self.handle, C.byref(v)))
         return v.value
 
+    @property
+    def graph_replays(self) -> int:
+        v = C.c_int64()
+        self._check(self.lib.kh_sim_graph_replays(self.handle, C.byref(v)))
+        return v.value
+
     # -- results ------------------------------------------------------------
     def field(self, comp: int) -> np.ndarray:
         """Component array in the reference's component dimensions, indexed [i, j, k]."""

@@ -284,3 +284,28 @@ def test_z_tiling_is_invisible(kh, oracle, gpu_lib, monkeypatch):
         assert np.array_equal(runs[zp][1], runs["16"][1]), zp
     monkeypatch.delenv("KHRONOS_GB300_ZPLANES")
     compare(sp, 70, oracle, gpu_lib, TOL["f32"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dtype", ["f32", "f64"])
+def test_step_graphs_are_invisible(kh, gpu_lib, dtype, monkeypatch):
+    """Batches replayed from captured CUDA graphs give bit-identical fields and
+    DFT values to directly launched batches, across the source cutoff."""
+    from khronos_gb300 import configs
+    from khronos_gb300.device import GpuSim
+
+    w = configs.waveguide(dtype=dtype, scale=0.25)
+    spec = w.sim.spec()
+    out = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("KHRONOS_GB300_GRAPHS", mode)
+        g = GpuSim(spec, lib=gpu_lib)
+        for n in (7, 1500, 64, 64, 300):  # irregular calls across the cutoff (step ~400)
+            g.step(n)
+        out[mode] = ([g.field(c) for c in range(6)], [g.dft(m) for m in range(len(spec.monitors))],
+                     g.graph_replays)
+        g.close()
+    assert out["0"][2] == 0
+    assert out["1"][2] > 0
+    for a, b in zip(out["0"][0] + out["0"][1], out["1"][0] + out["1"][1]):
+        assert np.array_equal(a, b)
