@@ -166,11 +166,11 @@ kh_status fail(kh_sim* s, kh_status st, const std::string& msg) {
   return st;
 }
 
+// Temporary device buffer from the library pool, on the legacy stream the
+// reduction kernels and their synchronous copies run on.
 struct DevBuf {
   void* p = nullptr;
-  ~DevBuf() {
-    if (p) cudaFree(p);
-  }
+  ~DevBuf() { kh_host::dev_free(p, cudaStreamLegacy); }
 };
 
 #define KH_ACUDA(sim, call)                                                              \
@@ -188,9 +188,9 @@ kh_status overlap_impl(kh_sim* sim, const MonitorView& m, const double* weights,
   const long long chunk = 8LL * kRedThreads;
   const int nblk = int(std::max<long long>(1, (ncell + chunk - 1) / chunk));
   DevBuf w, part, res;
-  KH_ACUDA(sim, cudaMalloc(&w.p, size_t(total) * sizeof(double2)));
-  KH_ACUDA(sim, cudaMalloc(&part.p, size_t(nblk) * m.nf * sizeof(double2)));
-  KH_ACUDA(sim, cudaMalloc(&res.p, size_t(m.nf) * sizeof(double2)));
+  KH_ACUDA(sim, kh_host::dev_alloc(&w.p, size_t(total) * sizeof(double2), cudaStreamLegacy));
+  KH_ACUDA(sim, kh_host::dev_alloc(&part.p, size_t(nblk) * m.nf * sizeof(double2), cudaStreamLegacy));
+  KH_ACUDA(sim, kh_host::dev_alloc(&res.p, size_t(m.nf) * sizeof(double2), cudaStreamLegacy));
   KH_ACUDA(sim, cudaMemcpy(w.p, weights, size_t(total) * sizeof(double2), cudaMemcpyHostToDevice));
   overlap_partial_kernel<T><<<dim3(nblk, m.nf), kRedThreads>>>(
       static_cast<const Cplx<T>*>(m.F), static_cast<const Cplx<T>*>(m.C),
@@ -219,7 +219,7 @@ kh_status gradient_impl(kh_sim* fwd, const MonitorView* fv, int ff, const Monito
   a.coef_re = coef_re;
   a.coef_im = coef_im;
   DevBuf out;
-  KH_ACUDA(fwd, cudaMalloc(&out.p, size_t(a.ncell) * sizeof(double)));
+  KH_ACUDA(fwd, kh_host::dev_alloc(&out.p, size_t(a.ncell) * sizeof(double), cudaStreamLegacy));
   int blocks = int(std::min<long long>((a.ncell + kRedThreads - 1) / kRedThreads, 152LL * 8));
   adjoint_gradient_kernel<T><<<std::max(blocks, 1), kRedThreads>>>(a, static_cast<double*>(out.p));
   fwd->impl->launches += 1;
@@ -238,8 +238,8 @@ kh_status sq_norms_impl(kh_sim* sim, const void* const* arrays, long long count,
   a.chunk = 16LL * kRedThreads;
   const int nblk = int(std::max<long long>(1, (count + a.chunk - 1) / a.chunk));
   DevBuf part, res;
-  KH_ACUDA(sim, cudaMalloc(&part.p, size_t(nblk) * 6 * sizeof(double2)));
-  KH_ACUDA(sim, cudaMalloc(&res.p, 6 * sizeof(double2)));
+  KH_ACUDA(sim, kh_host::dev_alloc(&part.p, size_t(nblk) * 6 * sizeof(double2), cudaStreamLegacy));
+  KH_ACUDA(sim, kh_host::dev_alloc(&res.p, 6 * sizeof(double2), cudaStreamLegacy));
   sq_norm_partial_kernel<T><<<dim3(nblk, 6), kRedThreads>>>(a, static_cast<double2*>(part.p));
   overlap_final_kernel<<<6, kRedThreads>>>(static_cast<const double2*>(part.p), nblk,
                                             static_cast<double2*>(res.p));
@@ -263,7 +263,7 @@ kh_status correlate_impl(kh_sim* fwd, const kh_host::HistoryView* fv, const kh_h
   a.nsteps = nsteps;
   a.coef = coef;
   DevBuf out;
-  KH_ACUDA(fwd, cudaMalloc(&out.p, size_t(a.ncell) * sizeof(double)));
+  KH_ACUDA(fwd, kh_host::dev_alloc(&out.p, size_t(a.ncell) * sizeof(double), cudaStreamLegacy));
   int blocks = int(std::min<long long>((a.ncell + kRedThreads - 1) / kRedThreads, 152LL * 16));
   history_correlate_kernel<T><<<std::max(blocks, 1), kRedThreads>>>(a, static_cast<double*>(out.p));
   fwd->impl->launches += 1;

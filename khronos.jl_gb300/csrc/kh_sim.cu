@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -72,6 +73,68 @@ kh_status flux_static_scratch(double** out, std::string& err) {
 
 using kh_host::SimBase;
 
+}  // namespace
+
+namespace kh_host {
+
+cudaError_t dev_alloc(void** p, size_t bytes, cudaStream_t s) {
+  static std::mutex mu;
+  static cudaMemPool_t pools[kMaxDevices] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  cudaMemPool_t pool;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (!pools[dev]) {
+      cudaMemPoolProps props;
+      std::memset(&props, 0, sizeof(props));
+      props.allocType = cudaMemAllocationTypePinned;
+      props.location.type = cudaMemLocationTypeDevice;
+      props.location.id = dev;
+      if ((e = cudaMemPoolCreate(&pools[dev], &props)) != cudaSuccess) return e;
+      uint64_t keep = UINT64_MAX;  // keep freed memory in the pool
+      if ((e = cudaMemPoolSetAttribute(pools[dev], cudaMemPoolAttrReleaseThreshold, &keep)) != cudaSuccess)
+        return e;
+    }
+    pool = pools[dev];
+  }
+  return cudaMallocFromPoolAsync(p, bytes, pool, s);
+}
+
+cudaError_t dev_free(void* p, cudaStream_t s) { return p ? cudaFreeAsync(p, s) : cudaSuccess; }
+
+namespace {
+std::mutex g_pinned_mu;
+std::multimap<size_t, void*> g_pinned_free;  // size -> buffer
+}  // namespace
+
+void* pinned_get(size_t bytes) {
+  {
+    std::lock_guard<std::mutex> lock(g_pinned_mu);
+    auto it = g_pinned_free.lower_bound(bytes);
+    if (it != g_pinned_free.end() && it->first <= 2 * bytes + 4096) {
+      void* p = it->second;
+      g_pinned_free.erase(it);
+      return p;
+    }
+  }
+  void* p = nullptr;
+  if (cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
+  return p;
+}
+
+void pinned_put(void* p, size_t bytes) {
+  if (!p) return;
+  std::lock_guard<std::mutex> lock(g_pinned_mu);
+  g_pinned_free.emplace(bytes, p);
+}
+
+}  // namespace kh_host
+
+namespace {
+
 #define KH_CUDA(call)                                                          \
   do {                                                                         \
     cudaError_t e_ = (call);                                                   \
@@ -106,9 +169,14 @@ class Sim : public SimBase {
   }
 
   ~Sim() override {
-    for (void* p : allocs_) cudaFree(p);
+    // wait for this simulation's own work only, then hand the memory back to
+    // the pools (no device-wide synchronisation)
+    if (batch_recorded_) cudaEventSynchronize(batch_done_);
+    for (int b = 0; b < 2; ++b)
+      if (copy_pending_[b]) cudaEventSynchronize(copy_ev_[b]);
+    for (void* p : allocs_) kh_host::dev_free(p, cudaStreamLegacy);
     for (int b = 0; b < 2; ++b) {
-      if (pinned_[b]) cudaFreeHost(pinned_[b]);
+      if (pinned_[b]) kh_host::pinned_put(pinned_[b], tab_cap_);
       if (copy_ev_[b]) cudaEventDestroy(copy_ev_[b]);
     }
     if (batch_done_) cudaEventDestroy(batch_done_);
@@ -487,7 +555,8 @@ class Sim : public SimBase {
     tab_cap_ = table_capacity() * sizeof(Cplx<T>);
     for (int b = 0; b < 2; ++b) {
       KH_TRY(alloc_raw(tab_cap_, &tab_dev_[b], false));
-      KH_CUDA(cudaMallocHost(&pinned_[b], tab_cap_));
+      pinned_[b] = kh_host::pinned_get(tab_cap_);
+      if (!pinned_[b]) return fail(KH_ERR_OOM, "pinned staging buffer");
       KH_CUDA(cudaEventCreateWithFlags(&copy_ev_[b], cudaEventDisableTiming));
     }
     KH_CUDA(cudaEventCreateWithFlags(&batch_done_, cudaEventDisableTiming));
@@ -652,14 +721,14 @@ class Sim : public SimBase {
     }
     if (kh_status es = wait_idle(); es != KH_OK) return es;
     double* dout = nullptr;
-    KH_CUDA(cudaMalloc(&dout, sizeof(double) * m[0]->nf));
+    KH_CUDA(kh_host::dev_alloc((void**)&dout, sizeof(double) * m[0]->nf, cudaStreamLegacy));
     kh::launch_flux<T>(m[0]->F, m[1]->F, m[2]->F, m[3]->F, m[0]->C, m[1]->C, m[2]->C, m[3]->C,
                        m[0]->dims, m[1]->dims, m[2]->dims, m[3]->dims, normal, m[0]->nf, dA, dout,
                        nullptr);
     ++launches;
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpy(out, dout, sizeof(double) * m[0]->nf, cudaMemcpyDeviceToHost);
-    cudaFree(dout);
+    kh_host::dev_free(dout, cudaStreamLegacy);
     if (e != cudaSuccess) return fail(KH_ERR_CUDA, cudaGetErrorString(e));
     return KH_OK;
   }
@@ -1023,10 +1092,10 @@ class Sim : public SimBase {
 
   kh_status alloc_raw(size_t bytes, void** out, bool is_state) {
     void* p = nullptr;
-    KH_CUDA(cudaMalloc(&p, bytes));
+    KH_CUDA(kh_host::dev_alloc(&p, bytes, cudaStreamLegacy));
     allocs_.push_back(p);
     device_bytes_ += int64_t(bytes);
-    KH_CUDA(cudaMemset(p, 0, bytes));
+    KH_CUDA(cudaMemsetAsync(p, 0, bytes, cudaStreamLegacy));
     if (is_state) state_.push_back({p, bytes});
     *out = p;
     return KH_OK;
@@ -1034,7 +1103,7 @@ class Sim : public SimBase {
   kh_status alloc_field(T** out) { return alloc_raw(size_t(total_) * sizeof(T), (void**)out, true); }
 
   kh_status upload_raw(const void* h, size_t bytes, void** out) {
-    KH_CUDA(cudaMalloc(out, bytes));
+    KH_CUDA(kh_host::dev_alloc(out, bytes, cudaStreamLegacy));
     allocs_.push_back(*out);
     device_bytes_ += int64_t(bytes);
     KH_CUDA(cudaMemcpy(*out, h, bytes, cudaMemcpyHostToDevice));

@@ -12,6 +12,17 @@
 
 namespace kh_host {
 
+// Library allocations.  Device memory comes from a per-device stream-ordered
+// pool (cudaMallocFromPoolAsync / cudaFreeAsync) that keeps freed memory for
+// reuse instead of returning it to the device: freeing never synchronises the
+// device, so simulations released while others step (the request server) or
+// temporaries of a flux read do not stall the other streams.  Pinned host
+// staging buffers are likewise recycled, never freed while the process runs.
+cudaError_t dev_alloc(void** p, size_t bytes, cudaStream_t s);
+cudaError_t dev_free(void* p, cudaStream_t s);
+void* pinned_get(size_t bytes);
+void pinned_put(void* p, size_t bytes);
+
 // Device view of one DFT monitor: accumulators F[f·ncell + cell] (cell x
 // fastest over the monitor box) and, for FP32 runs, the Kahan compensation
 // C (value = F − C); C is null in FP64 runs.
