@@ -142,6 +142,25 @@ typedef struct {
                           f(nΔt) then f(nΔt+Δt/2), interleaved                  */
 } kh_source_desc;
 
+/* Geometry objects of kh_sim_set_geometry (GeometryPrimitives shapes the
+ * reference paints, src/Geometry.jl:156-250): */
+#define KH_SHAPE_BALL 0     /* center, size[0] = radius                        */
+#define KH_SHAPE_CUBOID 1   /* axis-aligned box: center, size[0..2]             */
+#define KH_SHAPE_CYLINDER 2 /* center, size[0] = radius, size[1] = height, axis */
+
+/* Subpixel smoothing modes (src/Geometry.jl:795-990). */
+#define KH_SMOOTH_NONE 0
+#define KH_SMOOTH_VOLUME 1       /* VolumeAveraging: ε̄ = f·ε₁ + (1−f)·ε₂            */
+#define KH_SMOOTH_ANISOTROPIC 2  /* AnisotropicSmoothing (Farjadpour et al. 2006) */
+
+typedef struct {
+  int32_t shape;     /* KH_SHAPE_*                                  */
+  int32_t axis;      /* cylinder axis 0..2                          */
+  double center[3];
+  double size[3];
+  double eps;        /* isotropic relative permittivity of the object */
+} kh_object;
+
 /* Library and device information. */
 const char* kh_version(void);
 kh_status kh_device_info(int32_t* sm_count, int32_t* cc_major, int32_t* cc_minor);
@@ -159,6 +178,25 @@ kh_status kh_sim_add_dft_monitor(kh_sim* sim, int32_t component, const int32_t s
                                  const int32_t dims[3], int32_t nfreq, const double* freqs,
                                  int32_t decimation, int32_t* out_id);
 kh_status kh_sim_prepare(kh_sim* sim);
+
+/* Per-voxel ε⁻¹ of all three E components computed on the device at
+ * kh_sim_prepare from a list of objects (replaces init_geometry's host
+ * rasterisation and _apply_subpixel_smoothing!, src/Geometry.jl:450-664,
+ * 795-990).  Each component samples the objects at its own Yee position
+ * origin + (i, j, k)·Δ + shift_c (shift of Ex (0, −Δy/2, −Δz/2), Ey
+ * (−Δx/2, 0, −Δz/2), Ez (−Δx/2, −Δy/2, 0), src/utils.jl:139-170), `origin` being
+ * the centre of cell (0,0,0); the first object containing the point wins
+ * (objects are painted in reverse order, Geometry.jl:223-250); points in no
+ * object get background_eps.  `smoothing` = KH_SMOOTH_* then averages
+ * interface voxels (a voxel whose value differs from a face neighbour's)
+ * with the fill fraction of the nearest object surface.  Before prepare; it
+ * takes the place of kh_sim_set_material(KH_MAT_EPS_INV, ...).  The objects
+ * are copied; at most 65536. */
+kh_status kh_sim_set_geometry(kh_sim* sim, const kh_object* objects, int32_t n, double background_eps,
+                              const double origin[3], int32_t smoothing);
+/* Read back a per-voxel material array (Center range, x fastest): the
+ * kh_sim_set_material kinds; after prepare. */
+kh_status kh_sim_read_material(kh_sim* sim, int32_t kind, int32_t comp, double* out);
 
 /* Time stepping: nsteps full steps of step!(sim) on `stream`. */
 kh_status kh_sim_step(kh_sim* sim, int64_t nsteps, void* stream);

@@ -14,6 +14,8 @@ KH_OK, KH_ERR_INVALID, KH_ERR_OOM, KH_ERR_CUDA, KH_ERR_TIMEOUT, KH_ERR_NAN, KH_E
 KH_F32, KH_F64 = 0, 1
 KH_MAT_EPS_INV, KH_MAT_MU_INV, KH_MAT_SIGMA_D, KH_MAT_SIGMA_B, KH_MAT_CHI3 = range(5)
 KH_TIME_GAUSSIAN, KH_TIME_CW, KH_TIME_TABLE = range(3)
+KH_SHAPE_BALL, KH_SHAPE_CUBOID, KH_SHAPE_CYLINDER = range(3)
+KH_SMOOTH_NONE, KH_SMOOTH_VOLUME, KH_SMOOTH_ANISOTROPIC = range(3)
 KH_SEM_REFERENCE_CPU, KH_SEM_CPML = 0, 1
 KH_REQ_QUEUED, KH_REQ_ADMITTED, KH_REQ_RUNNING, KH_REQ_DONE, KH_REQ_FAILED, KH_REQ_RELEASED = range(6)
 
@@ -70,6 +72,16 @@ class SourceDesc(C.Structure):
     ]
 
 
+class GeomObject(C.Structure):
+    _fields_ = [
+        ("shape", C.c_int32),
+        ("axis", C.c_int32),
+        ("center", D3),
+        ("size", D3),
+        ("eps", C.c_double),
+    ]
+
+
 class ServerDesc(C.Structure):
     _fields_ = [
         ("budget_bytes", C.c_int64),
@@ -109,6 +121,9 @@ SIGNATURES = {
     "kh_sim_timestep": (C.c_int32, [C.c_void_p, C.POINTER(C.c_int64)]),
     "kh_sim_sources_active": (C.c_int32, [C.c_void_p, C.POINTER(C.c_int32)]),
     "kh_sim_launch_count": (C.c_int32, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "kh_sim_set_geometry": (C.c_int32, [C.c_void_p, C.POINTER(GeomObject), C.c_int32, C.c_double,
+                                        C.POINTER(C.c_double), C.c_int32]),
+    "kh_sim_read_material": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_double)]),
     "kh_sim_graph_replays": (C.c_int32, [C.c_void_p, C.POINTER(C.c_int64)]),
     "kh_sim_get_field": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]),
     "kh_sim_read_dft": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]),

@@ -18,8 +18,12 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = ROOT / "_build" / "khronos_gb300"
 LIB = PKG / "libkhronos_gb300.so"
-SOURCES = ["kh_kernels.cu", "kh_tma.cu", "kh_sim.cu", "kh_serve.cu", "kh_adjoint.cu"]
+SOURCES = ["kh_kernels.cu", "kh_tma.cu", "kh_sim.cu", "kh_serve.cu", "kh_adjoint.cu", "kh_geometry.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# The geometry set-up decides inside/outside at points that can sit exactly on
+# an object's boundary: its double arithmetic is kept unfused so each
+# coordinate and distance rounds as the IEEE expression it restates.
+PER_FILE_FLAGS = {"kh_geometry.cu": ["-fmad=false"]}
 
 
 def nvcc() -> str:
@@ -47,7 +51,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
 
     def compile_one(src: str) -> Path:
         obj = BUILD / (Path(src).stem + ".o")
-        cmd = [cc, *flags, "-c", str(CSRC / src), "-o", str(obj)]
+        cmd = [cc, *flags, *PER_FILE_FLAGS.get(src, []), "-c", str(CSRC / src), "-o", str(obj)]
         if verbose:
             print(" ".join(cmd), file=sys.stderr)
         r = subprocess.run(cmd, capture_output=True, text=True)

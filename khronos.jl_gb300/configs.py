@@ -277,28 +277,27 @@ class ServingRequest:
 
 def serving_request(index: int, grid, steps: int, seed: int, dtype="f32") -> Workload:
     """One request of the serving stream: `grid` cells at 20 cells/µm with a
-    10-cell CPML, 1–20 dielectric spheres (ε ~ U(2, 12), radius 3–15 cells),
-    an Ez Gaussian-pulse dipole at a random interior point and one x-normal
+    10-cell CPML, 1–20 dielectric spheres (ε ~ U(2, 12), radius 3–15 cells,
+    centres inside the CPML-free region; the first sphere wins where they
+    overlap) rasterised on the device at each component's Yee position, an Ez
+    Gaussian-pulse dipole at a random interior point and one x-normal
     5-frequency flux plane."""
+    from .geometry import Ball, Material, Object
+
     res = 20
     pml = 10 / res
     size = tuple(n / res for n in grid)
     rng = np.random.default_rng(seed)
     nsph = int(rng.integers(1, 21))
-    eps = np.ones(grid)
     lo = [int(res * pml)] * 3
     hi = [grid[a] - lo[a] for a in range(3)]
+    objs = []
     for _ in range(nsph):
         r = float(rng.uniform(3, 15))
         c = [float(rng.uniform(lo[a], hi[a])) for a in range(3)]
         e = float(rng.uniform(2, 12))
-        b0 = [max(0, int(math.floor(c[a] - r))) for a in range(3)]
-        b1 = [min(grid[a], int(math.ceil(c[a] + r)) + 1) for a in range(3)]
-        ii, jj, kk = np.meshgrid(*[np.arange(b0[a], b1[a]) + 0.5 for a in range(3)], indexing="ij")
-        m = (ii - c[0]) ** 2 + (jj - c[1]) ** 2 + (kk - c[2]) ** 2 <= r * r
-        sub = eps[b0[0]:b1[0], b0[1]:b1[1], b0[2]:b1[2]]
-        sub[m & (sub == 1.0)] = e  # first sphere wins
-    einv = 1.0 / eps
+        centre = tuple(c[a] / res - size[a] / 2 for a in range(3))  # cell units -> µm (cell_center 0)
+        objs.append(Object(Ball(centre, r / res), Material(e)))
     margin = 2
     pos = [float(rng.uniform(lo[a] + margin, hi[a] - margin)) / res - size[a] / 2 for a in range(3)]
     src = UniformSource(time_profile=GaussianPulseSource(fcen=FCEN, fwidth=0.2 * FCEN), component=G.EZ,
@@ -307,7 +306,7 @@ def serving_request(index: int, grid, steps: int, seed: int, dtype="f32") -> Wor
     fm = FluxMonitor(center=(0.3 * inner[0], 0.0, 0.0), size=(0.0, 0.9 * inner[1], 0.9 * inner[2]),
                      frequencies=_freqs(5, 0.8 * FCEN, 1.2 * FCEN))
     sim = Simulation(cell_size=size, resolution=res, sources=[src], boundaries=[[pml, pml]] * 3,
-                     monitors=[fm], dtype=dtype, eps_inv=[einv, einv, einv])
+                     monitors=[fm], dtype=dtype, geometry=objs, background_eps=1.0)
     assert tuple(sim.n) == tuple(grid), (sim.n, grid)
     return Workload(f"serve{index}", sim, steps, [fm],
                     f"{grid[0]}x{grid[1]}x{grid[2]}, {nsph} spheres, Ez dipole, {steps} steps")

@@ -150,6 +150,30 @@ struct alignas(128) TmaMaps {
 template <typename T>
 size_t tma_smem_bytes();
 
+// Geometry set-up (kh_geometry.cu): one object with its bounding box.
+struct GeomObj {
+  int shape, axis;
+  double c[3], s[3];
+  double eps;
+  double lo[3], hi[3];
+};
+
+// One component's rasterisation (+ smoothing) over the padded layout.
+struct GeomArgs {
+  const GeomObj* objs;  // device array
+  int nobj;
+  int n[3];
+  long long pitch, plane, origin, total;
+  double org[3];        // this component's position of cell (0,0,0)
+  double d[3];
+  double background;
+  int smoothing;        // KH_SMOOTH_*
+  int comp;             // 0..2 (anisotropic projection)
+};
+
+template <typename T>
+void launch_geometry(const GeomArgs& a, T* eps_inv, T* scratch, void* stream);
+
 template <typename T>
 void launch_half_step_tma(bool h_half, const HalfStepParams<T>& p, const TmaMaps& maps, void* stream);
 

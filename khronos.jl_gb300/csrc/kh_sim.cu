@@ -205,6 +205,71 @@ class Sim : public SimBase {
     return KH_OK;
   }
 
+  kh_status set_geometry(const kh_object* objs, int n, double background, const double* origin,
+                         int smoothing) override {
+    if (prepared_) return fail(KH_ERR_INVALID, "set_geometry after prepare");
+    if (n < 0 || n > 65536 || (n > 0 && !objs) || !origin) return fail(KH_ERR_INVALID, "bad geometry arguments");
+    if (smoothing < KH_SMOOTH_NONE || smoothing > KH_SMOOTH_ANISOTROPIC)
+      return fail(KH_ERR_INVALID, "unknown smoothing mode");
+    if (!(background > 0)) return fail(KH_ERR_INVALID, "background permittivity must be positive");
+    if (!eps_h_[0].empty() || !eps_h_[1].empty() || !eps_h_[2].empty())
+      return fail(KH_ERR_INVALID, "per-voxel ε⁻¹ was already set with kh_sim_set_material");
+    geo_.clear();
+    for (int q = 0; q < n; ++q) {
+      const kh_object& o = objs[q];
+      kh::GeomObj g;
+      g.shape = o.shape;
+      g.axis = o.axis;
+      for (int a = 0; a < 3; ++a) {
+        g.c[a] = o.center[a];
+        g.s[a] = o.size[a];
+      }
+      g.eps = o.eps;
+      if (!(o.eps > 0)) return fail(KH_ERR_INVALID, "object permittivity must be positive");
+      if (o.shape == KH_SHAPE_BALL) {
+        for (int a = 0; a < 3; ++a) { g.lo[a] = o.center[a] - o.size[0]; g.hi[a] = o.center[a] + o.size[0]; }
+      } else if (o.shape == KH_SHAPE_CUBOID) {
+        for (int a = 0; a < 3; ++a) { g.lo[a] = o.center[a] - 0.5 * o.size[a]; g.hi[a] = o.center[a] + 0.5 * o.size[a]; }
+      } else if (o.shape == KH_SHAPE_CYLINDER) {
+        if (o.axis < 0 || o.axis > 2) return fail(KH_ERR_INVALID, "cylinder axis must be 0..2");
+        for (int a = 0; a < 3; ++a) {
+          const double e = a == o.axis ? 0.5 * o.size[1] : o.size[0];
+          g.lo[a] = o.center[a] - e;
+          g.hi[a] = o.center[a] + e;
+        }
+      } else {
+        return fail(KH_ERR_INVALID, "unknown shape");
+      }
+      geo_.push_back(g);
+    }
+    geo_set_ = true;
+    geo_bg_ = background;
+    geo_smooth_ = smoothing;
+    for (int a = 0; a < 3; ++a) geo_origin_[a] = origin[a];
+    return KH_OK;
+  }
+
+  kh_status read_material(int kind, int comp, double* out) override {
+    if (!prepared_) return fail(KH_ERR_INVALID, "read_material before prepare");
+    if (!out || comp < 0 || comp > 2) return fail(KH_ERR_INVALID, "bad read_material arguments");
+    const T* src = nullptr;
+    if (kind == KH_MAT_EPS_INV) src = eps_[comp];
+    else if (kind == KH_MAT_MU_INV) src = mu_[comp];
+    else if (kind == KH_MAT_SIGMA_D) src = msigd_[comp];
+    else if (kind == KH_MAT_SIGMA_B) src = msigb_[comp];
+    else if (kind == KH_MAT_CHI3) src = chi3_;
+    else return fail(KH_ERR_INVALID, "unknown material kind");
+    if (!src) return fail(KH_ERR_INVALID, "no per-voxel array of this kind");
+    std::vector<T> h(static_cast<size_t>(total_));
+    if (kh_status es = wait_idle(); es != KH_OK) return es;
+    KH_CUDA(cudaMemcpy(h.data(), src, total_ * sizeof(T), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < n_[2]; ++k)
+      for (int j = 0; j < n_[1]; ++j)
+        for (int i = 0; i < n_[0]; ++i)
+          out[(size_t(k) * n_[1] + j) * n_[0] + i] = double(h[origin_ + (long long)k * plane_ + (long long)j * pitch_ + i]);
+    return KH_OK;
+  }
+
   kh_status add_pole(const kh_pole_coeffs& c, const double* s) override {
     if (prepared_) return fail(KH_ERR_INVALID, "add_pole after prepare");
     if (int(poles_.size()) >= kh::kMaxPoles) return fail(KH_ERR_UNSUPPORTED, "too many poles");
@@ -461,6 +526,7 @@ class Sim : public SimBase {
       if (msd && sigmask_d_ && (pml_axis_[nx] || pml_axis_[pv])) KH_TRY(alloc_field(&CD_[c]));
     }
     // materials
+    if (geo_set_) KH_TRY(build_geometry());
     for (int c = 0; c < 3; ++c) {
       if (!eps_h_[c].empty()) KH_TRY(upload_center(eps_h_[c], &eps_[c], false));
       if (!mu_h_[c].empty()) KH_TRY(upload_center(mu_h_[c], &mu_[c], false));
@@ -642,7 +708,7 @@ class Sim : public SimBase {
       if (pml[c]) b += 2 * field;
       if (msb && (pml[nx] || pml[pv])) b += field;
       if (msd && (pml[nx] || pml[pv])) b += field;
-      if (!eps_h_[c].empty()) b += field;
+      if (!eps_h_[c].empty() || geo_set_) b += field;
       if (!mu_h_[c].empty()) b += field;
       if (!msigd_h_[c].empty()) b += field;
       if (!msigb_h_[c].empty()) b += field;
@@ -786,7 +852,7 @@ class Sim : public SimBase {
         for (int i = 0; i < dm[0]; ++i) {
           const T val = T(v[(size_t(k) * dm[1] + j) * dm[0] + i]);
           plane[size_t(j) * dm[0] + i] = val;
-          (*host)[(size_t(st[2] + k) * n_[1] + (st[1] + j)) * n_[0] + (st[0] + i)] = val;
+          if (!host->empty()) (*host)[(size_t(st[2] + k) * n_[1] + (st[1] + j)) * n_[0] + (st[0] + i)] = val;
         }
       T* row0 = dst + origin_ + (long long)(st[2] + k) * plane_ + (long long)st[1] * pitch_ + st[0];
       KH_CUDA(cudaMemcpy2D(row0, size_t(pitch_) * sizeof(T), plane.data(), size_t(dm[0]) * sizeof(T),
@@ -923,7 +989,7 @@ class Sim : public SimBase {
   }
 
   void model_split(double& h_bytes, double& e_bytes, double& dft_bytes) const override {
-    const bool pervox_eps = eps_h_[0].size() > 0;
+    const bool pervox_eps = eps_h_[0].size() > 0 || geo_set_;
     const bool pervox_mu = mu_h_[0].size() > 0;
     const long long cells = 1LL * n_[0] * n_[1] * n_[2];
     // H: E 3 rd + H 3 rd + H 3 wr (+ μ⁻¹ 3 rd); E: H 3 rd + E 3 rd + E 3 wr (+ ε⁻¹ 3 rd)
@@ -1386,6 +1452,45 @@ class Sim : public SimBase {
     }
   }
 
+  // kh_sim_set_geometry: rasterise (and smooth) each E component's ε⁻¹ on the
+  // device at its Yee positions.
+  kh_status build_geometry() {
+    kh::GeomObj* dobjs = nullptr;
+    if (!geo_.empty()) {
+      const kh_status su = upload_raw(geo_.data(), geo_.size() * sizeof(kh::GeomObj), (void**)&dobjs);
+      if (su != KH_OK) return su;
+    }
+    void* scratch = nullptr;
+    if (geo_smooth_ != KH_SMOOTH_NONE) KH_CUDA(kh_host::dev_alloc(&scratch, size_t(total_) * sizeof(T), cudaStreamLegacy));
+    kh_status st = KH_OK;
+    for (int c = 0; c < 3 && st == KH_OK; ++c) {
+      st = alloc_raw(size_t(total_) * sizeof(T), (void**)&eps_[c], false);
+      if (st != KH_OK) break;
+      kh::GeomArgs a;
+      a.objs = dobjs;
+      a.nobj = int(geo_.size());
+      for (int q = 0; q < 3; ++q) {
+        a.n[q] = n_[q];
+        a.d[q] = double(delta_[q]);
+        // Yee shift of E_c: −Δ/2 along both axes other than c (utils.jl:139-170)
+        a.org[q] = geo_origin_[q] - (q == c ? 0.0 : 0.5 * double(delta_[q]));
+      }
+      a.pitch = pitch_;
+      a.plane = plane_;
+      a.origin = origin_;
+      a.total = total_;
+      a.background = geo_bg_;
+      a.smoothing = geo_smooth_;
+      a.comp = c;
+      kh::launch_geometry<T>(a, eps_[c], static_cast<T*>(scratch), cudaStreamLegacy);
+      launches += geo_smooth_ != KH_SMOOTH_NONE ? 2 : 1;
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) st = fail(KH_ERR_CUDA, std::string("geometry kernels: ") + cudaGetErrorString(e));
+    }
+    if (scratch) kh_host::dev_free(scratch, cudaStreamLegacy);
+    return st;
+  }
+
   void launch_dft_for(int mi, const Cplx<T>* phase, cudaStream_t stream) {
     const Mon& m = mons_[mi];
     kh::DftParams<T> p;
@@ -1577,6 +1682,10 @@ class Sim : public SimBase {
   std::vector<SrcH> srcs_;
   std::vector<Mon> mons_;
   std::vector<Hist> hists_;
+  std::vector<kh::GeomObj> geo_;
+  bool geo_set_ = false;
+  double geo_bg_ = 1.0, geo_origin_[3] = {0, 0, 0};
+  int geo_smooth_ = KH_SMOOTH_NONE;
   bool graphs_on_ = false;
   int align_ = 1, batch_len_ = 512;
   int64_t graph_misses_ = 0, graph_hits_ = 0;
@@ -1793,6 +1902,17 @@ kh_status kh_sim_model_bytes_per_step(const kh_sim* sim, double* out) {
   if (!sim || !out) return KH_ERR_INVALID;
   *out = sim->impl->model_bytes_per_step();
   return KH_OK;
+}
+
+kh_status kh_sim_set_geometry(kh_sim* sim, const kh_object* objects, int32_t n, double background_eps,
+                              const double origin[3], int32_t smoothing) {
+  if (!sim) return KH_ERR_INVALID;
+  return sim->impl->set_geometry(objects, n, background_eps, origin, smoothing);
+}
+
+kh_status kh_sim_read_material(kh_sim* sim, int32_t kind, int32_t comp, double* out) {
+  if (!sim) return KH_ERR_INVALID;
+  return sim->impl->read_material(kind, comp, out);
 }
 
 kh_status kh_sim_graph_replays(const kh_sim* sim, int64_t* out) {

@@ -99,6 +99,9 @@ struct SimBase {
   // (their multiples replay captured step graphs).
   virtual int step_alignment() const = 0;
   virtual int64_t graph_replays() const = 0;
+  virtual kh_status set_geometry(const kh_object* objs, int n, double background, const double* origin,
+                                 int smoothing) = 0;
+  virtual kh_status read_material(int kind, int comp, double* out) = 0;
 };
 
 }  // namespace kh_host

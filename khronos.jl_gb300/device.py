@@ -74,6 +74,17 @@ class GpuSim:
                 self._check(self.lib.kh_sim_add_dft_monitor(self.handle, m.component, st, dm, len(fr),
                                                             _dptr(fr), int(m.decimation), C.byref(mid)))
                 self.monitor_ids.append(mid.value)
+            if spec.geometry is not None:
+                g = spec.geometry
+                objs = (_abi.GeomObject * max(1, len(g.objects)))()
+                for q, (shape, axis, c, sz, eps) in enumerate(g.objects):
+                    objs[q].shape, objs[q].axis, objs[q].eps = shape, axis, eps
+                    for a in range(3):
+                        objs[q].center[a] = c[a]
+                        objs[q].size[a] = sz[a]
+                org = (C.c_double * 3)(*g.origin)
+                self._check(self.lib.kh_sim_set_geometry(self.handle, objs, len(g.objects), float(g.background),
+                                                         org, int(g.smoothing)))
             self.history_ids: List[int] = []
             for h in spec.histories:
                 st = (C.c_int32 * 3)(*h.start)
@@ -181,6 +192,12 @@ class GpuSim:
         self._check(self.lib.kh_sim_step_timed(self.handle, int(nsteps), C.c_void_p(stream) if stream else None,
                                                C.byref(h), C.byref(e), C.byref(d)))
         return h.value, e.value, d.value
+
+    def material(self, kind: int, comp: int) -> np.ndarray:
+        """A per-voxel material array (Center range), indexed [i, j, k]."""
+        out = np.zeros(int(np.prod(self.spec.n)))
+        self._check(self.lib.kh_sim_read_material(self.handle, int(kind), int(comp), _dptr(out)))
+        return out.reshape(tuple(self.spec.n), order="F")
 
     def field_sq_norms(self) -> np.ndarray:
         """Σ E_c², Σ H_c² over the grid (6 values, FP64 on the device)."""

@@ -32,6 +32,10 @@ class Simulation:
     stage that makes that path grow without bound once PML is present.
 
     Materials (all optional; arrays are (Nx, Ny, Nz), cell-indexed):
+      geometry: list of geometry.Object (Ball / Cuboid / Cylinder with an
+      isotropic ε) rasterised on the device at each component's Yee position,
+      with background_eps elsewhere and subpixel_smoothing "none", "volume" or
+      "anisotropic" (instead of eps_inv arrays),
       eps_inv: scalar or 3 arrays (ε⁻¹ per Yee component), mu_inv likewise,
       sigma_d / sigma_b: 3 conductivity arrays, chi3: one Center array,
       poles: list of (LorentzianSusceptibility, σ array) — ε⁻¹ must already
@@ -40,7 +44,8 @@ class Simulation:
 
     def __init__(self, *, cell_size, resolution, sources=(), cell_center=(0.0, 0.0, 0.0),
                  boundaries=None, monitors=(), dtype="f32", courant=0.5, eps_inv=1.0, mu_inv=1.0,
-                 sigma_d=None, sigma_b=None, chi3=None, poles=(), semantics="cpml"):
+                 sigma_d=None, sigma_b=None, chi3=None, poles=(), semantics="cpml", geometry=None,
+                 background_eps=1.0, subpixel_smoothing="none"):
         self.grid = G.Grid.build(cell_size, cell_center, resolution, dtype, courant)
         self.dtype = dtype
         self.sources = list(sources)
@@ -55,6 +60,11 @@ class Simulation:
         if semantics not in ("cpml", "reference_cpu"):
             raise ValueError("semantics must be 'cpml' or 'reference_cpu'")
         self.semantics = semantics
+        if geometry is not None and not np.isscalar(eps_inv):
+            raise ValueError("give either geometry objects or per-voxel eps_inv arrays, not both")
+        self.geometry = list(geometry) if geometry is not None else None
+        self.background_eps = background_eps
+        self.subpixel_smoothing = subpixel_smoothing
         self._dev = None
         self._dft_monitors: List[DFTMonitor] = []
 
@@ -97,7 +107,11 @@ class Simulation:
                 sp.sigma_b[a] = s
                 sp.sigma_d[a] = s.copy()
         # materials
-        if np.isscalar(self.eps_inv):
+        if self.geometry is not None:  # rasterised on the device (kh_sim_set_geometry)
+            from .geometry import geometry_spec
+
+            sp.geometry = geometry_spec(self.geometry, g, self.background_eps, self.subpixel_smoothing)
+        elif np.isscalar(self.eps_inv):
             sp.eps_inv = float(T(self.eps_inv))
         else:
             for c in range(3):

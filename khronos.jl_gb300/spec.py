@@ -118,6 +118,7 @@ class SimSpec:
     sources: List[SourceSpec] = field(default_factory=list)
     monitors: List[MonitorSpec] = field(default_factory=list)
     histories: List[HistorySpec] = field(default_factory=list)
+    geometry: Optional[object] = None  # geometry.GeometrySpec: ε⁻¹ rasterised on the device
 
     @property
     def np_dtype(self):

@@ -101,7 +101,14 @@ class OracleSim:
         self.h = C.c_void_p(self.lib.khref_create(C.byref(d)))
         if not self.h:
             raise RuntimeError("oracle create failed")
-        for kind, comp, arr in spec.materials:
+        mats = list(spec.materials)
+        if getattr(spec, "geometry", None) is not None:  # the device rasterises these; restated here
+            from .geometry import eps_inv_arrays
+
+            T = np.float32 if spec.dtype == 0 else np.float64
+            for c, arr in enumerate(eps_inv_arrays(spec.geometry, spec.n, spec.delta, T)):
+                mats.append((0, c, arr.astype(np.float64)))
+        for kind, comp, arr in mats:
             h = flat_f(arr)
             self._check(self.lib.khref_set_material(self.h, kind, comp, _dptr(h)))
         for p in spec.poles:
