@@ -226,6 +226,24 @@ class Simulation:
             until = until_after_sources
         self.step(self.steps_until(until))
 
+    def run_benchmark(self, until: int) -> float:
+        """run_benchmark(sim, until) (Simulation.jl:492-527): `until` steps,
+        timed from step 10 on with the device synchronised; returns the step
+        rate in MCells/s (cells × (until − 10) / seconds / 1e6)."""
+        import time
+
+        if until <= 10:
+            raise ValueError("run_benchmark times steps 10..until: until must exceed 10")
+        self.prepare()
+        self.step(10)
+        self._dev.synchronize()
+        t0 = time.perf_counter()
+        self.step(until - 10)
+        self._dev.synchronize()
+        dt = time.perf_counter() - t0
+        n = self.grid.n
+        return n[0] * n[1] * max(1, n[2]) * (until - 10) / dt / 1e6
+
     # -- results ----------------------------------------------------------------
     def get_field(self, comp: int) -> np.ndarray:
         self.prepare()

@@ -309,3 +309,15 @@ def test_step_graphs_are_invisible(kh, gpu_lib, dtype, monkeypatch):
     assert out["1"][2] > 0
     for a, b in zip(out["0"][0] + out["0"][1], out["1"][0] + out["1"][1]):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.gpu
+def test_run_benchmark(kh, gpu_lib):
+    """run_benchmark(sim, until) mirrors the reference: steps until times and
+    returns a positive MCells/s rate."""
+    from khronos_gb300 import configs
+
+    w = configs.dipole(dtype="f32", resolution=10)
+    rate = w.sim.run_benchmark(60)
+    assert rate > 0 and w.sim.timestep == 60
+    w.sim.close()
