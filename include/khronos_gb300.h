@@ -225,10 +225,11 @@ kh_status kh_sim_monitor_info(const kh_sim* sim, int32_t monitor_id, int32_t dim
 kh_status kh_sim_flux(kh_sim* sim, const int32_t ids[4], int32_t normal_axis, double dA,
                       double* out);
 /* kh_sim_flux without any device allocation (no counterpart in the reference).
- * For callers that must not allocate or free device memory while they run:
- * a cudaFree synchronises the whole device, stalling simulations running on
- * other streams, and a process whose device memory is fully committed to its
- * simulations may have nothing left for even a small cudaMalloc.  The
+ * For callers that must not allocate device memory while they run:
+ * kh_sim_flux takes its per-frequency buffer from the library's device memory
+ * pool, and a process whose device memory is fully committed to its
+ * simulations may have nothing left for even that small allocation (nor may
+ * code that forbids allocations inside its own critical sections).  The
  * per-frequency sums go to a fixed device array inside the library instead:
  * at most 4096 frequencies (more returns KH_ERR_INVALID; use kh_sim_flux).
  * The first call on each device does a one-time set-up (it resolves that
