@@ -54,7 +54,7 @@ from typing import Callable, List, Optional, Sequence
 
 import numpy as np
 
-from .spec import MAT_EPS_INV, KH_F32, HistorySpec, MonitorSpec, SimSpec, SourceSpec, TIME_TABLE
+from .spec import MAT_CHI3, MAT_EPS_INV, KH_F32, HistorySpec, MonitorSpec, SimSpec, SourceSpec, TIME_TABLE
 
 
 @dataclass
@@ -266,6 +266,11 @@ class OptimizationProblem:
         eps = [a for (k, c, a) in self.base.materials if k == MAT_EPS_INV]
         if len(eps) != 3:
             raise ValueError("the forward spec needs per-voxel ε⁻¹ arrays for all three components")
+        # the adjoint runs the same kernels as the forward run, which is exact
+        # for a linear system (dielectrics, conductors, Lorentz/Drude poles);
+        # a χ3 medium makes the step nonlinear
+        if any(k == MAT_CHI3 and np.any(np.asarray(a) != 0) for (k, c, a) in self.base.materials):
+            raise ValueError("adjoint gradients need a linear system: the spec carries χ3")
 
     def _np_T(self):
         return np.float32 if self.base.dtype == KH_F32 else np.float64

@@ -397,3 +397,42 @@ def test_fourier_fields_objective_matches_oracle(kh, oracle, gpu_lib, mode, step
     assert abs(f0 - oadj.objective(opt, rho)) <= 1e-10 * abs(f0)
     assert np.max(np.abs(g - g_ref)) <= 1e-9 * np.max(np.abs(g_ref))
     opt.close()
+
+
+def test_adjoint_with_dispersive_media_on_the_oracle(kh, oracle):
+    """Lorentz and Drude poles elsewhere in the domain keep the system
+    reciprocal: the windowed adjoint still equals central differences."""
+    import oracle.adjoint as oadj
+    from khronos_gb300.simulation import apply_chi1_correction
+    from khronos_gb300.spec import (MAT_EPS_INV, DrudeSusceptibility, LorentzianSusceptibility, PoleSpec,
+                                    ade_coefficients)
+
+    opt, rho = make_problem("f64", 700, 2, small=True)
+    sp = opt.base
+    n = sp.n
+    ii, jj, kk = np.meshgrid(*[np.arange(n[a]) + 0.5 for a in range(3)], indexing="ij")
+    lor, dru = LorentzianSusceptibility(1.0, 0.05, 1.0), DrudeSusceptibility(0.1, 30.0)
+    s_l = np.where((ii - 8) ** 2 + (jj - 15) ** 2 + (kk - 8) ** 2 <= 2.5 ** 2, lor.sigma, 0.0)
+    s_d = np.where((ii - 8) ** 2 + (jj - 5) ** 2 + (kk - 9) ** 2 <= 2.0 ** 2, dru.sigma, 0.0)
+    poles = [(lor, s_l), (dru, s_d)]
+    sp.poles = [PoleSpec(coeffs=ade_coefficients(s, float(sp.dt)), sigma=g) for s, g in poles]
+    eps = apply_chi1_correction([a for (k, c, a) in sp.materials if k == MAT_EPS_INV], poles, sp.dt)
+    sp.materials = [(k, c, a) for (k, c, a) in sp.materials if k != MAT_EPS_INV] + [
+        (MAT_EPS_INV, c, eps[c]) for c in range(3)]
+    opt._build_specs()
+    g, _ = oadj.gradient(opt, rho)
+    idx = [(0, 0, 0), (2, 3, 1)]
+    fd = oadj.fd_gradient(opt, rho, idx)
+    for i, f in zip(idx, fd):
+        assert abs(g[i] - f) <= FD_TOL * abs(f), (i, g[i], f)
+
+
+def test_adjoint_rejects_nonlinear_media(kh):
+    from khronos_gb300.adjoint import OptimizationProblem, power_overlap
+    from khronos_gb300.spec import MAT_CHI3
+
+    opt, _ = make_problem("f64", 10, 1, small=True)
+    sp = opt.base
+    sp.materials = list(sp.materials) + [(MAT_CHI3, 0, np.full(sp.n, 1e-3))]
+    with pytest.raises(ValueError, match="linear"):
+        OptimizationProblem(sp, power_overlap, opt.objective_arguments, opt.design_region, opt.frequencies, 10)
