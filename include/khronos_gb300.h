@@ -329,6 +329,13 @@ kh_status kh_history_correlate(kh_sim* fwd, const int32_t fwd_ids[3], kh_sim* ad
  * check (a non-finite field gives a non-finite norm). */
 kh_status kh_sim_field_sq_norms(kh_sim* sim, double out[6]);
 
+/* KH_OK while every E and H value is finite, KH_ERR_NAN (the message names
+ * the first non-finite component) once a run has diverged, e.g. a time step
+ * above the Courant limit.  One FP64 norm pass over the fields; the step
+ * loop itself never checks, as the reference's run loop does not
+ * (src/Simulation.jl:295-382). */
+kh_status kh_sim_check_finite(kh_sim* sim);
+
 /* Device memory: what kh_sim_prepare will allocate (estimate, available
  * before prepare; estimate_memory, src/Memory.jl:120-251) and what it has
  * allocated (0 before prepare). */

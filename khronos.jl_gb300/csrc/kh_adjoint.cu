@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <string>
 #include <vector>
 
@@ -319,6 +320,18 @@ kh_status kh_sim_read_history(kh_sim* sim, int32_t id, int64_t step, double* out
   for (long long q = 0; q < h.ncell; ++q)
     out[q] = h.dtype == KH_F32 ? double(reinterpret_cast<const float*>(buf.data())[q])
                                : reinterpret_cast<const double*>(buf.data())[q];
+  return KH_OK;
+}
+
+kh_status kh_sim_check_finite(kh_sim* sim) {
+  if (!sim) return KH_ERR_INVALID;
+  double n[6];
+  kh_status st = kh_sim_field_sq_norms(sim, n);
+  if (st != KH_OK) return st;
+  static const char* names[6] = {"Ex", "Ey", "Ez", "Hx", "Hy", "Hz"};
+  for (int c = 0; c < 6; ++c)
+    if (!std::isfinite(n[c]))
+      return fail(sim, KH_ERR_NAN, std::string("non-finite values in ") + names[c]);
   return KH_OK;
 }
 

@@ -205,6 +205,10 @@ class GpuSim:
         self._check(self.lib.kh_sim_field_sq_norms(self.handle, _dptr(out)))
         return out
 
+    def check_finite(self) -> None:
+        """Raise KhronosError(KH_ERR_NAN) once any field value is non-finite."""
+        self._check(self.lib.kh_sim_check_finite(self.handle))
+
     # -- adjoint support -------------------------------------------------------
     def update_material_box(self, kind: int, comp: int, start, values: np.ndarray):
         """Overwrite per-voxel ε⁻¹/μ⁻¹ of one component over the cell box
