@@ -218,6 +218,28 @@ kh_status kh_sim_graph_replays(const kh_sim* sim, int64_t* out);
 
 /* Results. */
 kh_status kh_sim_get_field(kh_sim* sim, int32_t component, double* out);
+
+/* A field component in place on the device, without a copy: element
+ * (i, j, k) of the component's dims (the Center range plus the staggered
+ * N+1 layer, as kh_sim_get_field) sits at
+ *   data + i·strides[0] + j·strides[1] + k·strides[2]   (strides in elements),
+ * of type dtype (KH_F32 / KH_F64).  Neighbours at −1 and dims are the zero
+ * ghost ring.  The memory belongs to the simulation: valid until
+ * kh_sim_destroy, its values current once the steps queued on it have
+ * finished (kh_sim_synchronize, or an event on the stepping stream).
+ * Writes through it change the simulation; values at cells that keep B/D
+ * state (CPML, source, χ3, pole cells) are recomputed from that state at the
+ * next step.  The zero-copy counterpart of the reference's fields
+ * (sim.fields.fEx … as device arrays, DataStructures.jl:100-148) for
+ * device-side post-processing; a Julia shim wraps it with unsafe_wrap and a
+ * strided view. */
+typedef struct {
+  void* data;
+  int32_t dtype;
+  int32_t dims[3];
+  int64_t strides[3];
+} kh_field_view;
+kh_status kh_sim_field_view(kh_sim* sim, int32_t component, kh_field_view* out);
 kh_status kh_sim_read_dft(kh_sim* sim, int32_t monitor_id, double* out);
 kh_status kh_sim_monitor_info(const kh_sim* sim, int32_t monitor_id, int32_t dims[3], int32_t* nfreq);
 /* Poynting flux of four DFT monitors (E1, E2, H1, H2 tangential), FP64 on the

@@ -82,6 +82,15 @@ class GeomObject(C.Structure):
     ]
 
 
+class FieldView(C.Structure):
+    _fields_ = [
+        ("data", C.c_void_p),
+        ("dtype", C.c_int32),
+        ("dims", C.c_int32 * 3),
+        ("strides", C.c_int64 * 3),
+    ]
+
+
 class ServerDesc(C.Structure):
     _fields_ = [
         ("budget_bytes", C.c_int64),
@@ -154,6 +163,7 @@ SIGNATURES = {
                                          C.c_int64, C.c_double, C.POINTER(C.c_double)]),
     "kh_sim_field_sq_norms": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double)]),
     "kh_sim_check_finite": (C.c_int32, [C.c_void_p]),
+    "kh_sim_field_view": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(FieldView)]),
     "kh_server_create": (C.c_int32, [C.POINTER(ServerDesc), C.POINTER(C.c_void_p)]),
     "kh_server_submit": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
     "kh_server_wait": (C.c_int32, [C.c_void_p, C.c_int64, C.c_double]),

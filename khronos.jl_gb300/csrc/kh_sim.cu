@@ -144,6 +144,10 @@ namespace {
     }                                                                          \
   } while (0)
 
+// Extra staggered layer per axis of Ex, Ey, Ez, Hx, Hy, Hz: component dims are
+// n + kStagger[c] (src/utils.jl:26-37).
+constexpr int kStagger[6][3] = {{0, 1, 1}, {1, 0, 1}, {1, 1, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+
 template <typename T>
 class Sim : public SimBase {
  public:
@@ -738,8 +742,7 @@ class Sim : public SimBase {
     if (kh_status es = wait_idle(); es != KH_OK) return es;
     KH_CUDA(cudaMemcpy(h.data(), comp < 3 ? E_[comp] : H_[comp - 3], total_ * sizeof(T),
                        cudaMemcpyDeviceToHost));
-    static const int add[6][3] = {{0, 1, 1}, {1, 0, 1}, {1, 1, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
-    const int cd[3] = {n_[0] + add[comp][0], n_[1] + add[comp][1], n_[2] + add[comp][2]};
+    const int cd[3] = {n_[0] + kStagger[comp][0], n_[1] + kStagger[comp][1], n_[2] + kStagger[comp][2]};
     for (int k = 0; k < cd[2]; ++k)
       for (int j = 0; j < cd[1]; ++j)
         for (int i = 0; i < cd[0]; ++i)
@@ -928,6 +931,19 @@ class Sim : public SimBase {
       out[3 + c] = H_[c];
     }
     *count = total_;
+    return KH_OK;
+  }
+
+  kh_status field_view(int comp, kh_field_view* out) override {
+    if (!prepared_) return fail(KH_ERR_INVALID, "field view before prepare");
+    if (comp < 0 || comp > 5 || !out) return fail(KH_ERR_INVALID, "bad field view arguments");
+    T* base = comp < 3 ? E_[comp] : H_[comp - 3];
+    out->data = base + origin_;
+    out->dtype = dtype();
+    for (int a = 0; a < 3; ++a) out->dims[a] = n_[a] + kStagger[comp][a];
+    out->strides[0] = 1;
+    out->strides[1] = pitch_;
+    out->strides[2] = plane_;
     return KH_OK;
   }
 
@@ -1835,6 +1851,11 @@ kh_status kh_sim_launch_count(const kh_sim* sim, int64_t* out) {
 kh_status kh_sim_get_field(kh_sim* sim, int32_t component, double* out) {
   if (!sim) return KH_ERR_INVALID;
   return sim->impl->get_field(component, out);
+}
+
+kh_status kh_sim_field_view(kh_sim* sim, int32_t component, kh_field_view* out) {
+  if (!sim) return KH_ERR_INVALID;
+  return sim->impl->field_view(component, out);
 }
 
 kh_status kh_sim_read_dft(kh_sim* sim, int32_t monitor_id, double* out) {

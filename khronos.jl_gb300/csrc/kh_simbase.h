@@ -92,6 +92,7 @@ struct SimBase {
   // Device arrays of E_x..E_z, H_x..H_z (padded layout, `count` elements each,
   // zero outside the grid), valid once this simulation's queued work is done.
   virtual kh_status field_arrays(const void* out[6], long long* count) = 0;
+  virtual kh_status field_view(int comp, kh_field_view* out) = 0;
   virtual kh_status add_history(int comp, const int32_t* st, const int32_t* dm, int64_t capacity,
                                 int32_t* id) = 0;
   virtual kh_status history_view(int id, HistoryView* out) = 0;

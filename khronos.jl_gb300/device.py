@@ -159,6 +159,31 @@ class GpuSim:
         self._check(self.lib.kh_sim_get_field(self.handle, comp, _dptr(out)))
         return out.reshape(dims, order="F")
 
+    def field_view(self, comp: int):
+        """Component `comp` in place on the device as a torch tensor indexed
+        [i, j, k] (no copy; strided over the padded layout).  Its values are
+        current after synchronize(); it keeps this simulation from being
+        garbage-collected, and is invalid after close()."""
+        import torch
+
+        v = _abi.FieldView()
+        self._check(self.lib.kh_sim_field_view(self.handle, comp, C.byref(v)))
+        item = 4 if v.dtype == _abi.KH_F32 else 8
+
+        class _Holder:
+            pass
+
+        h = _Holder()
+        h.sim = self
+        h.__cuda_array_interface__ = {
+            "shape": tuple(int(d) for d in v.dims),
+            "typestr": "<f4" if item == 4 else "<f8",
+            "strides": tuple(int(s) * item for s in v.strides),
+            "data": (int(v.data), False),
+            "version": 2,
+        }
+        return torch.as_tensor(h, device=torch.device("cuda", torch.cuda.current_device()))
+
     def dft(self, monitor_index: int) -> np.ndarray:
         """DFT accumulator of a monitor, shape (Nx, Ny, Nz, Nf), complex128."""
         m = self.spec.monitors[monitor_index]

@@ -321,3 +321,34 @@ def test_run_benchmark(kh, gpu_lib):
     rate = w.sim.run_benchmark(60)
     assert rate > 0 and w.sim.timestep == 60
     w.sim.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dtype", ["f32", "f64"])
+def test_field_view_is_the_field_in_place(kh, gpu_lib, dtype):
+    """kh_sim_field_view: a zero-copy strided view equal to kh_sim_get_field,
+    that follows later steps, and whose device-side norm matches
+    kh_sim_field_sq_norms."""
+    import torch
+
+    from khronos_gb300 import configs
+    from khronos_gb300.device import GpuSim
+
+    w = configs.waveguide(dtype=dtype, scale=0.25)
+    g = GpuSim(w.sim.spec(), lib=gpu_lib)
+    g.step(120)
+    g.synchronize()
+    views = [g.field_view(c) for c in range(6)]
+    for c in range(6):
+        host = g.field(c)
+        assert tuple(views[c].shape) == host.shape
+        assert np.array_equal(views[c].double().cpu().numpy(), host)
+    g.step(40)
+    g.synchronize()
+    norms = g.field_sq_norms()
+    for c in range(6):
+        assert np.array_equal(views[c].double().cpu().numpy(), g.field(c))
+        dev = float(torch.sum(views[c].double() ** 2))
+        assert math.isclose(dev, norms[c], rel_tol=1e-12, abs_tol=1e-300)
+    del views
+    g.close()
