@@ -9,15 +9,16 @@ This package is the host side: the set-up arithmetic of the reference's
 from .grid import CENTER, EX, EY, EZ, HX, HY, HZ, Grid, GridVolume, interpolation_weight
 from .monitors import DFTMonitor, FluxMonitor, flux_from_dft
 from .simulation import Simulation, apply_chi1_correction
-from .sources import (ContinuousWaveSource, CustomSource, GaussianPulseSource, ProfileSource,
-                      UniformSource)
+from .sources import (ContinuousWaveSource, CustomSource, GaussianPulseSource, PlaneWaveSource,
+                      ProfileSource, UniformSource)
 from .spec import (DrudeSusceptibility, LorentzianSusceptibility, SimSpec, ade_coefficients,
                    eval_susceptibility)
 
 __all__ = [
     "CENTER", "EX", "EY", "EZ", "HX", "HY", "HZ", "Grid", "GridVolume", "interpolation_weight",
     "DFTMonitor", "FluxMonitor", "flux_from_dft", "Simulation", "apply_chi1_correction",
-    "ContinuousWaveSource", "CustomSource", "GaussianPulseSource", "ProfileSource", "UniformSource",
+    "ContinuousWaveSource", "CustomSource", "GaussianPulseSource", "PlaneWaveSource", "ProfileSource",
+    "UniformSource",
     "DrudeSusceptibility", "LorentzianSusceptibility", "SimSpec", "ade_coefficients",
     "eval_susceptibility",
 ]
