@@ -351,6 +351,12 @@ kh_status kh_history_correlate(kh_sim* fwd, const int32_t fwd_ids[3], kh_sim* ad
  * check (a non-finite field gives a non-finite norm). */
 kh_status kh_sim_field_sq_norms(kh_sim* sim, double out[6]);
 
+/* L2 norm sqrt(Σ|F|²) of each DFT monitor's accumulated array (all cells and
+ * frequencies), FP64 on the device, out[id] for id = 0 .. monitors−1:
+ * dft_fields_norm (src/Simulation.jl:530-539), the quantity
+ * stop_when_dft_decayed tracks (src/Simulation.jl:411-485). */
+kh_status kh_sim_dft_norms(kh_sim* sim, double* out);
+
 /* KH_OK while every E and H value is finite, KH_ERR_NAN (the message names
  * the first non-finite component) once a run has diverged, e.g. a time step
  * above the Courant limit.  One FP64 norm pass over the fields; the step

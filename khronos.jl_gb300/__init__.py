@@ -8,7 +8,7 @@ This package is the host side: the set-up arithmetic of the reference's
 """
 from .grid import CENTER, EX, EY, EZ, HX, HY, HZ, Grid, GridVolume, interpolation_weight
 from .monitors import DFTMonitor, FluxMonitor, flux_from_dft
-from .simulation import Simulation, apply_chi1_correction
+from .simulation import Simulation, apply_chi1_correction, stop_when_dft_decayed
 from .sources import (ContinuousWaveSource, CustomSource, GaussianPulseSource, PlaneWaveSource,
                       ProfileSource, UniformSource)
 from .spec import (DrudeSusceptibility, LorentzianSusceptibility, SimSpec, ade_coefficients,
@@ -17,6 +17,7 @@ from .spec import (DrudeSusceptibility, LorentzianSusceptibility, SimSpec, ade_c
 __all__ = [
     "CENTER", "EX", "EY", "EZ", "HX", "HY", "HZ", "Grid", "GridVolume", "interpolation_weight",
     "DFTMonitor", "FluxMonitor", "flux_from_dft", "Simulation", "apply_chi1_correction",
+    "stop_when_dft_decayed",
     "ContinuousWaveSource", "CustomSource", "GaussianPulseSource", "PlaneWaveSource", "ProfileSource",
     "UniformSource",
     "DrudeSusceptibility", "LorentzianSusceptibility", "SimSpec", "ade_coefficients",

@@ -85,6 +85,23 @@ __global__ void __launch_bounds__(kRedThreads) overlap_final_kernel(const double
   if (threadIdx.x == 0) out[f] = s;
 }
 
+// Squared norm Σ|F|² of one DFT array (all cells and frequencies): block b
+// sums its contiguous chunk.
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) dft_sq_partial_kernel(const Cplx<T>* F, const Cplx<T>* C,
+                                                                     long long total, long long chunk,
+                                                                     double2* partial) {
+  const long long lo = (long long)blockIdx.x * chunk;
+  const long long hi = min(total, lo + chunk);
+  double s = 0.0;
+  for (long long q = lo + threadIdx.x; q < hi; q += kRedThreads) {
+    const double2 v = dft_value(F, C, q);
+    s += v.x * v.x + v.y * v.y;
+  }
+  const double2 r = block_sum(s, 0.0);
+  if (threadIdx.x == 0) partial[blockIdx.x] = r;
+}
+
 // Squared L2 norm of one field array: block (b, c) sums x² over its chunk.
 template <typename T>
 struct FieldArgs {
@@ -332,6 +349,49 @@ kh_status kh_sim_check_finite(kh_sim* sim) {
   for (int c = 0; c < 6; ++c)
     if (!std::isfinite(n[c]))
       return fail(sim, KH_ERR_NAN, std::string("non-finite values in ") + names[c]);
+  return KH_OK;
+}
+
+kh_status kh_sim_dft_norms(kh_sim* sim, double* out) {
+  if (!sim) return KH_ERR_INVALID;
+  if (!out) return fail(sim, KH_ERR_INVALID, "null output");
+  std::vector<MonitorView> ms(size_t(sim->impl->monitor_count()));
+  for (size_t id = 0; id < ms.size(); ++id) {
+    const kh_status st = sim->impl->monitor_view(int(id), &ms[id]);
+    if (st != KH_OK) return st;
+  }
+  if (ms.empty()) return KH_OK;
+  kh_status st = sim->impl->wait_idle();
+  if (st != KH_OK) return st;
+  const long long chunk = 16LL * kRedThreads;
+  std::vector<long long> nblk(ms.size());
+  long long tot_blk = 0;
+  for (size_t i = 0; i < ms.size(); ++i) {
+    nblk[i] = std::max<long long>(1, (ms[i].ncell() * ms[i].nf + chunk - 1) / chunk);
+    tot_blk += nblk[i];
+  }
+  DevBuf part, res;
+  KH_ACUDA(sim, kh_host::dev_alloc(&part.p, size_t(tot_blk) * sizeof(double2), cudaStreamLegacy));
+  KH_ACUDA(sim, kh_host::dev_alloc(&res.p, ms.size() * sizeof(double2), cudaStreamLegacy));
+  long long off = 0;
+  for (size_t i = 0; i < ms.size(); ++i) {
+    const MonitorView& m = ms[i];
+    double2* pp = static_cast<double2*>(part.p) + off;
+    const long long total = m.ncell() * m.nf;
+    if (m.dtype == KH_F32)
+      dft_sq_partial_kernel<float><<<unsigned(nblk[i]), kRedThreads>>>(
+          static_cast<const Cplx<float>*>(m.F), static_cast<const Cplx<float>*>(m.C), total, chunk, pp);
+    else
+      dft_sq_partial_kernel<double><<<unsigned(nblk[i]), kRedThreads>>>(
+          static_cast<const Cplx<double>*>(m.F), static_cast<const Cplx<double>*>(m.C), total, chunk, pp);
+    overlap_final_kernel<<<1, kRedThreads>>>(pp, int(nblk[i]), static_cast<double2*>(res.p) + i);
+    off += nblk[i];
+  }
+  sim->impl->launches += 2 * int64_t(ms.size());
+  KH_ACUDA(sim, cudaGetLastError());
+  std::vector<double2> h(ms.size());
+  KH_ACUDA(sim, cudaMemcpy(h.data(), res.p, h.size() * sizeof(double2), cudaMemcpyDeviceToHost));
+  for (size_t i = 0; i < ms.size(); ++i) out[i] = std::sqrt(h[i].x);
   return KH_OK;
 }
 

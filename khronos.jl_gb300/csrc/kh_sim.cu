@@ -922,6 +922,8 @@ class Sim : public SimBase {
     return KH_OK;
   }
 
+  int monitor_count() const override { return int(mons_.size()); }
+
   int dtype() const override { return sizeof(T) == 4 ? KH_F32 : KH_F64; }
 
   kh_status field_arrays(const void* out[6], long long* count) override {

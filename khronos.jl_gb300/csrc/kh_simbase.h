@@ -88,6 +88,7 @@ struct SimBase {
                                   const double* table, double cutoff) = 0;
   // Device arrays of a monitor, valid once this simulation's queued work is done.
   virtual kh_status monitor_view(int id, MonitorView* out) = 0;
+  virtual int monitor_count() const = 0;
   virtual int dtype() const = 0;
   // Device arrays of E_x..E_z, H_x..H_z (padded layout, `count` elements each,
   // zero outside the grid), valid once this simulation's queued work is done.

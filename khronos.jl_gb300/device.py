@@ -230,6 +230,12 @@ class GpuSim:
         self._check(self.lib.kh_sim_field_sq_norms(self.handle, _dptr(out)))
         return out
 
+    def dft_norms(self) -> np.ndarray:
+        """sqrt(Σ|F|²) of every DFT monitor of the spec (in spec order), FP64 on the device."""
+        out = np.zeros(max(1, max(self.monitor_ids, default=0) + 1))
+        self._check(self.lib.kh_sim_dft_norms(self.handle, _dptr(out)))
+        return np.array([out[m] for m in self.monitor_ids])
+
     def check_finite(self) -> None:
         """Raise KhronosError(KH_ERR_NAN) once any field value is non-finite."""
         self._check(self.lib.kh_sim_check_finite(self.handle))

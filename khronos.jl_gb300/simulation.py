@@ -1,16 +1,17 @@
 """Simulation: host mirror of Khronos's user API over the CUDA step loop.
 
 Mirrors the reference's ``Simulation(...)`` / ``prepare_simulation!`` /
-``run(sim; until, until_after_sources)`` / ``get_flux`` calls
-(src/DataStructures.jl:714-801, src/Simulation.jl:92-387,
-src/Monitors/FluxMonitor.jl:92-156).  Geometry is given as per-voxel material
+``run(sim; until, until_after_sources)`` (a time or a stop function such as
+``stop_when_dft_decayed``) / ``get_flux`` calls (src/DataStructures.jl:714-801,
+src/Simulation.jl:92-539, src/Monitors/FluxMonitor.jl:92-156).  Geometry is given as per-voxel material
 arrays on the Center range (rasterisation of shapes is set-up, not part of the
 step loop); everything else follows the reference's arithmetic.
 """
 from __future__ import annotations
 
 import math
-from typing import List, Optional, Sequence
+import warnings
+from typing import Callable, List, Optional, Sequence, Union
 
 import numpy as np
 
@@ -67,6 +68,7 @@ class Simulation:
         self.subpixel_smoothing = subpixel_smoothing
         self._dev = None
         self._dft_monitors: List[DFTMonitor] = []
+        self._norm_cache = None
 
     # -- convenience --------------------------------------------------------
     @property
@@ -211,8 +213,17 @@ class Simulation:
             n += 1
         return n
 
-    def run(self, until: Optional[float] = None, until_after_sources: Optional[float] = None):
-        """run(sim; until | until_after_sources) (Simulation.jl:295-382)."""
+    def run(self, until: Union[float, Callable, None] = None,
+            until_after_sources: Union[float, Callable, None] = None):
+        """run(sim; until | until_after_sources) (Simulation.jl:295-382).
+
+        Each is a time or a function ``f(sim) -> bool`` called before every
+        step, the run ending at the first True (``stop_when_dft_decayed``).
+        With ``until_after_sources`` the run first steps while
+        ``round_time <= last_source_time``.  A function may also offer
+        ``steps_before_decision(sim)``: how many steps from now it would
+        answer False without changing any state; those steps are then taken
+        in one batch instead of one call per step."""
         if (until is None) == (until_after_sources is None):
             raise ValueError("Must specify exactly one of until / until_after_sources")
         self.prepare()
@@ -224,7 +235,37 @@ class Simulation:
                 n += 1
             self.step(n)
             until = until_after_sources
-        self.step(self.steps_until(until))
+        if not callable(until):
+            self.step(self.steps_until(until))
+            return
+        skip = getattr(until, "steps_before_decision", None)
+        while True:
+            k = skip(self) if skip is not None else 0
+            if k > 0:
+                self.step(k)
+                continue
+            if until(self):
+                return
+            self.step(1)
+
+    def dft_fields_norms(self) -> np.ndarray:
+        """dft_fields_norm of every DFT monitor, flux sub-monitors included
+        (Simulation.jl:530-539): sqrt(Σ|F|²) over its accumulated array,
+        reduced in FP64 on the device.  Re-read only when a monitor has
+        updated since the last read (an update happens in the step taken at
+        timestep s when s is a multiple of its decimation)."""
+        self.prepare()
+        ts = self.timestep
+        c = self._norm_cache
+        if c is not None:
+            t0, norms = c
+            if t0 == ts or (t0 < ts and not any(s % m.decimation == 0 for s in range(t0, ts)
+                                                for m in self._dft_monitors)):
+                self._norm_cache = (ts, norms)
+                return norms
+        norms = self._dev.dft_norms()
+        self._norm_cache = (ts, norms)
+        return norms
 
     def run_benchmark(self, until: int) -> float:
         """run_benchmark(sim, until) (Simulation.jl:492-527): `until` steps,
@@ -243,6 +284,14 @@ class Simulation:
         dt = time.perf_counter() - t0
         n = self.grid.n
         return n[0] * n[1] * max(1, n[2]) * (until - 10) / dt / 1e6
+
+    def reset_fields(self):
+        """reset_fields! (Simulation.jl:571-637): fields, auxiliary state, DFT
+        accumulators and the step counter back to zero; materials, sources
+        and monitors stay."""
+        self.prepare()
+        self._dev.reset()
+        self._norm_cache = None
 
     # -- results ----------------------------------------------------------------
     def get_field(self, comp: int) -> np.ndarray:
@@ -267,6 +316,72 @@ class Simulation:
         if self._dev is not None:
             self._dev.close()
             self._dev = None
+
+
+class stop_when_dft_decayed:
+    """stop_when_dft_decayed(; tolerance, minimum_runtime, maximum_runtime)
+    (Simulation.jl:411-485): a stop function for ``run`` that is True once
+    every DFT monitor that has seen signal has a step-to-step change of its
+    norm at most ``tolerance`` times the largest change it has seen.
+
+    The reference's logic, call for call: nothing before ``minimum_runtime``;
+    True (with a warning) past ``maximum_runtime``; a monitor's first nonzero
+    norm only records it; a monitor with no change yet keeps the run going;
+    no active monitor keeps it going.  The norm of a decimated monitor does
+    not change between its updates, so on those steps its change is 0: once
+    each monitor has changed once after the first record, the next step
+    without an update reports convergence.  Reproduced as is.
+    """
+
+    def __init__(self, tolerance: float = 1e-6, minimum_runtime: float = 0.0,
+                 maximum_runtime: float = math.inf):
+        if minimum_runtime > maximum_runtime:
+            raise ValueError(f"Minimum runtime ({minimum_runtime}) cannot be greater than maximum "
+                             f"runtime ({maximum_runtime}).")
+        self.tolerance = tolerance
+        self.minimum_runtime = minimum_runtime
+        self.maximum_runtime = maximum_runtime
+        self.state = {}  # monitor index -> (previous norm, largest change)
+
+    def __call__(self, sim) -> bool:
+        t = sim.round_time()
+        if t < self.minimum_runtime:
+            return False
+        if t > self.maximum_runtime:
+            warnings.warn("Maximum runtime reached.")
+            return True
+        all_converged = True
+        n_active = 0
+        for i, cur in enumerate(sim.dft_fields_norms()):
+            cur = float(cur)
+            if cur == 0.0:
+                continue
+            if i not in self.state:
+                self.state[i] = (cur, 0.0)
+                all_converged = False
+                continue
+            prev, maxchange = self.state[i]
+            change = abs(cur - prev)
+            maxchange = max(maxchange, change)
+            self.state[i] = (cur, maxchange)
+            if maxchange == 0.0:
+                all_converged = False
+                continue
+            n_active += 1
+            if change / maxchange > self.tolerance:
+                all_converged = False
+        if n_active == 0:
+            return False
+        return all_converged
+
+    def steps_before_decision(self, sim) -> int:
+        """Steps from now whose calls would return False untouched (before
+        the minimum runtime)."""
+        ts = sim.timestep
+        n = 0
+        while sim.round_time(ts + n) < self.minimum_runtime:
+            n += 1
+        return n
 
 
 def apply_chi1_correction(eps_inv, poles, dt, T=np.float64):
