@@ -364,6 +364,15 @@ kh_status kh_sim_dft_norms(kh_sim* sim, double* out);
  * (src/Simulation.jl:295-382). */
 kh_status kh_sim_check_finite(kh_sim* sim);
 
+/* Bounds-checked builds of the library (compiled with KH_DEBUG_BOUNDS, a
+ * stand-in for a memory sanitizer): every global and shared-memory index of
+ * the step kernels (half-steps, source terms, DFT, history recording) is
+ * tested against its array's extent; a violating access is skipped and
+ * recorded.  Returns (and clears) the number of violations since the last
+ * call, with the first one's index and site code.  KH_ERR_UNSUPPORTED from
+ * the regular build.  No counterpart in the reference. */
+kh_status kh_debug_bounds(int64_t* count, int64_t* index, int32_t* site);
+
 /* Device memory: what kh_sim_prepare will allocate (estimate, available
  * before prepare; estimate_memory, src/Memory.jl:120-251) and what it has
  * allocated (0 before prepare). */

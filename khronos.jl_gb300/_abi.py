@@ -163,6 +163,7 @@ SIGNATURES = {
                                          C.c_int64, C.c_double, C.POINTER(C.c_double)]),
     "kh_sim_field_sq_norms": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double)]),
     "kh_sim_check_finite": (C.c_int32, [C.c_void_p]),
+    "kh_debug_bounds": (C.c_int32, [C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int32)]),
     "kh_sim_dft_norms": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double)]),
     "kh_sim_field_view": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(FieldView)]),
     "kh_server_create": (C.c_int32, [C.POINTER(ServerDesc), C.POINTER(C.c_void_p)]),

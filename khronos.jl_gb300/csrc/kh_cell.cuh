@@ -50,6 +50,20 @@ __device__ __forceinline__ void vzero(T (&v)[VN]) {
   for (int q = 0; q < VN; ++q) v[q] = T(0);
 }
 
+// Vector load / store of elements base[q .. q+VN-1] of an array of n
+// elements, bounds-checked in KH_DEBUG_BOUNDS builds (a load out of range
+// reads zeros, a store is skipped).
+template <typename T, int VN>
+__device__ __forceinline__ void vld_at(const T* base, long long q, long long n, int site, T (&v)[VN]) {
+  if (KH_IN(q, n, site) && KH_IN(q + VN - 1, n, site)) vld(base + q, v);
+  else vzero(v);
+}
+
+template <typename T, int VN>
+__device__ __forceinline__ void vst_at(T* base, long long q, long long n, int site, const T (&v)[VN]) {
+  if (KH_IN(q, n, site) && KH_IN(q + VN - 1, n, site)) vst(base + q, v);
+}
+
 // Update of one cell that carries a source, χ3, a pole or a material
 // conductivity (and may also sit in a CPML region).  t/u/w are the cell's B|D
 // state and CPML U/W values (loaded and stored by the caller), m its μ⁻¹|ε⁻¹,
@@ -75,10 +89,13 @@ __device__ __forceinline__ void general_cell(const HalfStepParams<T>& p, long lo
   bool h0 = false, h1 = false, h2 = false;
   if (p.sources_active && (cls & (H ? kHasSrcH : kHasSrcE))) {
     const int slot = int(cls >> kSlotShift);
-    const int e1 = p.slot_off[slot + 1];
-    for (int e = p.slot_off[slot]; e < e1; ++e) {
+    const bool slot_ok = KH_IN(slot + 1, p.n_slots + 1, 1001);
+    const int e1 = slot_ok ? p.slot_off[slot + 1] : 0;
+    for (int e = slot_ok ? p.slot_off[slot] : 0; e < e1; ++e) {
+      if (!KH_IN(e, p.n_ent, 1002)) break;
       const int c = p.ent_comp[e] - (H ? 3 : 0);  // entries carry components 0..5
       const Cplx<T> am = p.ent_amp[e];
+      if (!KH_IN(p.ent_src[e], p.n_src, 1003)) continue;
       const Cplx<T> fv = p.f_now[p.ent_src[e]];
       const T v = fv.re * am.re - fv.im * am.im;  // real(f(t) · amplitude)
       if (c == 0) { S0 += v; h0 = true; }
@@ -92,7 +109,7 @@ __device__ __forceinline__ void general_cell(const HalfStepParams<T>& p, long lo
   // Total polarisation Σ_p P_p (accumulate_polarization_kernel!, Dispersive.jl:95-104).
   T Ptot[3] = {T(0), T(0), T(0)};
   if constexpr (!H) {
-    if (cls & kHasPole) {
+    if ((cls & kHasPole) && KH_IN(q, p.total, 1004)) {
       for (int pp = 0; pp < p.npoles; ++pp) {
         Ptot[0] += p.poles[pp].P[0][q];
         Ptot[1] += p.poles[pp].P[1][q];
@@ -129,7 +146,7 @@ __device__ __forceinline__ void general_cell(const HalfStepParams<T>& p, long lo
       }
       tc = (f[pv] && ap.s != T(0)) ? (ap.om * tc + in_t) * ap.ir : tc + in_t;
     } else {
-      if (hasC && hasU) {
+      if (hasC && hasU && KH_IN(q, p.total, 1005)) {
         const T sD = hasSD ? T(0.5) * (p.dt * p.msig[c][q]) : T(0);
         const T uo = u[c];
         if (hasSD && sD != T(0)) {  // three-stage cascade (Helpers.jl:60-67)
@@ -149,7 +166,7 @@ __device__ __forceinline__ void general_cell(const HalfStepParams<T>& p, long lo
           u[c] = (an.om * uo + K[c]) * an.ir;
           tc = ((ap.om * tc + u[c]) - uo) * ap.ir;
         }
-      } else if (hasSD) {  // C and U absent, conductivity present (Helpers.jl:225-240)
+      } else if (hasSD && KH_IN(q, p.total, 1006)) {  // C and U absent, conductivity present (Helpers.jl:225-240)
         const T sD = T(0.5) * (p.dt * p.msig[c][q]);
         tc = ((T(1) - sD) * tc + K[c]) / (T(1) + sD);
       } else {  // C and U absent: σ_prev dropped (Helpers.jl:208-223)
@@ -182,7 +199,7 @@ __device__ __forceinline__ void general_cell(const HalfStepParams<T>& p, long lo
       O[2] = O[2] * corr;
     }
     // ADE poles with E^{n+1} (Dispersive.jl:25-88)
-    if (cls & kHasPole) {
+    if ((cls & kHasPole) && KH_IN(q, p.total, 1007)) {
       for (int pp = 0; pp < p.npoles; ++pp) {
         const PoleParams<T>& P = p.poles[pp];
         const T s = P.sigma[q];

@@ -30,6 +30,10 @@
 
 namespace kh {
 
+#ifdef KH_DEBUG_BOUNDS
+KH_DBG_READER(dbg_read_kernels)
+#endif
+
 template <typename T, int VN>
 struct PlaneLoads {
   T l0[VN], l1[VN], a2[VN], y0[VN], y2[VN];  // A0/A1 fresh plane, A2, y neighbours
@@ -55,42 +59,44 @@ __device__ __forceinline__ void load_plane(const HalfStepParams<T>& p, PlaneLoad
   const bool axis_any[3] = {anyfx, fy, fz};
   if (lane_ok) {
     if constexpr (H) {  // l = A(k+1)
-      vld(p.A[0] + q + p.plane, L.l0);
-      vld(p.A[1] + q + p.plane, L.l1);
+      vld_at(p.A[0], q + p.plane, p.total, 3001, L.l0);
+      vld_at(p.A[1], q + p.plane, p.total, 3001, L.l1);
     } else {  // l = A(k)
-      vld(p.A[0] + q, L.l0);
-      vld(p.A[1] + q, L.l1);
+      vld_at(p.A[0], q, p.total, 3001, L.l0);
+      vld_at(p.A[1], q, p.total, 3001, L.l1);
     }
-    vld(p.A[2] + q, L.a2);
-    vld(p.A[0] + q + s * p.pitch, L.y0);
-    vld(p.A[2] + q + s * p.pitch, L.y2);
+    vld_at(p.A[2], q, p.total, 3002, L.a2);
+    vld_at(p.A[0], q + s * p.pitch, p.total, 3003, L.y0);
+    vld_at(p.A[2], q + s * p.pitch, p.total, 3003, L.y2);
     if constexpr (H) {
-      if (lane == 31) {
+      if (lane == 31 && KH_IN(q + VN, p.total, 3004)) {
         L.xn1 = p.A[1][q + VN];
         L.xn2 = p.A[2][q + VN];
       }
     } else {
-      if (lane == 0) {
+      if (lane == 0 && KH_IN(q - 1, p.total, 3004)) {
         L.xn1 = p.A[1][q - 1];
         L.xn2 = p.A[2][q - 1];
       }
     }
 #pragma unroll
-    for (int c = 0; c < 3; ++c) vld(p.O[c] + q, L.O[c]);
+    for (int c = 0; c < 3; ++c) vld_at(p.O[c], q, p.total, 3005, L.O[c]);
     if (pervox) {
 #pragma unroll
-      for (int c = 0; c < 3; ++c) vld(p.m_inv[c] + q, L.m[c]);
+      for (int c = 0; c < 3; ++c) vld_at(p.m_inv[c], q, p.total, 3006, L.m[c]);
     }
 #pragma unroll
-    for (int v = 0; v < VN; ++v) L.cls[v] = (L.tf && lane_ok) ? p.cell_class[q + v] : 0u;
+    for (int v = 0; v < VN; ++v)
+      L.cls[v] = (L.tf && lane_ok && KH_IN(q + v, p.total, 3007)) ? p.cell_class[q + v] : 0u;
     const bool aux = anyRegion || L.tf;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      if (aux && p.Ts[c]) vld(p.Ts[c] + q, L.t[c]); else vzero(L.t[c]);
-      if (anyRegion && p.U[c] && axis_any[(c + 1) % 3]) vld(p.U[c] + q, L.u[c]); else vzero(L.u[c]);
-      if (anyRegion && p.W[c] && axis_any[c]) vld(p.W[c] + q, L.w[c]); else vzero(L.w[c]);
+      if (aux && p.Ts[c]) vld_at(p.Ts[c], q, p.total, 3008, L.t[c]); else vzero(L.t[c]);
+      if (anyRegion && p.U[c] && axis_any[(c + 1) % 3]) vld_at(p.U[c], q, p.total, 3009, L.u[c]);
+      else vzero(L.u[c]);
+      if (anyRegion && p.W[c] && axis_any[c]) vld_at(p.W[c], q, p.total, 3010, L.w[c]); else vzero(L.w[c]);
     }
-    if (FULL && !H && L.tf && p.chi3) vld(p.chi3 + q, L.c3); else vzero(L.c3);
+    if (FULL && !H && L.tf && p.chi3) vld_at(p.chi3, q, p.total, 3011, L.c3); else vzero(L.c3);
   } else {
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
@@ -168,7 +174,7 @@ __device__ __forceinline__ void compute_plane(const HalfStepParams<T>& p, PlaneL
 #pragma unroll
         for (int v = 0; v < VN; ++v) L.O[c][v] = L.O[c][v] + L.m[c][v] * K[c][v];
     } else {
-      const AxisCoef<T> az = p.ax[2][k];
+      const AxisCoef<T> az = KH_IN(k, p.nz, 3012) ? p.ax[2][k] : AxisCoef<T>{T(0), T(1), T(1), T(1)};
 #pragma unroll
       for (int v = 0; v < VN; ++v) {
         const int i = x0 + v;
@@ -211,18 +217,18 @@ __device__ __forceinline__ void compute_plane(const HalfStepParams<T>& p, PlaneL
       const bool axis_any[3] = {anyfx, fy, fz};
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        if (p.Ts[c]) vst(p.Ts[c] + q, L.t[c]);
-        if (p.U[c] && axis_any[(c + 1) % 3]) vst(p.U[c] + q, L.u[c]);
-        if (p.W[c] && axis_any[c]) vst(p.W[c] + q, L.w[c]);
+        if (p.Ts[c]) vst_at(p.Ts[c], q, p.total, 3013, L.t[c]);
+        if (p.U[c] && axis_any[(c + 1) % 3]) vst_at(p.U[c], q, p.total, 3014, L.u[c]);
+        if (p.W[c] && axis_any[c]) vst_at(p.W[c], q, p.total, 3015, L.w[c]);
       }
     }
     if (x0 + VN <= p.nx) {
 #pragma unroll
-      for (int c = 0; c < 3; ++c) vst(p.O[c] + q, L.O[c]);
+      for (int c = 0; c < 3; ++c) vst_at(p.O[c], q, p.total, 3016, L.O[c]);
     } else {
 #pragma unroll
       for (int v = 0; v < VN; ++v) {
-        if (x0 + v < p.nx) {
+        if (x0 + v < p.nx && KH_IN(q + v, p.total, 3017)) {
 #pragma unroll
           for (int c = 0; c < 3; ++c) p.O[c][q + v] = L.O[c][v];
         }
@@ -258,7 +264,8 @@ __global__ void __launch_bounds__(32 * kBlockY, sizeof(T) == 4 ? kMinBlocks : 2)
   const bool fy = j < p.pml_lo[1] || j >= p.ny - p.pml_hi[1];
   const bool pervox = p.m_inv[0] != nullptr;
   // special-tile bits of planes [64·(k0/64), +64) of this warp's row segment
-  const uint64_t tbits = p.tile_bits ? p.tile_bits[((long long)(k0 >> 6) * p.ny + j) * p.nxb + xb] : 0ull;
+  const long long tbi = ((long long)(k0 >> 6) * p.ny + j) * p.nxb + xb;
+  const uint64_t tbits = (p.tile_bits && KH_IN(tbi, p.n_tile_words, 3018)) ? p.tile_bits[tbi] : 0ull;
 
   // per-cell x flags and CPML coefficients of this thread's vector and the
   // row's y coefficients: static along the z march
@@ -270,9 +277,9 @@ __global__ void __launch_bounds__(32 * kBlockY, sizeof(T) == 4 ? kMinBlocks : 2)
     const int i = x0 + v;
     fxv[v] = i < p.nx && (i < p.pml_lo[0] || i >= p.nx - p.pml_hi[0]);
     anyfx |= fxv[v];
-    axv[v] = i < p.nx ? p.ax[0][i] : AxisCoef<T>{T(0), T(1), T(1), T(1)};
+    axv[v] = (i < p.nx && KH_IN(i, p.nx, 3019)) ? p.ax[0][i] : AxisCoef<T>{T(0), T(1), T(1), T(1)};
   }
-  const AxisCoef<T> ay = p.ax[1][j];
+  const AxisCoef<T> ay = KH_IN(j, p.ny, 3020) ? p.ax[1][j] : AxisCoef<T>{T(0), T(1), T(1), T(1)};
 
   // rotated z-neighbour plane of A0, A1: A(k0) for the H half, A(k0-1) for E
   T r0[VN], r1[VN];
@@ -280,8 +287,8 @@ __global__ void __launch_bounds__(32 * kBlockY, sizeof(T) == 4 ? kMinBlocks : 2)
   vzero(r1);
   if (lane_ok) {
     const long long q0 = row + (long long)k0 * p.plane + (H ? 0 : -p.plane);
-    vld(p.A[0] + q0, r0);
-    vld(p.A[1] + q0, r1);
+    vld_at(p.A[0], q0, p.total, 3021, r0);
+    vld_at(p.A[1], q0, p.total, 3021, r1);
   }
   PlaneLoads<T, VN> A, B;
   load_plane<T, VN, H, FULL>(p, A, k0, row, lane, lane_ok, pervox, fy, anyfx, tbits);
@@ -324,13 +331,16 @@ __global__ void source_fix_kernel(const SourceFixParams<T> p) {
   const int slot = blockIdx.x * blockDim.x + threadIdx.x;
   if (slot >= p.nslots) return;
   const long long q = p.slot_cell[slot];
+  if (!KH_IN(q, p.total, 3022)) return;
   const int base = p.h_half ? 3 : 0;
   T S[3] = {T(0), T(0), T(0)};
   bool has[3] = {false, false, false};
   for (int e = p.slot_off[slot]; e < p.slot_off[slot + 1]; ++e) {
+    if (!KH_IN(e, p.n_ent, 3023)) break;
     const int c = p.ent_comp[e] - base;
     if (c < 0 || c > 2) continue;
     const Cplx<T> a = p.ent_amp[e];
+    if (!KH_IN(p.ent_src[e], p.n_src, 3024)) continue;
     const Cplx<T> f = p.f_now[p.ent_src[e]];
     const T v = f.re * a.re - f.im * a.im;
     if (c == 0) { S[0] += v; has[0] = true; }
@@ -372,6 +382,7 @@ __global__ void dft_kernel(const DftParams<T> p) {
     const int kk = int(r / p.dims[1]);
     const long long q = p.origin + (long long)(p.start[2] + kk) * p.plane +
                         (long long)(p.start[1] + jj) * p.pitch + (p.start[0] + i);
+    if (!KH_IN(q, p.total, 3025)) continue;
     const T v = p.field[q];
     const Cplx<T> ph = p.phase[f];
     Cplx<T> acc = p.F[t];
@@ -414,8 +425,10 @@ __global__ void record_kernel(const RecordParams<T> p) {
     const T* src = p.field + p.origin + (long long)(p.start[2] + kk) * p.plane +
                    (long long)(p.start[1] + jj) * p.pitch + p.start[0];
     T* dst = p.dst + (long long)r * p.dims[0];
+    const long long s0 = src - p.field;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.dims[0]; i += gridDim.x * blockDim.x)
-      dst[i] = src[i];
+      if (KH_IN(s0 + i, p.total, 3026) && KH_IN((long long)r * p.dims[0] + i, (long long)rows * p.dims[0], 3027))
+        dst[i] = src[i];
   }
 }
 

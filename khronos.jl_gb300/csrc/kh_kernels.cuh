@@ -38,6 +38,46 @@ constexpr uint32_t kHasSrcE = 1u << 4;
 constexpr uint32_t kHasSrcH = 1u << 5;
 constexpr int kSlotShift = 8;            // source slot index in the upper 24 bits
 
+// Bounds-checked builds (-DKH_DEBUG_BOUNDS, a stand-in for a memory
+// sanitizer): every global and shared-memory index of the step kernels is
+// tested against its array's extent before the access; a violation is
+// counted, the first one's site and index recorded, and the access skipped
+// (loads read 0).  No trap and no wait.  Each translation unit has its own
+// record word, read back by kh_debug_bounds.  In other builds KH_IN is the
+// constant true and the kernels are unchanged.
+#ifdef KH_DEBUG_BOUNDS
+struct DbgWord {
+  unsigned long long count;
+  long long index;
+  int site;
+};
+static __device__ DbgWord kh_dbg;
+__device__ __forceinline__ bool dbg_in(long long idx, long long n, int site) {
+  if (idx >= 0 && idx < n) return true;
+  if (atomicAdd(&kh_dbg.count, 1ull) == 0ull) {
+    kh_dbg.index = idx;
+    kh_dbg.site = site;
+  }
+  return false;
+}
+#define KH_IN(idx, n, site) ::kh::dbg_in((long long)(idx), (long long)(n), (site))
+// Host side: read (and clear) this translation unit's record word.
+#define KH_DBG_READER(name)                                                              \
+  void name(unsigned long long* count, long long* index, int* site) {                   \
+    DbgWord w{};                                                                         \
+    cudaMemcpyFromSymbol(&w, kh_dbg, sizeof(w));                                         \
+    *count = w.count;                                                                    \
+    *index = w.index;                                                                    \
+    *site = w.site;                                                                      \
+    const DbgWord z{};                                                                   \
+    cudaMemcpyToSymbol(kh_dbg, &z, sizeof(z));                                           \
+  }
+void dbg_read_tma(unsigned long long* count, long long* index, int* site);
+void dbg_read_kernels(unsigned long long* count, long long* index, int* site);
+#else
+#define KH_IN(idx, n, site) true
+#endif
+
 // Row alignment unit of the layout: 16 bytes of the run's type.
 template <typename T>
 struct Vec;
@@ -80,6 +120,7 @@ template <typename T>
 struct HalfStepParams {
   int nx, ny, nz;
   long long pitch, plane, origin;
+  long long total;  // elements of every padded full-domain array
   int nxb;  // x tiles of 32*VN cells
   int full; // 1: cells with sources/χ3/poles/conductivity handled in-kernel (FULL variant)
   int zplanes;  // z planes marched by one CTA of the TMA-staged kernel
@@ -103,6 +144,7 @@ struct HalfStepParams {
   // per (k/64, j, xb): bit k%64 set when that plane's row segment of 32·VN
   // cells holds special cells of this half
   const uint64_t* tile_bits;
+  long long n_tile_words;     // entries of tile_bits
   const uint32_t* cell_class; // per cell
 
   // sources (folded into the half-step)
@@ -112,6 +154,7 @@ struct HalfStepParams {
   const int* ent_comp;        // component 0..2 within this half
   const Cplx<T>* ent_amp;     // complex amplitude of entry
   const Cplx<T>* f_now;       // per source: time factor f(t) of this half-step
+  int n_slots, n_ent, n_src;  // extents of slot_off (n_slots + 1), ent_*, f_now
 
   // E half only
   const T* chi3;
@@ -190,7 +233,7 @@ int tma_resident_ctas();
 template <typename T>
 struct RecordParams {
   const T* field;
-  long long pitch, plane, origin;
+  long long pitch, plane, origin, total;
   int start[3], dims[3];
   T* dst;
 };
@@ -201,7 +244,7 @@ void launch_record(const RecordParams<T>& p, void* stream);
 template <typename T>
 struct DftParams {
   const T* field;
-  long long pitch, plane, origin;
+  long long pitch, plane, origin, total;
   int start[3], dims[3];
   int nf;
   const Cplx<T>* phase;  // nf entries: Δt·exp(i 2π f t)
@@ -219,7 +262,8 @@ constexpr int kVN = 2;
 // and no χ3/pole, which the host checks before choosing this path.
 template <typename T>
 struct SourceFixParams {
-  int nslots;
+  int nslots, n_ent, n_src;
+  long long total;
   const long long* slot_cell;  // cell offset of each slot
   const int* slot_off;
   const int* ent_src;

@@ -1460,6 +1460,7 @@ class Sim : public SimBase {
       p.pitch = pitch_;
       p.plane = plane_;
       p.origin = origin_;
+      p.total = total_;
       for (int a = 0; a < 3; ++a) {
         p.start[a] = h.start[a];
         p.dims[a] = h.dims[a];
@@ -1516,6 +1517,7 @@ class Sim : public SimBase {
     p.pitch = pitch_;
     p.plane = plane_;
     p.origin = origin_;
+    p.total = total_;
     for (int a = 0; a < 3; ++a) {
       p.start[a] = m.start[a];
       p.dims[a] = m.dims[a];
@@ -1610,6 +1612,9 @@ class Sim : public SimBase {
     kh::SourceFixParams<T> f;
     std::memset(&f, 0, sizeof(f));
     f.nslots = nslots_;
+    f.n_ent = int(ent_amp_h_.size());
+    f.n_src = nsrc_;
+    f.total = total_;
     f.slot_cell = slot_cell_;
     f.slot_off = slot_off_;
     f.ent_src = ent_src_;
@@ -1634,6 +1639,7 @@ class Sim : public SimBase {
     p.pitch = pitch_;
     p.plane = plane_;
     p.origin = origin_;
+    p.total = total_;
     p.nxb = nxb_;
     p.zplanes = zplanes_;
     p.dt = dt_;
@@ -1658,6 +1664,10 @@ class Sim : public SimBase {
     p.m_scalar = h ? T(d_.mu_inv) : T(d_.eps_inv);
     p.sigma_region_mask = h ? sigmask_b_ : sigmask_d_;
     p.tile_bits = h ? tbits_h_ : tbits_e_;
+    p.n_tile_words = p.tile_bits ? (long long)((n_[2] + 63) / 64) * n_[1] * nxb_ : 0;
+    p.n_slots = nslots_;
+    p.n_ent = int(ent_amp_h_.size());
+    p.n_src = nsrc_;
     p.cell_class = cls_;
     p.err = err_dev_;
     p.slot_off = slot_off_;
@@ -1848,6 +1858,31 @@ kh_status kh_sim_launch_count(const kh_sim* sim, int64_t* out) {
   if (!sim || !out) return KH_ERR_INVALID;
   *out = sim->impl->launches;
   return KH_OK;
+}
+
+kh_status kh_debug_bounds(int64_t* count, int64_t* index, int32_t* site) {
+  if (!count || !index || !site) return KH_ERR_INVALID;
+  *count = 0;
+  *index = 0;
+  *site = 0;
+#ifdef KH_DEBUG_BOUNDS
+  if (cudaDeviceSynchronize() != cudaSuccess) return KH_ERR_CUDA;
+  void (*readers[])(unsigned long long*, long long*, int*) = {kh::dbg_read_tma, kh::dbg_read_kernels};
+  for (auto rd : readers) {
+    unsigned long long c = 0;
+    long long ix = 0;
+    int st = 0;
+    rd(&c, &ix, &st);
+    if (c && !*count) {
+      *index = ix;
+      *site = st;
+    }
+    *count += int64_t(c);
+  }
+  return KH_OK;
+#else
+  return KH_ERR_UNSUPPORTED;
+#endif
 }
 
 kh_status kh_sim_get_field(kh_sim* sim, int32_t component, double* out) {

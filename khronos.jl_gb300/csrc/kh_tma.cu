@@ -25,6 +25,10 @@
 
 namespace kh {
 
+#ifdef KH_DEBUG_BOUNDS
+KH_DBG_READER(dbg_read_tma)
+#endif
+
 namespace {
 
 constexpr long long kWaitLimit = 1ll << 22;
@@ -107,14 +111,15 @@ __device__ __forceinline__ void load_aux(const HalfStepParams<T>& p, AuxLoads<T>
   const bool axis_any[3] = {anyfx, fy, fz};
   const bool aux = lane_ok && (anyRegion || L.tf);
 #pragma unroll
-  for (int v = 0; v < 2; ++v) L.cls[v] = (L.tf && lane_ok) ? p.cell_class[q + v] : 0u;
+  for (int v = 0; v < 2; ++v) L.cls[v] = (L.tf && lane_ok && KH_IN(q + v, p.total, 2001)) ? p.cell_class[q + v] : 0u;
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    if (aux && p.Ts[c]) vld(p.Ts[c] + q, L.t[c]); else vzero(L.t[c]);
-    if (aux && anyRegion && p.U[c] && axis_any[(c + 1) % 3]) vld(p.U[c] + q, L.u[c]); else vzero(L.u[c]);
-    if (aux && anyRegion && p.W[c] && axis_any[c]) vld(p.W[c] + q, L.w[c]); else vzero(L.w[c]);
+    if (aux && p.Ts[c]) vld_at(p.Ts[c], q, p.total, 2002, L.t[c]); else vzero(L.t[c]);
+    if (aux && anyRegion && p.U[c] && axis_any[(c + 1) % 3]) vld_at(p.U[c], q, p.total, 2003, L.u[c]);
+    else vzero(L.u[c]);
+    if (aux && anyRegion && p.W[c] && axis_any[c]) vld_at(p.W[c], q, p.total, 2004, L.w[c]); else vzero(L.w[c]);
   }
-  if (FULL && !H && lane_ok && L.tf && p.chi3) vld(p.chi3 + q, L.c3); else vzero(L.c3);
+  if (FULL && !H && lane_ok && L.tf && p.chi3) vld_at(p.chi3, q, p.total, 2005, L.c3); else vzero(L.c3);
 }
 
 }  // namespace
@@ -195,9 +200,11 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
   const bool fy = row_ok && (j < p.pml_lo[1] || j >= p.ny - p.pml_hi[1]);
   // special-cell plane bits of this row segment for planes 64·g .. 64·g+63,
   // re-read when the march enters the next group of 64 planes
-  const uint64_t* tb_row = (p.tile_bits && row_ok) ? p.tile_bits + (long long)j * p.nxb + blockIdx.x : nullptr;
+  const long long tb_base = (long long)j * p.nxb + blockIdx.x;
+  const uint64_t* tb_row = (p.tile_bits && row_ok) ? p.tile_bits + tb_base : nullptr;
   const long long tb_group = (long long)p.ny * p.nxb;
-  uint64_t tbits = tb_row ? tb_row[(long long)(k0 >> 6) * tb_group] : 0ull;
+  uint64_t tbits = (tb_row && KH_IN(tb_base + (long long)(k0 >> 6) * tb_group, p.n_tile_words, 2006))
+                       ? tb_row[(long long)(k0 >> 6) * tb_group] : 0ull;
   bool fxv[VN];
   AxisCoef<T> axv[VN];
   bool anyfx = false;
@@ -206,9 +213,9 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
     const int i = x0 + v;
     fxv[v] = lane_ok && i < p.nx && (i < p.pml_lo[0] || i >= p.nx - p.pml_hi[0]);
     anyfx |= fxv[v];
-    axv[v] = (lane_ok && i < p.nx) ? p.ax[0][i] : AxisCoef<T>{T(0), T(1), T(1), T(1)};
+    axv[v] = (lane_ok && i < p.nx && KH_IN(i, p.nx, 2007)) ? p.ax[0][i] : AxisCoef<T>{T(0), T(1), T(1), T(1)};
   }
-  const AxisCoef<T> ay = row_ok ? p.ax[1][j] : AxisCoef<T>{T(0), T(1), T(1), T(1)};
+  const AxisCoef<T> ay = (row_ok && KH_IN(j, p.ny, 2008)) ? p.ax[1][j] : AxisCoef<T>{T(0), T(1), T(1), T(1)};
   // box coordinates of this thread's first cell in the A and O tiles
   const int bx = (H ? 0 : G::HX) + lane * VN;
   const int by = H ? wy : wy + 1;
@@ -222,7 +229,9 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
   for (int c = 0; c < N; ++c) {
     const int k = k0 + c;
     if (c + 1 < N) {
-      if (tb_row && ((k + 1) & 63) == 0) tbits = tb_row[(long long)((k + 1) >> 6) * tb_group];
+      if (tb_row && ((k + 1) & 63) == 0 &&
+          KH_IN(tb_base + (long long)((k + 1) >> 6) * tb_group, p.n_tile_words, 2009))
+        tbits = tb_row[(long long)((k + 1) >> 6) * tb_group];
       load_aux<T, H, FULL>(p, nxt, k + 1, row, lane_ok, fy, anyfx, tbits);
     }
     const int ncur = H ? c : c + 1;
@@ -233,7 +242,12 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
       bad = true;
       if (p.err) atomicExch(p.err, KH_ERR_TIMEOUT);
     }
-    if (!bad && lane_ok) {
+    // shared-memory reach of this thread's cells (checked in KH_DEBUG_BOUNDS builds)
+    const int a_chk = by * G::AX + bx;
+    const bool smem_ok = KH_IN(a_chk + (H ? 0 : -1), G::A_ELEMS, 2010) && KH_IN(a_chk + (H ? 2 : 1), G::A_ELEMS, 2011) &&
+                         KH_IN(a_chk + s * G::AX, G::A_ELEMS, 2012) &&
+                         KH_IN(a_chk + s * G::AX + 1, G::A_ELEMS, 2013) && KH_IN(ob + 1, G::O_ELEMS, 2014);
+    if (!bad && lane_ok && smem_ok) {
       using V2 = typename VT<T, 2>::V;
       const T* Sc = stages + (ncur % kTmaStages) * G::STAGE;
       const T* Sn = stages + (nnb % kTmaStages) * G::STAGE;
@@ -299,7 +313,7 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
 #pragma unroll
           for (int v = 0; v < VN; ++v) O[cc][v] = O[cc][v] + m[cc][v] * K[cc][v];
       } else {
-        const AxisCoef<T> az = p.ax[2][k];
+        const AxisCoef<T> az = KH_IN(k, p.nz, 2020) ? p.ax[2][k] : AxisCoef<T>{T(0), T(1), T(1), T(1)};
 #pragma unroll
         for (int v = 0; v < VN; ++v) {
           const int i = x0 + v;
@@ -364,19 +378,19 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
           const bool axis_any[3] = {anyfx, fy, fz};
 #pragma unroll
           for (int cc = 0; cc < 3; ++cc) {
-            if (p.Ts[cc]) vst(p.Ts[cc] + q, cur.t[cc]);
-            if (p.U[cc] && axis_any[(cc + 1) % 3]) vst(p.U[cc] + q, cur.u[cc]);
-            if (p.W[cc] && axis_any[cc]) vst(p.W[cc] + q, cur.w[cc]);
+            if (p.Ts[cc]) vst_at(p.Ts[cc], q, p.total, 2015, cur.t[cc]);
+            if (p.U[cc] && axis_any[(cc + 1) % 3]) vst_at(p.U[cc], q, p.total, 2016, cur.u[cc]);
+            if (p.W[cc] && axis_any[cc]) vst_at(p.W[cc], q, p.total, 2017, cur.w[cc]);
           }
         }
       }
       if (x0 + VN <= p.nx) {
 #pragma unroll
-        for (int cc = 0; cc < 3; ++cc) vst(p.O[cc] + q, O[cc]);
+        for (int cc = 0; cc < 3; ++cc) vst_at(p.O[cc], q, p.total, 2018, O[cc]);
       } else {
 #pragma unroll
         for (int v = 0; v < VN; ++v)
-          if (x0 + v < p.nx) {
+          if (x0 + v < p.nx && KH_IN(q + v, p.total, 2019)) {
 #pragma unroll
             for (int cc = 0; cc < 3; ++cc) p.O[cc][q + v] = O[cc][v];
           }

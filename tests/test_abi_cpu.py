@@ -69,3 +69,15 @@ def test_missing_library_fails_loudly(tmp_path):
 
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         _abi.load(tmp_path / "libkhronos_gb300.so")
+
+
+def test_regular_build_has_no_bounds_record(gpu_lib):
+    """kh_debug_bounds answers KH_ERR_UNSUPPORTED outside the bounds-checked
+    build (no device work)."""
+    import ctypes as C
+
+    from khronos_gb300 import _abi
+
+    c, i, s = C.c_int64(7), C.c_int64(7), C.c_int32(7)
+    assert gpu_lib.kh_debug_bounds(C.byref(c), C.byref(i), C.byref(s)) == _abi.KH_ERR_UNSUPPORTED
+    assert (c.value, i.value, s.value) == (0, 0, 0)
