@@ -6,6 +6,7 @@ DFT monitors, FP64 flux) runs as hand-written sm_103a CUDA kernels in
 This package is the host side: the set-up arithmetic of the reference's
 ``prepare_simulation!`` and a ctypes binding of the ABI.
 """
+from .boundaries import Bloch, PECBoundary, PMCBoundary, Periodic
 from .grid import CENTER, EX, EY, EZ, HX, HY, HZ, Grid, GridVolume, interpolation_weight
 from .monitors import DFTMonitor, FluxMonitor, flux_from_dft
 from .simulation import Simulation, apply_chi1_correction, stop_when_dft_decayed
@@ -15,6 +16,7 @@ from .spec import (DrudeSusceptibility, LorentzianSusceptibility, SimSpec, ade_c
                    eval_susceptibility)
 
 __all__ = [
+    "Bloch", "PECBoundary", "PMCBoundary", "Periodic",
     "CENTER", "EX", "EY", "EZ", "HX", "HY", "HZ", "Grid", "GridVolume", "interpolation_weight",
     "DFTMonitor", "FluxMonitor", "flux_from_dft", "Simulation", "apply_chi1_correction",
     "stop_when_dft_decayed",

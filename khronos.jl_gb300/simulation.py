@@ -32,6 +32,11 @@ class Simulation:
     reference's CPU-backend dispatch exactly, including the dropped σ_prev
     stage that makes that path grow without bound once PML is present.
 
+    ``boundary_conditions`` ([[lo, hi]] per axis of ``boundaries.PECBoundary``,
+    ``PMCBoundary``, ...) zeroes the PML conductivity on those sides while the
+    PML regions keep following ``boundaries``, as the reference's prepare
+    does; periodic and Bloch sides are refused.
+
     Materials (all optional; arrays are (Nx, Ny, Nz), cell-indexed):
       geometry: list of geometry.Object (Ball / Cuboid / Cylinder with an
       isotropic ε) rasterised on the device at each component's Yee position,
@@ -46,11 +51,15 @@ class Simulation:
     def __init__(self, *, cell_size, resolution, sources=(), cell_center=(0.0, 0.0, 0.0),
                  boundaries=None, monitors=(), dtype="f32", courant=0.5, eps_inv=1.0, mu_inv=1.0,
                  sigma_d=None, sigma_b=None, chi3=None, poles=(), semantics="cpml", geometry=None,
-                 background_eps=1.0, subpixel_smoothing="none"):
+                 background_eps=1.0, subpixel_smoothing="none", boundary_conditions=None):
         self.grid = G.Grid.build(cell_size, cell_center, resolution, dtype, courant)
         self.dtype = dtype
         self.sources = list(sources)
         self.boundaries = boundaries
+        from .boundaries import effective_pml
+
+        self.boundary_conditions = boundary_conditions
+        self._sigma_boundaries = effective_pml(boundaries, boundary_conditions)
         self.monitors = list(monitors)
         self.eps_inv = eps_inv
         self.mu_inv = mu_inv
@@ -104,7 +113,7 @@ class Simulation:
             lo, hi = G.pml_widths(g, self.boundaries)
             sp.pml_lo, sp.pml_hi = lo, hi
             for a in range(3):
-                L, R = self.boundaries[a]
+                L, R = self._sigma_boundaries[a]
                 s = G.cell_sigma(g, a, L, R).astype(np.float64)
                 sp.sigma_b[a] = s
                 sp.sigma_d[a] = s.copy()
