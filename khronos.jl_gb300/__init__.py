@@ -10,8 +10,8 @@ from .boundaries import Bloch, PECBoundary, PMCBoundary, Periodic
 from .grid import CENTER, EX, EY, EZ, HX, HY, HZ, Grid, GridVolume, interpolation_weight
 from .monitors import DFTMonitor, FluxMonitor, flux_from_dft
 from .simulation import Simulation, apply_chi1_correction, stop_when_dft_decayed
-from .sources import (ContinuousWaveSource, CustomSource, GaussianPulseSource, PlaneWaveSource,
-                      ProfileSource, UniformSource)
+from .sources import (ContinuousWaveSource, CustomSource, EquivalentSource, GaussianBeamSource,
+                      GaussianPulseSource, PlaneWaveSource, ProfileSource, TFSFSource, UniformSource)
 from .spec import (DrudeSusceptibility, LorentzianSusceptibility, SimSpec, ade_coefficients,
                    eval_susceptibility)
 
@@ -20,7 +20,8 @@ __all__ = [
     "CENTER", "EX", "EY", "EZ", "HX", "HY", "HZ", "Grid", "GridVolume", "interpolation_weight",
     "DFTMonitor", "FluxMonitor", "flux_from_dft", "Simulation", "apply_chi1_correction",
     "stop_when_dft_decayed",
-    "ContinuousWaveSource", "CustomSource", "GaussianPulseSource", "PlaneWaveSource", "ProfileSource",
+    "ContinuousWaveSource", "CustomSource", "GaussianPulseSource", "PlaneWaveSource", "ProfileSource", "EquivalentSource", "TFSFSource",
+    "GaussianBeamSource",
     "UniformSource",
     "DrudeSusceptibility", "LorentzianSusceptibility", "SimSpec", "ade_coefficients",
     "eval_susceptibility",
