@@ -188,6 +188,11 @@ struct alignas(128) TmaMaps {
   CUtensorMap a[3];
   CUtensorMap o[3];
   CUtensorMap m[3];
+  // B|D state and CPML U, W (maps of the arrays that exist; box kTmaX × kTmaY),
+  // used for L2 prefetch only
+  CUtensorMap t[3];
+  CUtensorMap u[3];
+  CUtensorMap w[3];
 };
 
 template <typename T>

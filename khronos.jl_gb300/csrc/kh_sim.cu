@@ -1575,6 +1575,12 @@ class Sim : public SimBase {
       if ((st = mk(&maps_e_.a[c], H_[c], box_a)) != KH_OK) return st;
       if ((st = mk(&maps_e_.o[c], E_[c], box_o)) != KH_OK) return st;
       if (eps_[c] && (st = mk(&maps_e_.m[c], eps_[c], box_o)) != KH_OK) return st;
+      if (B_[c] && (st = mk(&maps_h_.t[c], B_[c], box_o)) != KH_OK) return st;
+      if (UB_[c] && (st = mk(&maps_h_.u[c], UB_[c], box_o)) != KH_OK) return st;
+      if (WB_[c] && (st = mk(&maps_h_.w[c], WB_[c], box_o)) != KH_OK) return st;
+      if (D_[c] && (st = mk(&maps_e_.t[c], D_[c], box_o)) != KH_OK) return st;
+      if (UD_[c] && (st = mk(&maps_e_.u[c], UD_[c], box_o)) != KH_OK) return st;
+      if (WD_[c] && (st = mk(&maps_e_.w[c], WD_[c], box_o)) != KH_OK) return st;
     }
     return KH_OK;
   }

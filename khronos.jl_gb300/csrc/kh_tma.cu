@@ -82,6 +82,14 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
+// L2 prefetch of one tensor-map tile (no shared memory, no completion).
+__device__ __forceinline__ void tma_prefetch_3d(const CUtensorMap* map, int x, int y, int z) {
+  asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(x), "r"(y), "r"(z)
+               : "memory");
+}
+
 template <typename T>
 struct TmaGeom {
   static constexpr int HX = 16 / int(sizeof(T));  // x halo = XOFF of the layout
@@ -161,6 +169,9 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
     mbar_fence_init();
   }
   __syncthreads();
+  // tile-wide CPML flags along x and y: which CPML state tiles a plane needs
+  const bool tfx = x_tile < p.pml_lo[0] || x_tile + kTmaX > p.nx - p.pml_hi[0];
+  const bool tfy = y_tile < p.pml_lo[1] || y_tile + kTmaY > p.ny - p.pml_hi[1];
 
   // Load n brings the A arrays of plane (H: k0+n, E: k0-1+n) and, when that
   // plane is computed, its O and m⁻¹ tiles.
@@ -187,6 +198,22 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
         for (int c = 0; c < 3; ++c)
           tma_load_3d(dst + 3 * G::A_ELEMS + (3 + c) * G::O_ELEMS, &maps.m[c], G::HX + x_tile, 1 + y_tile,
                       zc, &bars[st]);
+      }
+      // LEAN variants: the CPML state of the plane (B|D, U, W where the tile
+      // touches the CPML of their axis) into L2, so that the per-thread
+      // register loads a plane ahead of its update find it there.  Tiles that
+      // keep state only for special cells are left to those loads (the
+      // tile-bit lookup on the issuing thread would delay the ring); the FULL
+      // variants, at their register limit, do without.
+      const bool tfz = plane < p.pml_lo[2] || plane >= p.nz - p.pml_hi[2];
+      if (!FULL && (tfx || tfy || tfz)) {
+        const bool af[3] = {tfx, tfy, tfz};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          if (p.Ts[c]) tma_prefetch_3d(&maps.t[c], G::HX + x_tile, 1 + y_tile, zc);
+          if (p.U[c] && af[(c + 1) % 3]) tma_prefetch_3d(&maps.u[c], G::HX + x_tile, 1 + y_tile, zc);
+          if (p.W[c] && af[c]) tma_prefetch_3d(&maps.w[c], G::HX + x_tile, 1 + y_tile, zc);
+        }
       }
     }
   };
