@@ -9,13 +9,17 @@ step loop); everything else follows the reference's arithmetic.
 """
 from __future__ import annotations
 
+import logging
 import math
+import time
 import warnings
 from typing import Callable, List, Optional, Sequence, Union
 
 import numpy as np
 
 from . import grid as G
+
+log = logging.getLogger("khronos_gb300")
 from .monitors import DFTMonitor, FluxMonitor, auto_decimation, flux_from_dft
 from .sources import ContinuousWaveSource, CustomSource, GaussianPulseSource
 from .spec import (KH_F32, KH_F64, MAT_CHI3, MAT_EPS_INV, MAT_MU_INV, MAT_SIGMA_B, MAT_SIGMA_D,
@@ -236,6 +240,21 @@ class Simulation:
         if (until is None) == (until_after_sources is None):
             raise ValueError("Must specify exactly one of until / until_after_sources")
         self.prepare()
+        log.info("Starting simulation...")
+        t_start = time.perf_counter()
+        step_start = self.timestep
+        try:
+            self._run_steps(until, until_after_sources)
+        finally:
+            self._dev.synchronize()
+            total = self.timestep - step_start
+            elapsed = time.perf_counter() - t_start
+            if total > 0 and elapsed > 0:
+                n = self.grid.n
+                rate = n[0] * n[1] * max(1, n[2]) * total / elapsed / 1e6
+                log.info("Simulation complete: %d steps in %.3fs (%.1f MVoxels/s)", total, elapsed, rate)
+
+    def _run_steps(self, until, until_after_sources):
         if until_after_sources is not None:
             last = self.last_source_time()
             n = 0
@@ -243,6 +262,7 @@ class Simulation:
             while self.round_time(ts + n) <= last:
                 n += 1
             self.step(n)
+            log.info("All sources have terminated...")
             until = until_after_sources
         if not callable(until):
             self.step(self.steps_until(until))

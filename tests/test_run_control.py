@@ -68,7 +68,9 @@ def test_stop_when_dft_decayed_runtime_bounds(kh):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("dtype", ["f32", "f64"])
-def test_run_until_stop_function_matches_per_step_replay(kh, gpu_lib, dtype):
+def test_run_until_stop_function_matches_per_step_replay(kh, gpu_lib, dtype, caplog):
+    import logging
+
     from khronos_gb300 import configs
 
     def fresh():
@@ -76,7 +78,11 @@ def test_run_until_stop_function_matches_per_step_replay(kh, gpu_lib, dtype):
 
     sim = fresh()
     stop = kh.stop_when_dft_decayed(tolerance=1e-6, minimum_runtime=2.0)
-    sim.run(until_after_sources=stop)
+    with caplog.at_level(logging.INFO, logger="khronos_gb300"):
+        sim.run(until_after_sources=stop)
+    msgs = [r.getMessage() for r in caplog.records]
+    assert "All sources have terminated..." in msgs
+    assert any(m.startswith(f"Simulation complete: {sim.timestep} steps") for m in msgs)
     t_stop = sim.timestep
     norms_at_stop = sim.dft_fields_norms()
     sim.close()
