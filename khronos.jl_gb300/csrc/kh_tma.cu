@@ -204,9 +204,12 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
       // register loads a plane ahead of its update find it there.  Tiles that
       // keep state only for special cells are left to those loads (the
       // tile-bit lookup on the issuing thread would delay the ring); the FULL
-      // variants, at their register limit, do without.
+      // variants, at their register limit, do without.  A tile that meets the
+      // CPML only along x has state in 12 of its 64 columns: the whole-tile
+      // prefetch pays off on the H half, while the E half, which runs at its
+      // DRAM limit, loses more to the unused bytes than it gains.
       const bool tfz = plane < p.pml_lo[2] || plane >= p.nz - p.pml_hi[2];
-      if (!FULL && (tfx || tfy || tfz)) {
+      if (!FULL && (tfy || tfz || (H && tfx))) {
         const bool af[3] = {tfx, tfy, tfz};
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
