@@ -162,6 +162,10 @@ struct HalfStepParams {
   PoleParams<T> poles[kMaxPoles];
 
   int* err;  // set to KH_ERR_TIMEOUT by a kernel whose bounded wait gave up
+  // Failure-detection test hook (0 in normal runs): nonzero launches the FP32
+  // LEAN TMA kernels' test instantiation, whose first ring stage expects 16
+  // bytes that never arrive, so its waits give up after 4096 polls.
+  uint32_t stall_tx;
 };
 
 // TMA-staged half-step: tile of kTmaX × kTmaY cells per CTA (one warp per

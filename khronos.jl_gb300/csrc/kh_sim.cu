@@ -645,6 +645,7 @@ class Sim : public SimBase {
     use_tma_ = !(kv && std::string(kv) == "simt");
     if (use_tma_) KH_TRY(build_tma_maps());
     zplanes_ = choose_zplanes();
+    if (const char* sv = std::getenv("KHRONOS_GB300_TEST_STALL")) stall_tx_ = std::string(sv) == "1" ? 16u : 0u;
     // the zeroing and uploads above ran on the legacy default stream; wait for
     // them only (work of other simulations on non-blocking streams goes on)
     KH_CUDA(cudaStreamSynchronize(cudaStreamLegacy));
@@ -1676,6 +1677,7 @@ class Sim : public SimBase {
     p.n_src = nsrc_;
     p.cell_class = cls_;
     p.err = err_dev_;
+    p.stall_tx = stall_tx_;
     p.slot_off = slot_off_;
     p.ent_src = ent_src_;
     p.ent_comp = ent_comp_;
@@ -1735,6 +1737,9 @@ class Sim : public SimBase {
   long long* slot_cell_ = nullptr;
   int nslots_ = 0;
   int* err_dev_ = nullptr;
+  // KHRONOS_GB300_TEST_STALL=1 at prepare: the TMA half-step kernels wait for
+  // bytes that never arrive and give up (tests of the timeout status only)
+  uint32_t stall_tx_ = 0;
   bool use_tma_ = true;
   int zplanes_ = 10;
   int tma_slots_ = 0;  // SMs × resident TMA-kernel CTAs per SM

@@ -32,6 +32,7 @@ KH_DBG_READER(dbg_read_tma)
 namespace {
 
 constexpr long long kWaitLimit = 1ll << 22;
+constexpr long long kStallWaitLimit = 4096;  // the failure-detection test hook's limit
 
 __device__ __forceinline__ uint32_t smem_u32(const void* ptr) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(ptr));
@@ -62,9 +63,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait for the phase with parity `parity`; false after kWaitLimit polls.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (long long it = 0; it < kWaitLimit; ++it)
+// Bounded wait for the phase with parity `parity`; false after `limit` polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long limit = kWaitLimit) {
+  for (long long it = 0; it < limit; ++it)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
@@ -140,7 +141,7 @@ constexpr int tma_min_blocks() {
   return sizeof(T) == 4 ? (FULL ? kTmaMinBlocks - 1 : kTmaMinBlocks) : 2;
 }
 
-template <typename T, bool H, bool CPML, bool FULL>
+template <typename T, bool H, bool CPML, bool FULL, bool STALL = false>
 __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
     half_step_tma_kernel(const HalfStepParams<T> p, const __grid_constant__ TmaMaps maps) {
   using G = TmaGeom<T>;
@@ -163,6 +164,8 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
   const int k1 = min(k0 + p.zplanes, p.nz);
   const int N = k1 - k0;  // planes computed; loads n = 0..N
   const bool pervox = p.m_inv[0] != nullptr;
+  // the failure-detection test instantiation waits briefly for bytes that never come
+  constexpr long long kLimit = STALL ? kStallWaitLimit : kWaitLimit;
 
   if (tid == 0) {
     for (int st = 0; st < kTmaStages; ++st) mbar_init(&bars[st], 1);
@@ -182,7 +185,8 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
     T* dst = stages + st * G::STAGE;
     const int plane = H ? k0 + n : k0 - 1 + n;
     const bool comp = H ? (n < N) : (n >= 1);
-    mbar_arrive_expect_tx(&bars[st], a_bytes + (comp ? o_bytes : 0u));
+    // (STALL: failure-detection test instantiation, 16 bytes that never arrive)
+    mbar_arrive_expect_tx(&bars[st], a_bytes + (comp ? o_bytes : 0u) + (STALL && n == 0 ? 16u : 0u));
     const int zc = plane + 1;                      // padded plane index
     const int ax = H ? G::HX + x_tile : x_tile;    // padded x of the A box
     const int ay = H ? 1 + y_tile : y_tile;        // padded y of the A box
@@ -266,8 +270,8 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
     }
     const int ncur = H ? c : c + 1;
     const int nnb = H ? c + 1 : c;
-    bool ok = mbar_wait(&bars[ncur % kTmaStages], uint32_t((ncur / kTmaStages) & 1));
-    ok = ok && mbar_wait(&bars[nnb % kTmaStages], uint32_t((nnb / kTmaStages) & 1));
+    bool ok = mbar_wait(&bars[ncur % kTmaStages], uint32_t((ncur / kTmaStages) & 1), kLimit);
+    ok = ok && mbar_wait(&bars[nnb % kTmaStages], uint32_t((nnb / kTmaStages) & 1), kLimit);
     if (!ok) {
       bad = true;
       if (p.err) atomicExch(p.err, KH_ERR_TIMEOUT);
@@ -432,7 +436,7 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
       // stop: wait (bounded) for the copies this CTA issued, then leave
       if (tid == 0) {
         const int issued = min(c + kTmaStages, N + 1);
-        for (int n = c; n < issued; ++n) mbar_wait(&bars[n % kTmaStages], uint32_t((n / kTmaStages) & 1));
+        for (int n = c; n < issued; ++n) mbar_wait(&bars[n % kTmaStages], uint32_t((n / kTmaStages) & 1), kLimit);
       }
       return;
     }
@@ -455,6 +459,13 @@ static void launch_tma_variant(bool h_half, const HalfStepParams<T>& p, const Tm
   dim3 block(32, kTmaY, 1);
   dim3 grid((p.nx + kTmaX - 1) / kTmaX, (p.ny + kTmaY - 1) / kTmaY, (p.nz + p.zplanes - 1) / p.zplanes);
   const size_t smem = TmaGeom<T>::SMEM;
+  if constexpr (sizeof(T) == 4 && !FULL) {
+    if (p.stall_tx) {  // failure-detection test instantiation (FP32 LEAN only)
+      if (h_half) half_step_tma_kernel<T, true, CPML, FULL, true><<<grid, block, smem, st>>>(p, maps);
+      else half_step_tma_kernel<T, false, CPML, FULL, true><<<grid, block, smem, st>>>(p, maps);
+      return;
+    }
+  }
   if (h_half) half_step_tma_kernel<T, true, CPML, FULL><<<grid, block, smem, st>>>(p, maps);
   else half_step_tma_kernel<T, false, CPML, FULL><<<grid, block, smem, st>>>(p, maps);
 }
@@ -471,9 +482,9 @@ void launch_half_step_tma(bool h_half, const HalfStepParams<T>& p, const TmaMaps
   }
 }
 
-template <typename T, bool H, bool CPML, bool FULL>
+template <typename T, bool H, bool CPML, bool FULL, bool STALL = false>
 static int set_smem_attr() {
-  return int(cudaFuncSetAttribute(half_step_tma_kernel<T, H, CPML, FULL>,
+  return int(cudaFuncSetAttribute(half_step_tma_kernel<T, H, CPML, FULL, STALL>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, int(TmaGeom<T>::SMEM)));
 }
 
@@ -488,6 +499,12 @@ int prepare_tma_kernels() {
   e |= set_smem_attr<T, false, true, false>();
   e |= set_smem_attr<T, false, false, true>();
   e |= set_smem_attr<T, false, false, false>();
+  if constexpr (sizeof(T) == 4) {
+    e |= set_smem_attr<T, true, true, false, true>();
+    e |= set_smem_attr<T, true, false, false, true>();
+    e |= set_smem_attr<T, false, true, false, true>();
+    e |= set_smem_attr<T, false, false, false, true>();
+  }
   return e;
 }
 
