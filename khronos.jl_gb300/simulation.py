@@ -130,22 +130,22 @@ class Simulation:
             sp.eps_inv = float(T(self.eps_inv))
         else:
             for c in range(3):
-                sp.materials.append((MAT_EPS_INV, c, np.asarray(self.eps_inv[c], dtype=np.float64)))
+                sp.materials.append((MAT_EPS_INV, c, _xfast(self.eps_inv[c])))
         if np.isscalar(self.mu_inv):
             sp.mu_inv = float(T(self.mu_inv))
         else:
             for c in range(3):
-                sp.materials.append((MAT_MU_INV, c, np.asarray(self.mu_inv[c], dtype=np.float64)))
+                sp.materials.append((MAT_MU_INV, c, _xfast(self.mu_inv[c])))
         for kind, arrs in ((MAT_SIGMA_D, self.sigma_d), (MAT_SIGMA_B, self.sigma_b)):
             if arrs is not None:
                 for c in range(3):
                     if arrs[c] is not None:
-                        sp.materials.append((kind, c, np.asarray(arrs[c], dtype=np.float64)))
+                        sp.materials.append((kind, c, _xfast(arrs[c])))
         if self.chi3 is not None:
-            sp.materials.append((MAT_CHI3, 0, np.asarray(self.chi3, dtype=np.float64)))
+            sp.materials.append((MAT_CHI3, 0, _xfast(self.chi3)))
         for sus, sigma in self.poles:
             sp.poles.append(PoleSpec(coeffs=ade_coefficients(sus, float(g.dt)),
-                                     sigma=np.asarray(sigma, dtype=np.float64)))
+                                     sigma=_xfast(sigma)))
         # sources (assemble_sources, Sources.jl:44-92)
         for src in self.sources:
             tp = src.time_profile
@@ -345,6 +345,13 @@ class Simulation:
         if self._dev is not None:
             self._dev.close()
             self._dev = None
+
+
+def _xfast(a) -> np.ndarray:
+    """A cell-indexed [i, j, k] array in FP64 with x fastest in memory (the
+    ABI's layout, Julia's column-major order), so that handing it to the
+    library needs no transposing copy."""
+    return np.asfortranarray(a, dtype=np.float64)
 
 
 class stop_when_dft_decayed:

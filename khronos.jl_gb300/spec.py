@@ -139,8 +139,9 @@ class SimSpec:
 
 
 def flat_f(a: np.ndarray) -> np.ndarray:
-    """x-fastest contiguous float64 copy of a cell-indexed array."""
-    return np.ascontiguousarray(np.asarray(a, dtype=np.float64).ravel(order="F"))
+    """x-fastest contiguous float64 view (or copy) of a cell-indexed array: no
+    copy when it is already FP64 with x fastest."""
+    return np.asarray(a, dtype=np.float64).ravel(order="F")
 
 
 def flat_complex(a: np.ndarray) -> np.ndarray:
