@@ -393,9 +393,11 @@ kh_status kh_sim_model_bytes_per_step(const kh_sim* sim, double* out);
 kh_status kh_sim_model_bytes_split(const kh_sim* sim, double* h_half, double* e_half,
                                    double* dft);
 
-/* kh_sim_step with CUDA events recorded on `stream` around every launch
- * group; returns the summed device time (ms) of the H half-step kernels, the
- * E half-step kernels and the DFT launches of these nsteps. */
+/* kh_sim_step with CUDA events recorded on `stream` around the launch groups
+ * (H half-step, E half-step, DFT) of every 8th step (timestep a multiple of
+ * 8); returns the device time (ms) of the H half-step kernels, the E
+ * half-step kernels and the DFT launches of these nsteps, the sampled steps'
+ * sums scaled to all nsteps.  No step-graph replay in timed runs. */
 kh_status kh_sim_step_timed(kh_sim* sim, int64_t nsteps, void* stream, double* h_ms,
                             double* e_ms, double* dft_ms);
 

@@ -352,3 +352,23 @@ def test_field_view_is_the_field_in_place(kh, gpu_lib, dtype):
         assert math.isclose(dev, norms[c], rel_tol=1e-12, abs_tol=1e-300)
     del views
     g.close()
+
+
+@pytest.mark.gpu
+def test_step_timed_is_invisible(kh, gpu_lib):
+    """kh_sim_step_timed (events around the launches of every 8th step) gives
+    the fields of a plain run and positive per-half times."""
+    from khronos_gb300 import configs
+    from khronos_gb300.device import GpuSim
+
+    spec = configs.waveguide(dtype="f32", scale=0.25).sim.spec()
+    a = GpuSim(spec, lib=gpu_lib)
+    a.step(93)
+    b = GpuSim(spec, lib=gpu_lib)
+    h, e, d = b.step_timed(93)
+    assert h > 0 and e > 0 and d >= 0
+    for c in range(6):
+        assert np.array_equal(a.field(c), b.field(c))
+    assert np.array_equal(a.dft(0), b.dft(0))
+    a.close()
+    b.close()
