@@ -394,8 +394,8 @@ kh_status kh_sim_model_bytes_split(const kh_sim* sim, double* h_half, double* e_
                                    double* dft);
 
 /* kh_sim_step with CUDA events recorded on `stream` around the launch groups
- * (H half-step, E half-step, DFT) of every 8th step (timestep a multiple of
- * 8); returns the device time (ms) of the H half-step kernels, the E
+ * (H half-step, E half-step, DFT) of every 8th step of the call (its first
+ * step included); returns the device time (ms) of the H half-step kernels, the E
  * half-step kernels and the DFT launches of these nsteps, the sampled steps'
  * sums scaled to all nsteps.  No step-graph replay in timed runs. */
 kh_status kh_sim_step_timed(kh_sim* sim, int64_t nsteps, void* stream, double* h_ms,

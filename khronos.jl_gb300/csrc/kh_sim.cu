@@ -1096,10 +1096,11 @@ class Sim : public SimBase {
   struct Timing {
     double h = 0, e = 0, dft = 0;
     int64_t sampled = 0;  // steps whose launches were bracketed with events
+    int64_t done = 0;     // steps of the timed call issued so far
   };
-  // Timed runs bracket the launches of every kTimeSample-th step (timestep a
-  // multiple of it) with events; one event pair per launch group on every
-  // step would itself cost ~4 % of the step time.
+  // Timed runs bracket the launches of every kTimeSample-th step of the call
+  // (its first step included) with events; one event pair per launch group on
+  // every step would itself cost ~4 % of the step time.
   static constexpr int kTimeSample = 8;
   struct PoleH {
     kh_pole_coeffs c;
@@ -1334,7 +1335,7 @@ class Sim : public SimBase {
         events_.push_back(ev);
       }
     }
-    auto sampled = [&](int s) { return timing && (timestep_ + s) % kTimeSample == 0; };
+    auto sampled = [&](int s) { return timing && (timing->done + s) % kTimeSample == 0; };
     auto mark = [&](int s, int k) {
       if (sampled(s)) cudaEventRecord(events_[5 * s + k], stream);
     };
@@ -1446,7 +1447,7 @@ class Sim : public SimBase {
     if (timing) {
       KH_CUDA(cudaEventSynchronize(batch_done_));
       for (int s = 0; s < nb; ++s) {
-        if ((timestep_ - nb + s) % kTimeSample != 0) continue;
+        if (!sampled(s)) continue;
         ++timing->sampled;
         float a = 0, b = 0, c = 0, d = 0;
         KH_CUDA(cudaEventElapsedTime(&a, events_[5 * s], events_[5 * s + 1]));
@@ -1457,6 +1458,7 @@ class Sim : public SimBase {
         timing->dft += b + d;
         timing->e += c;
       }
+      timing->done += nb;
     }
     return KH_OK;
   }
