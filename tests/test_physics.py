@@ -154,3 +154,23 @@ def test_fresnel_case_matches_oracle(kh, oracle, gpu_lib, dtype):
 
     sim = _fresnel_sim(kh, 10, True, dtype)
     compare(sim.spec(), 400, oracle, gpu_lib, TOL[dtype])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_oblique_planewave_matches_oracle(kh, oracle, gpu_lib, dtype):
+    """An oblique, rotated plane wave (phase varying across the injection
+    plane, four current components) over a dielectric block, device against
+    the oracle."""
+    from khronos_gb300.geometry import Cuboid, Material, Object
+    from test_gpu_parity import TOL, compare
+
+    src = kh.PlaneWaveSource(time_profile=kh.GaussianPulseSource(fcen=0.9, fwidth=0.3),
+                             center=(0.0, 0.0, -0.6), size=(math.inf, math.inf, 0.0),
+                             angle_theta=0.7, angle_phi=0.35, polarization_angle=0.6)
+    assert len(src.components()) == 4
+    geom = [Object(Cuboid((0.1, -0.1, 0.3), (0.8, 0.6, 0.4)), Material(eps=6.0))]
+    mon = kh.DFTMonitor(component=kh.EY, center=(0, 0, 0.5), size=(1.2, 1.0, 0.0), frequencies=[0.8, 1.0])
+    sim = kh.Simulation(cell_size=(2.2, 1.9, 2.1), resolution=10, sources=[src], geometry=geom,
+                        boundaries=[[0.3, 0.3]] * 3, monitors=[mon], dtype=dtype)
+    compare(sim.spec(), 120, oracle, gpu_lib, TOL[dtype])
