@@ -52,7 +52,16 @@ class Cylinder:
 
 @dataclass
 class Material:
+    """Material(ε, μ, σD, σB, χ3) of an object (isotropic scalars).  ε is
+    rasterised on the device with optional subpixel smoothing; μ, σD, σB and
+    χ3 on the host (``material_arrays``), unsmoothed, as the reference
+    rasterises them (Geometry.jl:223-250, 610-636)."""
+
     eps: float = 1.0
+    mu: float = 1.0
+    sigma_d: float = 0.0
+    sigma_b: float = 0.0
+    chi3: float = 0.0
 
 
 @dataclass
@@ -82,3 +91,76 @@ def geometry_spec(objects: Sequence[Object], grid, background: float = 1.0, smoo
         shape, axis, c, s = o.shape.raw()
         raw.append((shape, axis, c, s, float(o.material.eps)))
     return GeometrySpec(raw, float(background), tuple(grid.component_origin(CENTER)), SMOOTHING[smoothing])
+
+
+def _component_axes(grid, comp: int):
+    """Sample coordinates of a component along x, y, z: the centre of cell
+    (0,0,0) moved by the component's Yee shift, plus i·Δ (the device's
+    arithmetic for ε)."""
+    import numpy as np
+
+    from .grid import CENTER
+
+    base = grid.component_origin(CENTER)
+    sh = grid.yee_shift(comp)
+    d = [float(v) for v in grid.delta]
+    return [(base[a] + sh[a]) + np.arange(grid.n[a], dtype=np.float64) * d[a] for a in range(3)]
+
+
+def _inside_mask(raw, axes):
+    """Inclusive inside test of one raw object over the sample lattice
+    (the device predicate, same operation order, no fused multiply-add)."""
+    import numpy as np
+
+    shape, axis, c, s = raw[:4]
+    X = [axes[a].reshape([-1 if b == a else 1 for b in range(3)]) - c[a] for a in range(3)]
+    if shape == SHAPE_BALL:
+        return np.sqrt(X[0] * X[0] + X[1] * X[1] + X[2] * X[2]) <= s[0]
+    if shape == SHAPE_CUBOID:
+        m = np.ones(tuple(len(x) for x in axes), dtype=bool)
+        for a in range(3):
+            m &= np.abs(X[a]) <= 0.5 * s[a]
+        return m
+    a1, a2 = (axis + 1) % 3, (axis + 2) % 3
+    return (np.sqrt(X[a1] * X[a1] + X[a2] * X[a2]) <= s[0]) & (np.abs(X[axis]) <= 0.5 * s[1])
+
+
+def rasterize_values(objects: Sequence[Object], grid, comp: int, values: Sequence[float], background: float):
+    """One value per object painted at component ``comp``'s Yee positions:
+    the first object that contains a point sets it (objects painted in
+    reverse order, Geometry.jl:223-250), ``background`` elsewhere.  Returns
+    an [i, j, k] array, x fastest in memory."""
+    import numpy as np
+
+    axes = _component_axes(grid, comp)
+    out = np.full(tuple(grid.n), float(background), dtype=np.float64, order="F")
+    for o, v in reversed(list(zip(objects, values))):
+        out[_inside_mask(o.shape.raw(), axes)] = float(v)
+    return out
+
+
+def material_arrays(objects: Sequence[Object], grid):
+    """Per-voxel μ⁻¹, σD, σB and χ3 arrays of the objects, each only when some
+    object departs from free space (the reference allocates them on the same
+    condition, needs_perm / needs_conductivities, Geometry.jl:314-351):
+    list of (kind, component, array) in the SimSpec materials format.
+    μ⁻¹ and σB sample the H components' positions, σD the E components', χ3
+    the cell centres.  Dispersive susceptibilities of objects are not
+    rasterised (give poles as arrays)."""
+    from .grid import CENTER, EX, HX
+    from .spec import MAT_CHI3, MAT_MU_INV, MAT_SIGMA_B, MAT_SIGMA_D
+
+    out = []
+    mats = [o.material for o in objects]
+    if any(m.mu != 1.0 for m in mats):
+        for c in range(3):
+            out.append((MAT_MU_INV, c, rasterize_values(objects, grid, HX + c, [1.0 / m.mu for m in mats], 1.0)))
+    if any(m.sigma_d != 0.0 for m in mats):
+        for c in range(3):
+            out.append((MAT_SIGMA_D, c, rasterize_values(objects, grid, EX + c, [m.sigma_d for m in mats], 0.0)))
+    if any(m.sigma_b != 0.0 for m in mats):
+        for c in range(3):
+            out.append((MAT_SIGMA_B, c, rasterize_values(objects, grid, HX + c, [m.sigma_b for m in mats], 0.0)))
+    if any(m.chi3 != 0.0 for m in mats):
+        out.append((MAT_CHI3, 0, rasterize_values(objects, grid, CENTER, [m.chi3 for m in mats], 0.0)))
+    return out

@@ -143,6 +143,16 @@ class Simulation:
                         sp.materials.append((kind, c, _xfast(arrs[c])))
         if self.chi3 is not None:
             sp.materials.append((MAT_CHI3, 0, _xfast(self.chi3)))
+        if self.geometry is not None:  # μ, σD, σB, χ3 of the objects (host rasterisation)
+            from .geometry import material_arrays
+
+            geo_mats = material_arrays(self.geometry, g)
+            given = {(kind, c) for kind, c, _ in sp.materials}
+            clash = [(kind, c) for kind, c, _ in geo_mats if (kind, c) in given or
+                     (kind == MAT_MU_INV and not np.isscalar(self.mu_inv))]
+            if clash:
+                raise ValueError("a material property is given both by geometry objects and by an array")
+            sp.materials.extend(geo_mats)
         for sus, sigma in self.poles:
             sp.poles.append(PoleSpec(coeffs=ade_coefficients(sus, float(g.dt)),
                                      sigma=_xfast(sigma)))

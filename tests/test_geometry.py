@@ -177,3 +177,65 @@ def test_run_with_device_geometry_matches_oracle(kh, oracle, gpu_lib):
     gpu.close()
     ref.close()
     assert max(errs) <= 1e-10, errs
+
+
+def test_host_rasterisation_matches_oracle_eps_lattice(kh):
+    """The host rasteriser of μ, σD, σB and χ3 samples the same Yee positions
+    with the same inside test as the ε rasterisation: painting the objects'
+    ε with it gives the oracle's unsmoothed ε⁻¹ arrays exactly."""
+    import oracle.geometry as og
+    from khronos_gb300.geometry import Ball, Cuboid, Cylinder, Material, Object, geometry_spec, rasterize_values
+
+    objs = [Object(Ball((0.12, -0.05, 0.07), 0.31), Material(eps=4.0)),
+            Object(Cuboid((-0.2, 0.1, 0.0), (0.5, 0.3, 0.4)), Material(eps=2.5)),
+            Object(Cylinder((0.05, 0.2, -0.1), 0.2, 0.6, axis=0), Material(eps=9.0))]
+    for dtype in ("f64", "f32"):
+        sim = kh.Simulation(cell_size=(1.3, 1.1, 0.9), resolution=20, dtype=dtype, geometry=objs,
+                            background_eps=1.5)
+        g = sim.grid
+        ref = og.eps_inv_arrays(geometry_spec(objs, g, 1.5, "none"), g.n, g.delta)
+        for c in range(3):
+            got = 1.0 / rasterize_values(objs, g, kh.EX + c, [o.material.eps for o in objs], 1.5)
+            assert np.array_equal(got, ref[c]), (dtype, c)
+
+
+def test_material_arrays_from_objects(kh):
+    from khronos_gb300.geometry import Ball, Cuboid, Material, Object
+    from khronos_gb300.spec import MAT_CHI3, MAT_MU_INV, MAT_SIGMA_B, MAT_SIGMA_D
+
+    objs = [Object(Ball((0.0, 0.0, 0.0), 0.25), Material(eps=2.0, mu=2.0, chi3=0.01)),
+            Object(Cuboid((0.0, 0.0, 0.0), (0.9, 0.9, 0.2)), Material(eps=3.0, sigma_d=0.4))]
+    sim = kh.Simulation(cell_size=(1.2, 1.2, 1.0), resolution=10, geometry=objs, dtype="f64")
+    sp = sim.spec()
+    kinds = sorted({k for k, _, _ in sp.materials})
+    assert kinds == sorted([MAT_MU_INV, MAT_SIGMA_D, MAT_CHI3])  # no σB anywhere → no array
+    mats = {(k, c): a for k, c, a in sp.materials}
+    mu = mats[(MAT_MU_INV, 0)]
+    assert set(np.unique(mu)) == {0.5, 1.0}
+    # the ball wins where it overlaps the slab: χ3 there, σD of the slab elsewhere
+    chi3 = mats[(MAT_CHI3, 0)]
+    n = sp.n
+    assert chi3[n[0] // 2, n[1] // 2, n[2] // 2] == 0.01
+    sd = mats[(MAT_SIGMA_D, 2)]
+    assert sd.max() == 0.4 and sd[n[0] // 2, n[1] // 2, n[2] // 2] == 0.0
+    with pytest.raises(ValueError):
+        kh.Simulation(cell_size=(1.2, 1.2, 1.0), resolution=10, geometry=objs, dtype="f64",
+                      chi3=np.zeros(n)).spec()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_object_materials_match_oracle(kh, oracle, gpu_lib, dtype):
+    """Objects carrying μ, χ3 and σD next to device-rasterised, smoothed ε:
+    the step loop against the oracle (no PML, so the conductivity stays out of
+    play as on the reference's CPU path)."""
+    from khronos_gb300.geometry import Ball, Cuboid, Material, Object
+    from test_gpu_parity import TOL, compare
+
+    objs = [Object(Ball((0.1, 0.0, 0.05), 0.3), Material(eps=3.0, mu=1.5, chi3=0.02)),
+            Object(Cuboid((-0.1, 0.05, 0.0), (0.8, 0.5, 0.3)), Material(eps=2.0, sigma_d=0.3))]
+    src = kh.UniformSource(time_profile=kh.GaussianPulseSource(fcen=0.9, fwidth=0.4), component=kh.EY,
+                           center=(-0.4, 0.0, 0.0), size=(0.0, 0.4, 0.4), amplitude=3.0)
+    sim = kh.Simulation(cell_size=(1.7, 1.5, 1.3), resolution=10, sources=[src], geometry=objs,
+                        subpixel_smoothing="volume", dtype=dtype)
+    compare(sim.spec(), 90, oracle, gpu_lib, TOL[dtype], check_dft=False)
