@@ -52,16 +52,18 @@ class Cylinder:
 
 @dataclass
 class Material:
-    """Material(ε, μ, σD, σB, χ3) of an object (isotropic scalars).  ε is
-    rasterised on the device with optional subpixel smoothing; μ, σD, σB and
-    χ3 on the host (``material_arrays``), unsmoothed, as the reference
-    rasterises them (Geometry.jl:223-250, 610-636)."""
+    """Material(ε, μ, σD, σB, χ3, susceptibilities) of an object (isotropic
+    scalars; ε is ε∞ when poles are given).  ε is rasterised on the device
+    with optional subpixel smoothing; μ, σD, σB and χ3 on the host
+    (``material_arrays``), unsmoothed, as the reference rasterises them
+    (Geometry.jl:223-250, 610-636); poles through ``pole_arrays``."""
 
     eps: float = 1.0
     mu: float = 1.0
     sigma_d: float = 0.0
     sigma_b: float = 0.0
     chi3: float = 0.0
+    susceptibilities: tuple = ()  # LorentzianSusceptibility / DrudeSusceptibility poles
 
 
 @dataclass
@@ -163,4 +165,52 @@ def material_arrays(objects: Sequence[Object], grid):
             out.append((MAT_SIGMA_B, c, rasterize_values(objects, grid, HX + c, [m.sigma_b for m in mats], 0.0)))
     if any(m.chi3 != 0.0 for m in mats):
         out.append((MAT_CHI3, 0, rasterize_values(objects, grid, CENTER, [m.chi3 for m in mats], 0.0)))
+    return out
+
+
+def pole_arrays(objects: Sequence[Object], grid, boundaries):
+    """init_polarization! (Geometry.jl:1059-1250): one σ array per distinct
+    pole (keyed by (ω0, γ), in the order first met), sampled at the Ex
+    positions and shared by the three components.  Each pole's array is
+    painted by the objects that carry that pole, in reverse order (so an
+    earlier object without the pole does not clear it, as in the
+    reference), then zeroed at points inside a PML slab by physical
+    coordinate.  Returns [(susceptibility, σ array)]."""
+    import numpy as np
+
+    from .grid import EX
+
+    poles, seen = [], set()
+    for o in objects:
+        for sus in o.material.susceptibilities:
+            key = (float(sus.omega_0), float(sus.gamma))
+            if key not in seen:
+                seen.add(key)
+                poles.append(sus)
+    if not poles:
+        return []
+    axes = _component_axes(grid, EX)
+    out = []
+    for pole in poles:
+        key = (float(pole.omega_0), float(pole.gamma))
+        sig = np.zeros(tuple(grid.n), dtype=np.float64, order="F")
+        for o in reversed(list(objects)):
+            val = next((float(x.sigma) for x in o.material.susceptibilities
+                        if (float(x.omega_0), float(x.gamma)) == key), None)
+            if val is not None:
+                sig[_inside_mask(o.shape.raw(), axes)] = val
+        if boundaries is not None:
+            pml = np.zeros(tuple(grid.n), dtype=bool)
+            for a in range(3):
+                lo = grid.cell_center[a] - float(grid.cell_size[a]) / 2
+                hi = grid.cell_center[a] + float(grid.cell_size[a]) / 2
+                left, right = float(boundaries[a][0]), float(boundaries[a][1])
+                m = np.zeros(grid.n[a], dtype=bool)
+                if left > 0:
+                    m |= axes[a] < lo + left
+                if right > 0:
+                    m |= axes[a] > hi - right
+                pml |= m.reshape([-1 if b == a else 1 for b in range(3)])
+            sig[pml] = 0.0
+        out.append((pole, sig))
     return out

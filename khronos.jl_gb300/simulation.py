@@ -122,7 +122,26 @@ class Simulation:
                 sp.sigma_b[a] = s
                 sp.sigma_d[a] = s.copy()
         # materials
-        if self.geometry is not None:  # rasterised on the device (kh_sim_set_geometry)
+        geo_poles = []
+        if self.geometry is not None:
+            from .geometry import pole_arrays
+
+            geo_poles = pole_arrays(self.geometry, g, self.boundaries)
+        if self.geometry is not None and geo_poles:
+            # dispersive objects: ε∞ on the host too, so that the χ1
+            # correction (Geometry.jl:1236-1250) can act on it
+            from .geometry import rasterize_values
+
+            if self.subpixel_smoothing != "none":
+                raise NotImplementedError("subpixel smoothing together with dispersive objects")
+            if self.poles:
+                raise ValueError("give poles either on geometry objects or as arrays, not both")
+            eps = [1.0 / rasterize_values(self.geometry, g, G.EX + c, [o.material.eps for o in self.geometry],
+                                          self.background_eps) for c in range(3)]
+            eps = apply_chi1_correction(eps, geo_poles, g.dt, T=np.float64)
+            for c in range(3):
+                sp.materials.append((MAT_EPS_INV, c, _xfast(eps[c])))
+        elif self.geometry is not None:  # rasterised on the device (kh_sim_set_geometry)
             from .geometry import geometry_spec
 
             sp.geometry = geometry_spec(self.geometry, g, self.background_eps, self.subpixel_smoothing)
@@ -153,7 +172,7 @@ class Simulation:
             if clash:
                 raise ValueError("a material property is given both by geometry objects and by an array")
             sp.materials.extend(geo_mats)
-        for sus, sigma in self.poles:
+        for sus, sigma in list(self.poles) + geo_poles:
             sp.poles.append(PoleSpec(coeffs=ade_coefficients(sus, float(g.dt)),
                                      sigma=_xfast(sigma)))
         # sources (assemble_sources, Sources.jl:44-92)

@@ -239,3 +239,63 @@ def test_object_materials_match_oracle(kh, oracle, gpu_lib, dtype):
     sim = kh.Simulation(cell_size=(1.7, 1.5, 1.3), resolution=10, sources=[src], geometry=objs,
                         subpixel_smoothing="volume", dtype=dtype)
     compare(sim.spec(), 90, oracle, gpu_lib, TOL[dtype], check_dft=False)
+
+
+def test_dispersive_objects_pole_arrays(kh):
+    """init_polarization! on the host: one σ array per distinct (ω0, γ) pole,
+    painted only by the objects that carry it (an earlier object without the
+    pole does not clear it), zeroed inside PML slabs by physical coordinate;
+    ε∞ rasterised on the host and χ1-corrected."""
+    from khronos_gb300.geometry import Ball, Cuboid, Material, Object, pole_arrays, rasterize_values
+    from khronos_gb300.simulation import apply_chi1_correction
+
+    lor = kh.LorentzianSusceptibility(1.0, 0.05, 1.0)
+    lor_b = kh.LorentzianSusceptibility(1.0, 0.05, 3.0)  # same pole key, other strength
+    dru = kh.DrudeSusceptibility(0.1, 5.0)
+    objs = [Object(Cuboid((0.0, 0.0, 0.0), (0.3, 0.3, 0.3)), Material(eps=1.5)),          # no pole, first
+            Object(Ball((0.0, 0.0, 0.0), 0.35), Material(eps=2.0, susceptibilities=(lor,))),
+            Object(Ball((0.45, 0.0, 0.0), 0.3), Material(eps=1.0, susceptibilities=(dru, lor_b)))]
+    bnd = [[0.3, 0.3]] * 3
+    sim = kh.Simulation(cell_size=(1.8, 1.2, 1.2), resolution=10, geometry=objs, boundaries=bnd, dtype="f64")
+    g = sim.grid
+    poles = pole_arrays(objs, g, bnd)
+    assert [(p.omega_0, p.gamma) for p, _ in poles] == [(1.0, 0.05), (0.0, 0.1)]
+    sig_l, sig_d = poles[0][1], poles[1][1]
+    c = tuple(v // 2 for v in g.n)
+    assert sig_l[c] == 1.0  # under the pole-free cuboid that wins ε: still painted
+    assert set(np.unique(sig_l)) <= {0.0, 1.0, 3.0} and 3.0 in sig_l
+    assert set(np.unique(sig_d)) == {0.0, 5.0}
+    # no pole inside the PML slabs, by physical coordinate of the Ex samples:
+    # x at cell centres (3 samples per side), y and z on the nodes (3 below
+    # −0.3, 2 above +0.3)
+    for arr in (sig_l, sig_d):
+        assert not arr[:3].any() and not arr[-3:].any()
+        assert not arr[:, :3].any() and not arr[:, -2:].any()
+        assert not arr[:, :, :3].any() and not arr[:, :, -2:].any()
+    sp = sim.spec()
+    assert sp.geometry is None and len(sp.poles) == 2
+    eps = [1.0 / rasterize_values(objs, g, kh.EX + k, [o.material.eps for o in objs], 1.0) for k in range(3)]
+    want = apply_chi1_correction(eps, poles, g.dt, T=np.float64)
+    got = {k: a for kind, k, a in sp.materials if kind == 0}
+    for k in range(3):
+        assert np.array_equal(got[k], want[k])
+    with pytest.raises(NotImplementedError):
+        kh.Simulation(cell_size=(1.8, 1.2, 1.2), resolution=10, geometry=objs, boundaries=bnd,
+                      subpixel_smoothing="volume").spec()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_dispersive_objects_match_oracle(kh, oracle, gpu_lib, dtype):
+    from khronos_gb300.geometry import Ball, Material, Object
+    from test_gpu_parity import TOL, compare
+
+    lor = kh.LorentzianSusceptibility(1.0, 0.05, 1.0)
+    dru = kh.DrudeSusceptibility(0.1, 5.0)
+    objs = [Object(Ball((0.25, 0.0, 0.0), 0.3), Material(eps=2.0, susceptibilities=(lor,))),
+            Object(Ball((-0.3, 0.05, 0.0), 0.25), Material(eps=1.0, susceptibilities=(dru,), chi3=0.01))]
+    src = kh.UniformSource(time_profile=kh.GaussianPulseSource(fcen=0.9, fwidth=0.4), component=kh.EZ,
+                           center=(0.0, -0.35, 0.0), size=(0.5, 0.0, 0.4), amplitude=2.0)
+    sim = kh.Simulation(cell_size=(1.9, 1.6, 1.4), resolution=10, sources=[src], geometry=objs,
+                        boundaries=[[0.3, 0.3]] * 3, dtype=dtype)
+    compare(sim.spec(), 100, oracle, gpu_lib, TOL[dtype], check_dft=False)
