@@ -100,6 +100,16 @@ typedef struct {
   double eps_inv;      /* scalar ε⁻¹ used where no per-voxel array is set (1) */
   double mu_inv;       /* scalar μ⁻¹ (1)                                       */
   int32_t semantics;   /* KH_SEM_*: which of the reference's CPML paths to follow */
+  /* Bit a set: axis a is periodic (Periodic, or Bloch with k = 0).  After each
+   * half-step the updated field's last interior layer along a is copied into
+   * the ghost layer below the first, and the first into the layer above the
+   * last, over the Center range of the other axes (_add_periodic_connections!
+   * single-chunk branch, Chunking.jl:1751-1768; _exchange_halos_local!,
+   * Chunking.jl:2138-2172).  The E copy is taken before the χ3 correction:
+   * exchange_halos!(:E) ends step_E_fused! (Kernels.jl:452), which step!
+   * calls before step_chi3_correction! (Kernels.jl:76-79).  0 = zero ghost
+   * walls on every side. */
+  int32_t periodic;
 } kh_sim_desc;
 
 /* CPML stage semantics.

@@ -42,6 +42,7 @@ class SimDesc(C.Structure):
         ("eps_inv", C.c_double),
         ("mu_inv", C.c_double),
         ("semantics", C.c_int32),
+        ("periodic", C.c_int32),
     ]
 
 

@@ -64,6 +64,29 @@ __device__ __forceinline__ void vst_at(T* base, long long q, long long n, int si
   if (KH_IN(q, n, site) && KH_IN(q + VN - 1, n, site)) vst(base + q, v);
 }
 
+// E of a χ3 cell before its Kerr correction, into the ghost layers that the
+// periodic wrap fills from this cell: the reference exchanges E halos at the
+// end of step_E_fused! (Kernels.jl:452), before step_chi3_correction!.
+template <typename T>
+__device__ __forceinline__ void wrap_pre_chi3(const HalfStepParams<T>& p, long long q, int i, int j, int k,
+                                              const T (&O)[3]) {
+  const int co[3] = {i, j, k};
+  const int na[3] = {p.nx, p.ny, p.nz};
+  const long long st[3] = {1, p.pitch, p.plane};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    if (!((p.periodic >> a) & 1u)) continue;
+    const long long to[2] = {co[a] == na[a] - 1 ? q - (long long)na[a] * st[a] : -1,
+                             co[a] == 0 ? q + (long long)na[a] * st[a] : -1};
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      if (to[s] < 0 || !KH_IN(to[s], p.total, 1008)) continue;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) p.O[c][to[s]] = O[c];
+    }
+  }
+}
+
 // Update of one cell that carries a source, χ3, a pole or a material
 // conductivity (and may also sit in a CPML region).  t/u/w are the cell's B|D
 // state and CPML U/W values (loaded and stored by the caller), m its μ⁻¹|ε⁻¹,
@@ -192,6 +215,7 @@ __device__ __forceinline__ void general_cell(const HalfStepParams<T>& p, long lo
   if constexpr (!H) {
     // χ3 Kerr correction (Dispersive.jl:127-147)
     if ((cls & kHasChi3) && c3 != T(0)) {
+      if (p.periodic) wrap_pre_chi3(p, q, i, j, k, O);
       const T esq = (O[0] * O[0] + O[1] * O[1]) + O[2] * O[2];
       const T corr = T(1) / (T(1) + c3 * esq);
       O[0] = O[0] * corr;

@@ -26,6 +26,8 @@
 //    CPML auxiliaries their region allocates (Chunking.jl:1069-1146).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "kh_cell.cuh"
 
 namespace kh {
@@ -365,6 +367,41 @@ void launch_source_fix(const SourceFixParams<T>& p, void* stream) {
 }
 
 // ---------------------------------------------------------------------------
+// Periodic wrap.  blockIdx.y = 3·axis + component; threads stride over the
+// face's (n_t1 × n_t2) cells; each copies both directions of one cell.
+template <typename T>
+__global__ void wrap_kernel(const WrapParams<T> p) {
+  const int a = blockIdx.y / 3, c = blockIdx.y % 3;
+  if (!((p.periodic >> a) & 1u)) return;
+  const int t1 = (a + 1) % 3, t2 = (a + 2) % 3;
+  const long long st[3] = {1, p.pitch, p.plane};
+  const long long face = (long long)p.n[t1] * p.n[t2];
+  T* f = p.O[c];
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < face;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long u = e % p.n[t1], v = e / p.n[t1];
+    const long long base = p.origin + u * st[t1] + v * st[t2];
+    const long long lo = base, hi = base + (long long)(p.n[a] - 1) * st[a];
+    const long long ghost_lo = base - st[a], ghost_hi = base + (long long)p.n[a] * st[a];
+    if (!(KH_IN(ghost_lo, p.total, 3028) && KH_IN(ghost_hi, p.total, 3029))) continue;
+    if (!(p.chi3 && p.chi3[hi] != T(0))) f[ghost_lo] = f[hi];
+    if (!(p.chi3 && p.chi3[lo] != T(0))) f[ghost_hi] = f[lo];
+  }
+}
+
+template <typename T>
+void launch_wrap(const WrapParams<T>& p, void* stream) {
+  if (!p.periodic) return;
+  long long face = 0;
+  for (int a = 0; a < 3; ++a)
+    if ((p.periodic >> a) & 1u) face = std::max(face, (long long)p.n[(a + 1) % 3] * p.n[(a + 2) % 3]);
+  const int threads = 256;
+  const long long blocks = std::min<long long>((face + threads - 1) / threads, 1024);
+  wrap_kernel<T><<<dim3(unsigned(std::max<long long>(blocks, 1)), 9), threads, 0,
+                   static_cast<cudaStream_t>(stream)>>>(p);
+}
+
+// ---------------------------------------------------------------------------
 // DFT accumulation (update_dft_monitor!, Monitors.jl:361-379):
 //   F[cell, f] += Δt·exp(i2πf t)·field[cell]
 // FP32 accumulators carry a Kahan compensation term.
@@ -539,6 +576,8 @@ void launch_flux(const Cplx<T>* e1, const Cplx<T>* e2, const Cplx<T>* h1, const 
 
 template void launch_half_step<float>(bool, const HalfStepParams<float>&, void*);
 template void launch_half_step<double>(bool, const HalfStepParams<double>&, void*);
+template void launch_wrap<float>(const WrapParams<float>&, void*);
+template void launch_wrap<double>(const WrapParams<double>&, void*);
 template void launch_source_fix<float>(const SourceFixParams<float>&, void*);
 template void launch_source_fix<double>(const SourceFixParams<double>&, void*);
 template void launch_record<float>(const RecordParams<float>&, void*);

@@ -161,6 +161,11 @@ struct HalfStepParams {
   int npoles;
   PoleParams<T> poles[kMaxPoles];
 
+  // bit a set: axis a is periodic.  E half: a χ3 cell on a wrap face stores
+  // its pre-correction E into the ghost layer the wrap fills (the reference
+  // exchanges E before the Kerr correction); the wrap kernel skips those cells.
+  uint32_t periodic;
+
   int* err;  // set to KH_ERR_TIMEOUT by a kernel whose bounded wait gave up
   // Failure-detection test hook (0 in normal runs): nonzero launches the FP32
   // LEAN TMA kernels' test instantiation, whose first ring stage expects 16
@@ -286,8 +291,24 @@ struct SourceFixParams {
   int h_half;
 };
 
+// Periodic wrap of one field group after its half-step (_exchange_halos_local!
+// single-chunk connections, Chunking.jl:1751-1768, 2138-2172): for each axis a
+// in `periodic` and each component, layer n_a-1 → ghost layer -1 and layer 0 →
+// layer n_a, over the Center range 0..n-1 of the other two axes.
+template <typename T>
+struct WrapParams {
+  int n[3];
+  long long pitch, plane, origin, total;
+  uint32_t periodic;
+  T* O[3];
+  const T* chi3;  // E group: cells with χ3 ≠ 0 already stored their pre-correction value
+};
+
 template <typename T>
 void launch_half_step(bool h_half, const HalfStepParams<T>& p, void* stream);
+
+template <typename T>
+void launch_wrap(const WrapParams<T>& p, void* stream);
 
 template <typename T>
 void launch_source_fix(const SourceFixParams<T>& p, void* stream);

@@ -380,6 +380,8 @@ class Sim : public SimBase {
 
     if (d_.semantics != KH_SEM_REFERENCE_CPU && d_.semantics != KH_SEM_CPML)
       return fail(KH_ERR_INVALID, "unknown CPML semantics");
+    if (d_.periodic & ~7)
+      return fail(KH_ERR_INVALID, "periodic is a mask of axes 0..2");
     // Regions with material conductivity (PhysicsFlags.has_sigma_{B,D}).
     sigmask_b_ = region_mask(msigb_h_);
     sigmask_d_ = region_mask(msigd_h_);
@@ -1347,6 +1349,7 @@ class Sim : public SimBase {
     const bool full_h_base = msb || (ref_cpu && special_in_region_[1]);
     const bool full_e_base = msd || chi3_ != nullptr || !poles_d_.empty() || (ref_cpu && special_in_region_[0]);
     kh::SourceFixParams<T> fh = fix_params(true), fe = fix_params(false);
+    const kh::WrapParams<T> wh = wrap_params(true), we = wrap_params(false);
     auto issue_all = [&](cudaStream_t st) {
     for (int s = 0; s < nb; ++s) {
       const StepPlan& P = plan[s];
@@ -1363,6 +1366,10 @@ class Sim : public SimBase {
         kh::launch_source_fix<T>(fh, st);
         ++launches;
       }
+      if (d_.periodic) {
+        kh::launch_wrap<T>(wh, st);
+        ++launches;
+      }
       mark(s, 1);
       for (auto& dm : P.dftH) launch_dft_for(dm.first, dtab + dm.second, st);
       record_histories(true, timestep_ + s, st);
@@ -1377,6 +1384,10 @@ class Sim : public SimBase {
       if (src_e && !pe.full) {
         fe.f_now = dtab + P.fE;
         kh::launch_source_fix<T>(fe, st);
+        ++launches;
+      }
+      if (d_.periodic) {
+        kh::launch_wrap<T>(we, st);
         ++launches;
       }
       mark(s, 3);
@@ -1649,6 +1660,20 @@ class Sim : public SimBase {
     return f;
   }
 
+  kh::WrapParams<T> wrap_params(bool h) const {
+    kh::WrapParams<T> w;
+    std::memset(&w, 0, sizeof(w));
+    for (int a = 0; a < 3; ++a) w.n[a] = n_[a];
+    w.pitch = pitch_;
+    w.plane = plane_;
+    w.origin = origin_;
+    w.total = total_;
+    w.periodic = uint32_t(d_.periodic);
+    for (int c = 0; c < 3; ++c) w.O[c] = h ? H_[c] : E_[c];
+    w.chi3 = h ? nullptr : chi3_;
+    return w;
+  }
+
   kh::HalfStepParams<T> base_params(bool h) const {
     kh::HalfStepParams<T> p;
     std::memset(&p, 0, sizeof(p));
@@ -1690,6 +1715,7 @@ class Sim : public SimBase {
     p.cell_class = cls_;
     p.err = err_dev_;
     p.stall_tx = stall_tx_;
+    p.periodic = h ? 0u : uint32_t(d_.periodic);
     p.slot_off = slot_off_;
     p.ent_src = ent_src_;
     p.ent_comp = ent_comp_;

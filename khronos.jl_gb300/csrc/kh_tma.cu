@@ -376,6 +376,7 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
                 Oc[cc] = mc[cc] * tc[cc];
               }
               if (cur.c3[v] != T(0)) {
+                if (p.periodic) wrap_pre_chi3(p, q + v, i, j, k, Oc);
                 const T esq = (Oc[0] * Oc[0] + Oc[1] * Oc[1]) + Oc[2] * Oc[2];
                 const T corr = T(1) / (T(1) + cur.c3[v] * esq);
 #pragma unroll

@@ -40,6 +40,7 @@ class GpuSim:
         d.eps_inv = float(spec.eps_inv)
         d.mu_inv = float(spec.mu_inv)
         d.semantics = int(spec.semantics)
+        d.periodic = int(spec.periodic)
         self._check(self.lib.kh_sim_create(C.byref(d), C.byref(self.handle)))
         try:
             for kind, comp, arr in spec.materials:

@@ -39,7 +39,8 @@ class Simulation:
     ``boundary_conditions`` ([[lo, hi]] per axis of ``boundaries.PECBoundary``,
     ``PMCBoundary``, ...) zeroes the PML conductivity on those sides while the
     PML regions keep following ``boundaries``, as the reference's prepare
-    does; periodic and Bloch sides are refused.
+    does; an axis with Periodic (or Bloch with k = 0) on both sides wraps its
+    fields' halo after every half-step.
 
     Materials (all optional; arrays are (Nx, Ny, Nz), cell-indexed):
       geometry: list of geometry.Object (Ball / Cuboid / Cylinder with an
@@ -60,10 +61,11 @@ class Simulation:
         self.dtype = dtype
         self.sources = list(sources)
         self.boundaries = boundaries
-        from .boundaries import effective_pml
+        from .boundaries import effective_pml, periodic_mask
 
         self.boundary_conditions = boundary_conditions
         self._sigma_boundaries = effective_pml(boundaries, boundary_conditions)
+        self._periodic = periodic_mask(boundary_conditions)
         self.monitors = list(monitors)
         self.eps_inv = eps_inv
         self.mu_inv = mu_inv
@@ -112,7 +114,8 @@ class Simulation:
         T = g.T
         sp = SimSpec(n=g.n, dtype=KH_F32 if T is np.float32 else KH_F64,
                      delta=tuple(float(d) for d in g.delta), dt=float(g.dt),
-                     semantics=SEM_CPML if self.semantics == "cpml" else SEM_REFERENCE_CPU)
+                     semantics=SEM_CPML if self.semantics == "cpml" else SEM_REFERENCE_CPU,
+                     periodic=self._periodic)
         if self.boundaries is not None:
             lo, hi = G.pml_widths(g, self.boundaries)
             sp.pml_lo, sp.pml_hi = lo, hi

@@ -113,6 +113,7 @@ class SimSpec:
     eps_inv: float = 1.0
     mu_inv: float = 1.0
     semantics: int = 1   # SEM_CPML (stable, the reference's CUDA-path CPML); 0 = CPU path
+    periodic: int = 0    # bit a: axis a wraps its halo (Periodic / Bloch with k = 0)
     materials: List[Tuple[int, int, np.ndarray]] = field(default_factory=list)  # (kind, comp, array)
     poles: List[PoleSpec] = field(default_factory=list)
     sources: List[SourceSpec] = field(default_factory=list)

@@ -25,6 +25,7 @@
 //   DFT monitors               src/Monitors/Monitors.jl:274-379
 //   χ3 correction              src/Kernels/Dispersive.jl:127-173
 //   ADE poles                  src/Kernels/Dispersive.jl:25-117, 186-228
+//   periodic halo wrap         src/Chunking.jl:1751-1768, 2138-2172 (single chunk)
 // Field arrays are one global domain; the reference's multi-chunk halo
 // exchange (Chunking.jl:2082-2214) copies exactly the neighbour values a
 // single domain reads, so per-region loops over global arrays reproduce it.
@@ -277,10 +278,12 @@ class Oracle {
     const bool sa = sources_active;
     if (sa) inject(true, t);
     half_step(true, sa);
+    exchange_periodic(true);  // exchange_halos!(:H) ends step_H_fused! (Kernels.jl:294)
     update_monitors(true, t);
     const double tE = t + double(dt / T(2));
     if (sa) inject(false, tE);
     half_step(false, sa);
+    exchange_periodic(false);  // exchange_halos!(:E) ends step_E_fused! (Kernels.jl:452)
     chi3_correction();
     polarization();
     update_monitors(false, tE);
@@ -351,6 +354,32 @@ class Oracle {
             if (g[c].g(ix, iy, iz) != T(0)) return true;
     }
     return false;
+  }
+
+  // Single-chunk periodic connections (_add_periodic_connections!,
+  // Chunking.jl:1751-1768) as _exchange_halos_local! copies them
+  // (Chunking.jl:2138-2172): per periodic axis and component, Julia layer N
+  // → ghost 0 and layer 1 → layer N+1, over the Center range 1..N of the
+  // other axes (_component_send_range / _component_recv_range clamp it to
+  // the component, which it never exceeds).
+  void exchange_periodic(bool h) {
+    if (!desc.periodic) return;
+    for (int a = 0; a < 3; ++a) {
+      if (!((desc.periodic >> a) & 1)) continue;
+      const int t1 = (a + 1) % 3, t2 = (a + 2) % 3;
+      for (int c = 0; c < 3; ++c) {
+        Field3<T>& F = h ? H[c] : E[c];
+        for (int v = 2; v <= n[t2] + 1; ++v)
+          for (int u = 2; u <= n[t1] + 1; ++u) {
+            int g_lo[3], s_hi[3], g_hi[3], s_lo[3];
+            g_lo[t1] = s_hi[t1] = g_hi[t1] = s_lo[t1] = u;
+            g_lo[t2] = s_hi[t2] = g_hi[t2] = s_lo[t2] = v;
+            g_lo[a] = 1; s_hi[a] = n[a] + 1; g_hi[a] = n[a] + 2; s_lo[a] = 2;
+            F.r(g_lo[0], g_lo[1], g_lo[2]) = F.r(s_hi[0], s_hi[1], s_hi[2]);
+            F.r(g_hi[0], g_hi[1], g_hi[2]) = F.r(s_lo[0], s_lo[1], s_lo[2]);
+          }
+      }
+    }
   }
 
   const Field3<T>& src_field(bool h, int c) const { return h ? E[c] : H[c]; }

@@ -98,6 +98,7 @@ class OracleSim:
         d.eps_inv = float(spec.eps_inv)
         d.mu_inv = float(spec.mu_inv)
         d.semantics = int(spec.semantics)
+        d.periodic = int(spec.periodic)
         self.h = C.c_void_p(self.lib.khref_create(C.byref(d)))
         if not self.h:
             raise RuntimeError("oracle create failed")

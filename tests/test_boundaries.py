@@ -1,6 +1,8 @@
 """Boundary conditions (DataStructures.jl:157-162, Boundaries.jl:99-164): a
 PEC or PMC side keeps the PML region its ``boundaries`` thickness gives but
-with zero conductivity; periodic and Bloch sides are refused (no halo wrap)."""
+with zero conductivity; so does a Periodic or Bloch side, whose halo wrap
+(tests/test_periodic.py) needs both sides of the axis; a Bloch phase k ≠ 0
+is refused (complex fields)."""
 import numpy as np
 import pytest
 
@@ -31,10 +33,14 @@ def test_pec_pmc_sides_zero_sigma_keep_regions(kh):
 
 
 @pytest.mark.parametrize("bc", ["Periodic", "Bloch"])
-def test_periodic_and_bloch_refused(kh, bc):
+def test_periodic_and_bloch_sides(kh, bc):
     cond = getattr(kh, bc)()
+    sp = _sim(kh, bcs=[[cond, cond], [None, None], [None, None]]).spec()
+    assert sp.periodic == 1 and np.all(sp.sigma_b[0] == 0) and sp.pml_lo[0] > 0
+    one = _sim(kh, bcs=[[cond, None], [None, None], [None, None]]).spec()
+    assert one.periodic == 0 and np.all(one.sigma_b[0][:one.pml_lo[0]] == 0)
     with pytest.raises(NotImplementedError):
-        _sim(kh, bcs=[[cond, cond], [None, None], [None, None]])
+        _sim(kh, bcs=[[kh.Bloch(k=0.5), kh.Bloch(k=0.5)], [None, None], [None, None]])
 
 
 @pytest.mark.gpu
