@@ -31,9 +31,12 @@ def _slab_sim(kh, semantics="cpml", dtype="f64", src_center_x=0.0, src_size_x=ma
     bcs = [[kh.Periodic(), kh.Periodic()] if a in periodic else [None, None] for a in range(3)]
     src = kh.UniformSource(time_profile=_pulse(kh), component=kh.EX,
                            center=(src_center_x, 0.11, -0.3), size=(src_size_x, 0.5, 0))
-    mons = [kh.DFTMonitor(component=kh.EX, center=(0, 0, 0.35), size=(math.inf, math.inf, 0),
+    # monitors on the wrap faces: the first reaches layer n along x in FP32
+    # (a full-span box there reads one layer past the component in FP32 and is
+    # refused by the device)
+    mons = [kh.DFTMonitor(component=kh.EX, center=(0.15, 0.1, 0.35), size=(1.0, 0.9, 0),
                           frequencies=[0.7, 0.8]),
-            kh.DFTMonitor(component=kh.HY, center=(0, 0, 0.2), size=(math.inf, 0.6, 0), frequencies=[0.8],
+            kh.DFTMonitor(component=kh.HY, center=(-0.15, 0, 0.2), size=(1.0, 0.6, 0), frequencies=[0.8],
                           decimation=2)]
     return kh.Simulation(cell_size=(1.3, 1.1, 2.3), resolution=res, sources=[src], monitors=mons,
                          boundaries=bnd, boundary_conditions=bcs, dtype=dtype, semantics=semantics, **kw)
