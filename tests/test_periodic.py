@@ -209,3 +209,32 @@ def test_periodic_bounds_checked(kh, gpu_lib):
     blib = _abi.load(build.build(bounds=True))
     _same(_kerr_sim(kh, "f64").spec(), gpu_lib, blib, chunks=(5, 17))
     _same(_slab_sim(kh, "cpml", "f32", periodic=(0, 1, 2)).spec(), gpu_lib, blib, chunks=(5, 17))
+
+
+@pytest.mark.gpu
+def test_periodic_requests_in_server_mix(kh, gpu_lib):
+    """Periodic and zero-wall requests served together: each matches its solo
+    run bit for bit (the wrap launches ride in each request's own step loop)."""
+    from khronos_gb300.device import GpuSim
+    from khronos_gb300.serve import Server
+
+    specs = [_slab_sim(kh, "cpml", "f32", periodic=p, src_center_x=0.07, src_size_x=0.6).spec()
+             for p in ((0, 1), (), (0, 1, 2), (2,))]
+    specs.append(_kerr_sim(kh, "f32", "cpml").spec())
+    steps = [90, 70, 110, 50, 60]
+    solo = []
+    for sp, n in zip(specs, steps):
+        g = GpuSim(sp, lib=gpu_lib)
+        g.step(n)
+        solo.append([g.dft(m) for m in range(len(sp.monitors))] + [g.field(c) for c in range(6)])
+        g.close()
+    with Server(budget_bytes=4 << 30, max_resident=3, quantum_steps=16, lib=gpu_lib) as srv:
+        reqs = [srv.submit(sp, n) for sp, n in zip(specs, steps)]
+        for _ in reqs:
+            r = srv.next_done(timeout=120)
+            assert r is not None and r.wait()
+            i = reqs.index(r)
+            got = [r.sim.dft(m) for m in range(len(specs[i].monitors))] + [r.sim.field(c) for c in range(6)]
+            for a, b in zip(got, solo[i]):
+                np.testing.assert_array_equal(a, b)
+            r.release()
