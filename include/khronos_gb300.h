@@ -173,6 +173,11 @@ typedef struct {
 
 /* Library and device information. */
 const char* kh_version(void);
+/* Device allocations the library has made in this process, over all devices
+ * (each request to its stream-ordered memory pool counts one).  Diagnostic
+ * with no counterpart in the reference: lets a caller check that a call
+ * allocates nothing. */
+kh_status kh_device_alloc_count(int64_t* out);
 kh_status kh_device_info(int32_t* sm_count, int32_t* cc_major, int32_t* cc_minor);
 
 /* Lifecycle. */
@@ -266,7 +271,10 @@ kh_status kh_sim_flux(kh_sim* sim, const int32_t ids[4], int32_t normal_axis, do
  * at most 4096 frequencies (more returns KH_ERR_INVALID; use kh_sim_flux).
  * The first call on each device does a one-time set-up (it resolves that
  * array's device address with the device current); make it before any
- * stream capture begins.  The array is shared by all simulations of the
+ * stream capture begins.  The resolved address is kept for the life of the
+ * process: it does not survive cudaDeviceReset (or any other teardown of the
+ * device's primary context), after which this entry point must not be used
+ * on that device.  kh_device_alloc_count shows that it allocates nothing.  The array is shared by all simulations of the
  * process on a device and keeps the last call's values: calls that overlap
  * on one device (from several host threads) race on it, so serialise them.
  * Same result as kh_sim_flux. */

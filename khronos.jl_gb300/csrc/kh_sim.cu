@@ -77,7 +77,10 @@ using kh_host::SimBase;
 
 namespace kh_host {
 
+std::atomic<int64_t> g_alloc_count{0};
+
 cudaError_t dev_alloc(void** p, size_t bytes, cudaStream_t s) {
+  ++g_alloc_count;
   static std::mutex mu;
   static cudaMemPool_t pools[kMaxDevices] = {};
   int dev = 0;
@@ -1819,6 +1822,12 @@ class Sim : public SimBase {
 extern "C" {
 
 const char* kh_version(void) { return kVersion; }
+
+kh_status kh_device_alloc_count(int64_t* out) {
+  if (!out) return KH_ERR_INVALID;
+  *out = kh_host::g_alloc_count.load();
+  return KH_OK;
+}
 
 kh_status kh_device_info(int32_t* sm_count, int32_t* cc_major, int32_t* cc_minor) {
   int dev = 0;

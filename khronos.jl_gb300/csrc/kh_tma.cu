@@ -185,8 +185,14 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
     T* dst = stages + st * G::STAGE;
     const int plane = H ? k0 + n : k0 - 1 + n;
     const bool comp = H ? (n < N) : (n >= 1);
-    // (STALL: failure-detection test instantiation, 16 bytes that never arrive)
-    mbar_arrive_expect_tx(&bars[st], a_bytes + (comp ? o_bytes : 0u) + (STALL && n == 0 ? 16u : 0u));
+    if (STALL && n == 0) {
+      // failure-detection test instantiation: the first stage expects 16
+      // bytes and no copy is issued into it, so the wait on it runs out and
+      // nothing is left in flight when the CTA returns
+      mbar_arrive_expect_tx(&bars[st], 16u);
+      return;
+    }
+    mbar_arrive_expect_tx(&bars[st], a_bytes + (comp ? o_bytes : 0u));
     const int zc = plane + 1;                      // padded plane index
     const int ax = H ? G::HX + x_tile : x_tile;    // padded x of the A box
     const int ay = H ? 1 + y_tile : y_tile;        // padded y of the A box

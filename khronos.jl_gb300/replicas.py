@@ -1,9 +1,9 @@
 """Replicas across GPUs: independent simulations per rank, no domain decomposition.
 
 The step loop runs on one GPU with no halo exchange (the reference shards one
-grid into chunks and exchanges halos over NCCL, src/Parallel/Distributed.jl:
-448-506; that decomposition is not rebuilt).  Several GPUs serve independent
-work: each rank (one process per GPU, launched by torchrun) steps its own
+grid into chunks and exchanges halos over NCCL, src/Distributed.jl:448-506;
+that decomposition is not rebuilt).  Several GPUs serve independent work:
+each rank (one process per GPU, launched by torchrun) steps its own
 simulations, and the only collective is on the host side of a measurement —
 a barrier around the timed region and the maximum of the ranks' times.
 

@@ -16,13 +16,17 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "libkhronos_oracle.so"
+# The same restatement built with FMA contraction: the timed CPU baseline only
+# (its last-bit rounding differs, so parity checks use LIB).
+LIB_TIMED = HERE / "libkhronos_oracle_timed.so"
 
 COMPONENT_EXTRA = {0: (0, 1, 1), 1: (1, 0, 1), 2: (1, 1, 0), 3: (1, 0, 0), 4: (0, 1, 0), 5: (0, 0, 1)}
 
 
 def build(force: bool = False) -> Path:
     src = HERE / "khronos_oracle.cpp"
-    if force or not LIB.exists() or LIB.stat().st_mtime < src.stat().st_mtime:
+    stale = any(not p.exists() or p.stat().st_mtime < src.stat().st_mtime for p in (LIB, LIB_TIMED))
+    if force or stale:
         r = subprocess.run(["make", "-C", str(HERE), "-B" if force else "all"], capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
@@ -30,35 +34,46 @@ def build(force: bool = False) -> Path:
 
 
 _lib = None
+_lib_timed = None
 
 
-def load():
-    global _lib
+def load(timed: bool = False):
+    """The parity build, or (timed=True) the FMA-contracted build used only
+    for the timed CPU baseline."""
+    global _lib, _lib_timed
+    if timed:
+        if _lib_timed is None:
+            build()
+            _lib_timed = _declare(C.CDLL(str(LIB_TIMED)))
+        return _lib_timed
     if _lib is None:
         build()
-        lib = C.CDLL(str(LIB))
-        vp = C.c_void_p
-        pd = C.POINTER(C.c_double)
-        pi = C.POINTER(C.c_int32)
-        lib.khref_create.restype = vp
-        lib.khref_create.argtypes = [vp]
-        lib.khref_destroy.argtypes = [vp]
-        lib.khref_last_error.restype = C.c_char_p
-        lib.khref_last_error.argtypes = [vp]
-        lib.khref_set_material.argtypes = [vp, C.c_int, C.c_int, pd]
-        lib.khref_add_pole.argtypes = [vp, vp, pd]
-        lib.khref_add_source.argtypes = [vp, vp]
-        lib.khref_add_dft_monitor.argtypes = [vp, C.c_int, pi, pi, C.c_int, pd, C.c_int, pi]
-        lib.khref_prepare.argtypes = [vp]
-        lib.khref_step.argtypes = [vp, C.c_int64]
-        lib.khref_timestep.restype = C.c_int64
-        lib.khref_timestep.argtypes = [vp]
-        lib.khref_sources_active.argtypes = [vp]
-        lib.khref_get_field.argtypes = [vp, C.c_int, pd]
-        lib.khref_read_dft.argtypes = [vp, C.c_int, pd]
-        lib.khref_num_threads.restype = C.c_int
-        _lib = lib
+        _lib = _declare(C.CDLL(str(LIB)))
     return _lib
+
+
+def _declare(lib):
+    vp = C.c_void_p
+    pd = C.POINTER(C.c_double)
+    pi = C.POINTER(C.c_int32)
+    lib.khref_create.restype = vp
+    lib.khref_create.argtypes = [vp]
+    lib.khref_destroy.argtypes = [vp]
+    lib.khref_last_error.restype = C.c_char_p
+    lib.khref_last_error.argtypes = [vp]
+    lib.khref_set_material.argtypes = [vp, C.c_int, C.c_int, pd]
+    lib.khref_add_pole.argtypes = [vp, vp, pd]
+    lib.khref_add_source.argtypes = [vp, vp]
+    lib.khref_add_dft_monitor.argtypes = [vp, C.c_int, pi, pi, C.c_int, pd, C.c_int, pi]
+    lib.khref_prepare.argtypes = [vp]
+    lib.khref_step.argtypes = [vp, C.c_int64]
+    lib.khref_timestep.restype = C.c_int64
+    lib.khref_timestep.argtypes = [vp]
+    lib.khref_sources_active.argtypes = [vp]
+    lib.khref_get_field.argtypes = [vp, C.c_int, pd]
+    lib.khref_read_dft.argtypes = [vp, C.c_int, pd]
+    lib.khref_num_threads.restype = C.c_int
+    return lib
 
 
 def num_threads() -> int:
@@ -72,14 +87,14 @@ def _dptr(a):
 class OracleSim:
     """CPU oracle run of one SimSpec."""
 
-    def __init__(self, spec):
+    def __init__(self, spec, timed: bool = False):
         import importlib
 
         abi = importlib.import_module("khronos_gb300._abi")
         from khronos_gb300.spec import flat_complex, flat_f
 
         self.spec = spec
-        self.lib = load()
+        self.lib = load(timed)
         keep = []
         d = abi.SimDesc()
         for a in range(3):

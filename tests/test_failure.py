@@ -2,8 +2,8 @@
 TMA half-step kernels is bounded, and a kernel that gives up records
 KH_ERR_TIMEOUT for the host instead of hanging.  The test makes the wait run
 out through a test hook (KHRONOS_GB300_TEST_STALL=1: the first ring stage of
-each CTA expects 16 bytes that never arrive, and the limit drops to 4096
-polls); the status reaches kh_sim_synchronize, the kernels return, and the
+each CTA expects 16 bytes, no copy is issued into it, and the limit drops to
+4096 polls); the status reaches kh_sim_synchronize, the kernels return, and the
 context stays usable for the next simulation."""
 import numpy as np
 import pytest

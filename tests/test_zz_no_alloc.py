@@ -59,6 +59,33 @@ def test_flux_static_matches_flux(kh, gpu_lib, dtype):
 
 
 @pytest.mark.gpu
+def test_flux_static_allocates_nothing(kh, gpu_lib):
+    """The library's device-allocation counter does not move across repeated
+    kh_sim_flux_static calls (and does move for kh_sim_flux, so it counts)."""
+    from khronos_gb300 import configs
+    from khronos_gb300.device import GpuSim
+
+    def count():
+        v = C.c_int64()
+        assert gpu_lib.kh_device_alloc_count(C.byref(v)) == 0
+        return v.value
+
+    w = configs.waveguide(dtype="f32", scale=0.25)
+    gpu = GpuSim(w.sim.spec(), lib=gpu_lib)
+    gpu.step(100)
+    fm = w.flux_monitors[0]
+    _flux_static(gpu, [0, 1, 2, 3], fm.normal_axis, fm.dA)  # first call on the device: set-up
+    n0 = count()
+    for _ in range(5):
+        st, _ = _flux_static(gpu, [0, 1, 2, 3], fm.normal_axis, fm.dA)
+        assert st == 0
+    assert count() == n0
+    gpu.flux([0, 1, 2, 3], fm.normal_axis, fm.dA)
+    assert count() > n0
+    gpu.close()
+
+
+@pytest.mark.gpu
 def test_flux_static_shared_between_simulations(kh, gpu_lib):
     """A call with fewer frequencies after one with more, from another
     simulation, reads only its own sums."""
