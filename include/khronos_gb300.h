@@ -187,6 +187,18 @@ const char* kh_last_error(const kh_sim* sim);
 
 /* Set-up (before kh_sim_prepare). */
 kh_status kh_sim_set_material(kh_sim* sim, int32_t kind, int32_t comp, const double* values);
+/* kh_sim_set_material for an array in its own precision (dtype KH_F32 or
+ * KH_F64), the way GeometryData holds ε_inv_x … σD in the run's type T
+ * (src/DataStructures.jl:214-242), so a Float32 run hands its arrays over
+ * without a conversion pass.  Same layout (Center range, x fastest).
+ * KH_MAT_EPS_INV and KH_MAT_MU_INV are not copied here: the library reads
+ * `values` during kh_sim_prepare, with one host-to-device copy straight from
+ * it (a DMA when the array is pinned) and the conversion, if the precisions
+ * differ, on the device; the caller keeps the array valid and unchanged until
+ * kh_sim_prepare returns (for a simulation handed to kh_server_submit: until
+ * the request has been prepared).  The other kinds are classified on the host
+ * and are copied before this call returns. */
+kh_status kh_sim_attach_material(kh_sim* sim, int32_t kind, int32_t comp, const void* values, int32_t dtype);
 kh_status kh_sim_add_pole(kh_sim* sim, const kh_pole_coeffs* coeffs, const double* sigma);
 kh_status kh_sim_add_source(kh_sim* sim, const kh_source_desc* src);
 kh_status kh_sim_add_dft_monitor(kh_sim* sim, int32_t component, const int32_t start[3],

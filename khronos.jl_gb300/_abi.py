@@ -121,6 +121,7 @@ SIGNATURES = {
     "kh_sim_destroy": (None, [C.c_void_p]),
     "kh_last_error": (C.c_char_p, [C.c_void_p]),
     "kh_sim_set_material": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_double)]),
+    "kh_sim_attach_material": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int32]),
     "kh_device_alloc_count": (C.c_int32, [C.POINTER(C.c_int64)]),
     "kh_sim_add_pole": (C.c_int32, [C.c_void_p, C.POINTER(PoleCoeffs), C.POINTER(C.c_double)]),
     "kh_sim_add_source": (C.c_int32, [C.c_void_p, C.POINTER(SourceDesc)]),

@@ -22,7 +22,8 @@ LIB = PKG / "libkhronos_gb300.so"
 # tested against its array's extent, violations recorded for kh_debug_bounds.
 BUILD_BOUNDS = ROOT / "_build" / "khronos_gb300_bounds"
 LIB_BOUNDS = PKG / "libkhronos_gb300_bounds.so"
-SOURCES = ["kh_kernels.cu", "kh_tma.cu", "kh_sim.cu", "kh_serve.cu", "kh_adjoint.cu", "kh_geometry.cu"]
+SOURCES = ["kh_kernels.cu", "kh_tma.cu", "kh_sim.cu", "kh_serve.cu", "kh_adjoint.cu", "kh_geometry.cu",
+           "kh_setup.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # The geometry set-up decides inside/outside at points that can sit exactly on
 # an object's boundary: its double arithmetic is kept unfused so each

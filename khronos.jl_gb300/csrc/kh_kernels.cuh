@@ -316,6 +316,46 @@ void launch_source_fix(const SourceFixParams<T>& p, void* stream);
 template <typename T>
 void launch_dft(const DftParams<T>& p, void* stream);
 
+// ---- set-up kernels (kh_setup.cu) ----
+// Compact Center-range array (x fastest) → padded layout, converted to T.
+template <typename Tin, typename T>
+void launch_scatter_center(const Tin* src, T* dst, const int n[3], long long pitch, long long plane,
+                           long long origin, void* stream);
+
+// Cell classes of χ3 and pole cells (ORed into cls) from the device arrays.
+template <typename T>
+struct ClassifyArgs {
+  int n[3];
+  long long pitch, plane, origin;
+  const T* chi3;                     // nullptr if no χ3 array
+  int npoles;
+  const T* pole_sigma[kMaxPoles];
+  uint32_t* cls;
+};
+template <typename T>
+void launch_classify(const ClassifyArgs<T>& a, void* stream);
+
+// cls[cell[s]] |= bits[s] for s < n (source cells: class bits and slot index).
+void launch_mark_cells(const long long* cell, const uint32_t* bits, int n, uint32_t* cls, void* stream);
+
+// Plane bitmasks of special cells per row segment, and CPML-region flags.
+struct TileBitsArgs {
+  int n[3];
+  long long pitch, plane, origin;
+  int nxb;
+  int lo[3], hi[3];
+  const uint32_t* cls;
+  unsigned long long* bits_e;
+  unsigned long long* bits_h;
+  unsigned int* region_flags;  // bit 0: special E cell in a CPML region; bit 1: special H cell
+};
+void launch_tile_bits(const TileBitsArgs& a, void* stream);
+
+// DFT accumulators (with Kahan compensation C, or nullptr) → interleaved
+// (re, im) doubles, value = F − C.
+template <typename T>
+void launch_dft_read(const Cplx<T>* F, const Cplx<T>* C, double* out, long long n, void* stream);
+
 // FP64 flux reduction: one block per frequency.
 template <typename T>
 void launch_flux(const Cplx<T>* e1, const Cplx<T>* e2, const Cplx<T>* h1, const Cplx<T>* h2,

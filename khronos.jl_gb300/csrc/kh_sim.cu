@@ -209,6 +209,40 @@ class Sim : public SimBase {
     const size_t cnt = size_t(n_[0]) * n_[1] * n_[2];
     dst->resize(cnt);
     for (size_t q = 0; q < cnt; ++q) (*dst)[q] = T(v[q]);
+    if (kind == KH_MAT_EPS_INV) att_eps_[comp] = {};
+    if (kind == KH_MAT_MU_INV) att_mu_[comp] = {};
+    return KH_OK;
+  }
+
+  // kh_sim_attach_material: ε⁻¹ / μ⁻¹ stay in the caller's array until
+  // prepare copies them straight to the device (converted there when the
+  // precision differs); the other kinds are classified on the host and are
+  // copied now.
+  kh_status attach_material(int kind, int comp, const void* v, int dtype) override {
+    if (prepared_) return fail(KH_ERR_INVALID, "attach_material after prepare");
+    if (!v) return fail(KH_ERR_INVALID, "null material array");
+    if (dtype != KH_F32 && dtype != KH_F64) return fail(KH_ERR_INVALID, "material dtype must be KH_F32 or KH_F64");
+    if (kind != KH_MAT_CHI3 && (comp < 0 || comp > 2)) return fail(KH_ERR_INVALID, "material component must be 0..2");
+    if (kind == KH_MAT_EPS_INV || kind == KH_MAT_MU_INV) {
+      (kind == KH_MAT_EPS_INV ? att_eps_ : att_mu_)[comp] = {v, dtype};
+      std::vector<T>& h = kind == KH_MAT_EPS_INV ? eps_h_[comp] : mu_h_[comp];
+      std::vector<T>().swap(h);
+      return KH_OK;
+    }
+    std::vector<T>* dst = nullptr;
+    if (kind == KH_MAT_CHI3) dst = &chi3_h_;
+    else if (kind == KH_MAT_SIGMA_D) dst = &msigd_h_[comp];
+    else if (kind == KH_MAT_SIGMA_B) dst = &msigb_h_[comp];
+    else return fail(KH_ERR_INVALID, "unknown material kind");
+    const size_t cnt = size_t(n_[0]) * n_[1] * n_[2];
+    dst->resize(cnt);
+    if (dtype == KH_F32) {
+      const float* f = static_cast<const float*>(v);
+      for (size_t q = 0; q < cnt; ++q) (*dst)[q] = T(f[q]);
+    } else {
+      const double* f = static_cast<const double*>(v);
+      for (size_t q = 0; q < cnt; ++q) (*dst)[q] = T(f[q]);
+    }
     return KH_OK;
   }
 
@@ -219,7 +253,7 @@ class Sim : public SimBase {
     if (smoothing < KH_SMOOTH_NONE || smoothing > KH_SMOOTH_ANISOTROPIC)
       return fail(KH_ERR_INVALID, "unknown smoothing mode");
     if (!(background > 0)) return fail(KH_ERR_INVALID, "background permittivity must be positive");
-    if (!eps_h_[0].empty() || !eps_h_[1].empty() || !eps_h_[2].empty())
+    if (has_eps(0) || has_eps(1) || has_eps(2))
       return fail(KH_ERR_INVALID, "per-voxel ε⁻¹ was already set with kh_sim_set_material");
     geo_.clear();
     for (int q = 0; q < n; ++q) {
@@ -426,32 +460,8 @@ class Sim : public SimBase {
       KH_TRY(alloc_field(&E_[c]));
       KH_TRY(alloc_field(&H_[c]));
     }
-    // classification and source tables
-    std::vector<uint32_t> cls(static_cast<size_t>(total_), 0u);
-    std::vector<uint8_t> tiles(size_t(nxb_) * n_[1] * n_[2], 0);
-    bool anySpecialE = false, anySpecialH = false;
     auto cidx = [&](int i, int j, int k) { return origin_ + (long long)k * plane_ + (long long)j * pitch_ + i; };
-    auto mark = [&](int i, int j, int k, uint32_t bits) {
-      cls[cidx(i, j, k)] |= bits;
-      tiles[(size_t(k) * n_[1] + j) * nxb_ + i / (32 * kh::kVN)] |= (bits & kh::kSpecialE) ? 1 : 0;
-      tiles[(size_t(k) * n_[1] + j) * nxb_ + i / (32 * kh::kVN)] |= (bits & kh::kSpecialH) ? 2 : 0;
-    };
-    const size_t ncenter = size_t(n_[0]) * n_[1] * n_[2];
-    if (!chi3_h_.empty()) {
-      for (size_t q = 0; q < ncenter; ++q)
-        if (chi3_h_[q] != T(0)) {
-          const int i = int(q % n_[0]), j = int((q / n_[0]) % n_[1]), k = int(q / (size_t(n_[0]) * n_[1]));
-          mark(i, j, k, kh::kSpecialE | kh::kHasChi3);
-          anySpecialE = true;
-        }
-    }
-    for (auto& p : poles_)
-      for (size_t q = 0; q < ncenter; ++q)
-        if (p.sigma[q] != T(0)) {
-          const int i = int(q % n_[0]), j = int((q / n_[0]) % n_[1]), k = int(q / (size_t(n_[0]) * n_[1]));
-          mark(i, j, k, kh::kSpecialE | kh::kHasPole);
-          anySpecialE = true;
-        }
+    auto center = [&](int i, int j, int k) { return (size_t(k) * n_[1] + j) * n_[0] + i; };
     // Sparse source table: entries per cell in injection order
     // (components Ex..Hz, then sources in order; Kernels.jl:455-463, Sources.jl:330-340).
     struct Ent { long long cell; int src, comp; std::complex<double> amp; int i, j, k; long long q; };
@@ -471,56 +481,56 @@ class Sim : public SimBase {
               const std::complex<T> aT(T(a.real()), T(a.imag()));
               if (aT.real() == T(0) && aT.imag() == T(0)) continue;
               ents.push_back({cidx(gi, gj, gk), int(si), comp, std::complex<double>(aT.real(), aT.imag()), gi, gj, gk, q});
-              mark(gi, gj, gk, comp < 3 ? (kh::kSpecialE | kh::kHasSrcE) : (kh::kSpecialH | kh::kHasSrcH));
-              if (comp < 3) anySpecialE = true; else anySpecialH = true;
             }
       }
     std::stable_sort(ents.begin(), ents.end(), [](const Ent& a, const Ent& b) { return a.cell < b.cell; });
+    // Special cells keep their B|D state: E sources, χ3 and poles (E half), H
+    // sources (H half).  An all-zero χ3 or pole array counts as present.
+    bool anySpecialE = !chi3_h_.empty() || !poles_.empty(), anySpecialH = false;
     src_ent_.assign(srcs_.size(), {});
     std::vector<int> slot_off(1, 0), ent_src, ent_comp;
     std::vector<long long> slot_cell;
+    std::vector<uint32_t> slot_bits;
     std::vector<Cplx<T>> ent_amp;
     for (size_t e = 0; e < ents.size();) {
       size_t e2 = e;
       const int slot = int(slot_off.size() - 1);
       if (slot >= (1 << 24)) return fail(KH_ERR_UNSUPPORTED, "too many source cells");
+      uint32_t bits = uint32_t(slot) << kh::kSlotShift;
       while (e2 < ents.size() && ents[e2].cell == ents[e].cell) {
         src_ent_[ents[e2].src].push_back({ents[e2].q, int(ent_src.size())});
         ent_src.push_back(ents[e2].src);
         ent_comp.push_back(ents[e2].comp);
         ent_amp.push_back({T(ents[e2].amp.real()), T(ents[e2].amp.imag())});
+        if (ents[e2].comp < 3) { bits |= kh::kSpecialE | kh::kHasSrcE; anySpecialE = true; }
+        else { bits |= kh::kSpecialH | kh::kHasSrcH; anySpecialH = true; }
         ++e2;
       }
       slot_off.push_back(int(ent_src.size()));
       slot_cell.push_back(ents[e].cell);
-      cls[ents[e].cell] |= uint32_t(slot) << kh::kSlotShift;
+      slot_bits.push_back(bits);
       e = e2;
     }
     // Which cells the LEAN kernels can take (see run_batch): a source cell's
-    // term can be added after the kernel when its component has no W stage
-    // there and the cell carries no χ3 or pole; CPU-path semantics keep B|D
-    // for every component of a special cell inside CPML, which LEAN does not.
+    // term is O = m⁻¹·(T + S) there, exact when its component has no W stage
+    // in that cell and the cell carries no χ3 or pole; CPU-path semantics keep
+    // B|D for every component of a special cell inside CPML, which LEAN does not.
     auto flag = [&](int a, int idx) { return idx < lo_[a] || idx >= n_[a] - hi_[a]; };
     has_src_[0] = has_src_[1] = false;
-    src_fix_ok_[0] = src_fix_ok_[1] = true;
+    src_lean_ok_[0] = src_lean_ok_[1] = true;
     for (const Ent& e : ents) {
       const int half = e.comp >= 3 ? 1 : 0;
       has_src_[half] = true;
       const int own = e.comp % 3;
       const bool fown = flag(own, own == 0 ? e.i : (own == 1 ? e.j : e.k));
-      if (fown) src_fix_ok_[half] = false;
-      if (!half && (cls[e.cell] & (kh::kHasChi3 | kh::kHasPole))) src_fix_ok_[0] = false;
+      if (fown) src_lean_ok_[half] = false;
+      if (!half) {
+        const size_t ci = center(e.i, e.j, e.k);
+        bool dispersive = !chi3_h_.empty() && chi3_h_[ci] != T(0);
+        for (auto& p : poles_) dispersive = dispersive || p.sigma[ci] != T(0);
+        if (dispersive) src_lean_ok_[0] = false;
+      }
     }
-    special_in_region_[0] = special_in_region_[1] = false;
-    for (int k = 0; k < n_[2]; ++k)
-      for (int j = 0; j < n_[1]; ++j)
-        for (int i = 0; i < n_[0]; ++i) {
-          const uint32_t c = cls[cidx(i, j, k)];
-          if (!(c & (kh::kSpecialE | kh::kSpecialH))) continue;
-          if (!(flag(0, i) || flag(1, j) || flag(2, k))) continue;
-          if (c & kh::kSpecialE) special_in_region_[0] = true;
-          if (c & kh::kSpecialH) special_in_region_[1] = true;
-        }
 
     // state arrays that some cell needs
     const bool msb = !msigb_h_[0].empty() || !msigb_h_[1].empty() || !msigb_h_[2].empty();
@@ -534,22 +544,25 @@ class Sim : public SimBase {
       if (msb && sigmask_b_ && (pml_axis_[nx] || pml_axis_[pv])) KH_TRY(alloc_field(&CB_[c]));
       if (msd && sigmask_d_ && (pml_axis_[nx] || pml_axis_[pv])) KH_TRY(alloc_field(&CD_[c]));
     }
-    // materials
+    // materials: compact uploads scattered into the padded layout on the device
     if (geo_set_) KH_TRY(build_geometry());
+    const int tdt = sizeof(T) == 4 ? KH_F32 : KH_F64;
     for (int c = 0; c < 3; ++c) {
-      if (!eps_h_[c].empty()) KH_TRY(upload_center(eps_h_[c], &eps_[c], false));
-      if (!mu_h_[c].empty()) KH_TRY(upload_center(mu_h_[c], &mu_[c], false));
-      if (!msigd_h_[c].empty()) KH_TRY(upload_center(msigd_h_[c], &msigd_[c], false));
-      if (!msigb_h_[c].empty()) KH_TRY(upload_center(msigb_h_[c], &msigb_[c], false));
+      if (att_eps_[c].ptr) KH_TRY(upload_center(att_eps_[c].ptr, att_eps_[c].dtype, &eps_[c]));
+      else if (!eps_h_[c].empty()) KH_TRY(upload_center(eps_h_[c].data(), tdt, &eps_[c]));
+      if (att_mu_[c].ptr) KH_TRY(upload_center(att_mu_[c].ptr, att_mu_[c].dtype, &mu_[c]));
+      else if (!mu_h_[c].empty()) KH_TRY(upload_center(mu_h_[c].data(), tdt, &mu_[c]));
+      if (!msigd_h_[c].empty()) KH_TRY(upload_center(msigd_h_[c].data(), tdt, &msigd_[c]));
+      if (!msigb_h_[c].empty()) KH_TRY(upload_center(msigb_h_[c].data(), tdt, &msigb_[c]));
     }
     if ((eps_[0] != nullptr) != (eps_[2] != nullptr) || (eps_[0] != nullptr) != (eps_[1] != nullptr))
       return fail(KH_ERR_INVALID, "per-voxel ε⁻¹ must be given for all three components");
     if ((mu_[0] != nullptr) != (mu_[2] != nullptr) || (mu_[0] != nullptr) != (mu_[1] != nullptr))
       return fail(KH_ERR_INVALID, "per-voxel μ⁻¹ must be given for all three components");
-    if (!chi3_h_.empty()) KH_TRY(upload_center(chi3_h_, &chi3_, false));
+    if (!chi3_h_.empty()) KH_TRY(upload_center(chi3_h_.data(), tdt, &chi3_));
     for (auto& p : poles_) {
       PoleD pd;
-      KH_TRY(upload_center(p.sigma, &pd.sigma, false));
+      KH_TRY(upload_center(p.sigma.data(), tdt, &pd.sigma));
       for (int c = 0; c < 3; ++c) {
         KH_TRY(alloc_field(&pd.P[c]));
         KH_TRY(alloc_field(&pd.Pp[c]));
@@ -569,22 +582,6 @@ class Sim : public SimBase {
         KH_TRY(upload_raw(tab.data(), tab.size() * sizeof(kh::AxisCoef<T>), (void**)(h ? &axb_[a] : &axd_[a])));
       }
     }
-    if (anySpecialE || anySpecialH) {
-      KH_TRY(upload_raw(cls.data(), cls.size() * sizeof(uint32_t), (void**)&cls_));
-      // per-row-segment plane bitmasks: word (k/64, j, xb), bit k%64
-      const int nkw = (n_[2] + 63) / 64;
-      std::vector<uint64_t> bits_e(size_t(nkw) * n_[1] * nxb_, 0ull), bits_h(bits_e.size(), 0ull);
-      for (int k = 0; k < n_[2]; ++k)
-        for (int j = 0; j < n_[1]; ++j)
-          for (int xb = 0; xb < nxb_; ++xb) {
-            const uint8_t tv = tiles[(size_t(k) * n_[1] + j) * nxb_ + xb];
-            const size_t wi = (size_t(k >> 6) * n_[1] + j) * nxb_ + xb;
-            if (tv & 1) bits_e[wi] |= 1ull << (k & 63);
-            if (tv & 2) bits_h[wi] |= 1ull << (k & 63);
-          }
-      KH_TRY(upload_raw(bits_e.data(), bits_e.size() * sizeof(uint64_t), (void**)&tbits_e_));
-      KH_TRY(upload_raw(bits_h.data(), bits_h.size() * sizeof(uint64_t), (void**)&tbits_h_));
-    }
     nsrc_ = int(srcs_.size());
     if (!ent_src.empty()) {
       KH_TRY(upload_raw(slot_off.data(), slot_off.size() * sizeof(int), (void**)&slot_off_));
@@ -594,6 +591,62 @@ class Sim : public SimBase {
       ent_amp_h_ = ent_amp;
       KH_TRY(upload_raw(slot_cell.data(), slot_cell.size() * sizeof(long long), (void**)&slot_cell_));
       nslots_ = int(slot_cell.size());
+    }
+    // Cell classes and the per-row-segment plane bitmasks (word (k/64, j, xb),
+    // bit k%64), computed on the device from the material arrays and the
+    // source table.
+    unsigned int* region_flags = nullptr;
+    if (anySpecialE || anySpecialH) {
+      KH_TRY(alloc_raw(size_t(total_) * sizeof(uint32_t), (void**)&cls_, false));
+      kh::ClassifyArgs<T> ca;
+      std::memset(&ca, 0, sizeof(ca));
+      for (int a = 0; a < 3; ++a) ca.n[a] = n_[a];
+      ca.pitch = pitch_;
+      ca.plane = plane_;
+      ca.origin = origin_;
+      ca.chi3 = chi3_;
+      ca.npoles = int(poles_d_.size());
+      for (size_t q = 0; q < poles_d_.size(); ++q) ca.pole_sigma[q] = poles_d_[q].sigma;
+      ca.cls = cls_;
+      if (ca.chi3 || ca.npoles) {
+        kh::launch_classify<T>(ca, cudaStreamLegacy);
+        ++launches;
+      }
+      if (nslots_ > 0) {
+        uint32_t* dbits = nullptr;
+        KH_CUDA(kh_host::dev_alloc((void**)&dbits, slot_bits.size() * sizeof(uint32_t), cudaStreamLegacy));
+        cudaError_t e = cudaMemcpyAsync(dbits, slot_bits.data(), slot_bits.size() * sizeof(uint32_t),
+                                        cudaMemcpyHostToDevice, cudaStreamLegacy);
+        if (e == cudaSuccess) {
+          kh::launch_mark_cells(slot_cell_, dbits, nslots_, cls_, cudaStreamLegacy);
+          ++launches;
+        }
+        // the host vector stays alive until the synchronisation at the end of prepare
+        kh_host::dev_free(dbits, cudaStreamLegacy);
+        if (e != cudaSuccess) return fail(KH_ERR_CUDA, cudaGetErrorString(e));
+      }
+      const size_t nwords = size_t((n_[2] + 63) / 64) * n_[1] * nxb_;
+      KH_TRY(alloc_raw(nwords * sizeof(uint64_t), (void**)&tbits_e_, false));
+      KH_TRY(alloc_raw(nwords * sizeof(uint64_t), (void**)&tbits_h_, false));
+      KH_TRY(alloc_raw(sizeof(unsigned int), (void**)&region_flags, false));
+      kh::TileBitsArgs ta;
+      for (int a = 0; a < 3; ++a) {
+        ta.n[a] = n_[a];
+        ta.lo[a] = lo_[a];
+        ta.hi[a] = hi_[a];
+      }
+      ta.pitch = pitch_;
+      ta.plane = plane_;
+      ta.origin = origin_;
+      ta.nxb = nxb_;
+      ta.cls = cls_;
+      ta.bits_e = reinterpret_cast<unsigned long long*>(tbits_e_);
+      ta.bits_h = reinterpret_cast<unsigned long long*>(tbits_h_);
+      ta.region_flags = region_flags;
+      kh::launch_tile_bits(ta, cudaStreamLegacy);
+      ++launches;
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return fail(KH_ERR_CUDA, std::string("classification kernels: ") + cudaGetErrorString(e));
     }
     // monitors
     for (auto& m : mons_) {
@@ -654,6 +707,13 @@ class Sim : public SimBase {
     // the zeroing and uploads above ran on the legacy default stream; wait for
     // them only (work of other simulations on non-blocking streams goes on)
     KH_CUDA(cudaStreamSynchronize(cudaStreamLegacy));
+    special_in_region_[0] = special_in_region_[1] = false;
+    if (region_flags) {
+      unsigned int rf = 0;
+      KH_CUDA(cudaMemcpy(&rf, region_flags, sizeof(rf), cudaMemcpyDeviceToHost));
+      special_in_region_[0] = (rf & 1u) != 0;
+      special_in_region_[1] = (rf & 2u) != 0;
+    }
     prepared_ = true;
     return KH_OK;
 #undef KH_TRY
@@ -718,8 +778,8 @@ class Sim : public SimBase {
       if (pml[c]) b += 2 * field;
       if (msb && (pml[nx] || pml[pv])) b += field;
       if (msd && (pml[nx] || pml[pv])) b += field;
-      if (!eps_h_[c].empty() || geo_set_) b += field;
-      if (!mu_h_[c].empty()) b += field;
+      if (has_eps(c) || geo_set_) b += field;
+      if (has_mu(c)) b += field;
       if (!msigd_h_[c].empty()) b += field;
       if (!msigb_h_[c].empty()) b += field;
     }
@@ -762,19 +822,16 @@ class Sim : public SimBase {
     if (!prepared_) return fail(KH_ERR_INVALID, "read_dft before prepare");
     const Mon& m = mons_[id];
     const size_t cnt = size_t(m.ncell) * m.nf;
-    std::vector<Cplx<T>> F(cnt), C;
     if (kh_status es = wait_idle(); es != KH_OK) return es;
-    KH_CUDA(cudaMemcpy(F.data(), m.F, cnt * sizeof(Cplx<T>), cudaMemcpyDeviceToHost));
-    if (m.C) {
-      C.resize(cnt);
-      KH_CUDA(cudaMemcpy(C.data(), m.C, cnt * sizeof(Cplx<T>), cudaMemcpyDeviceToHost));
-    }
-    for (size_t q = 0; q < cnt; ++q) {
-      double re = double(F[q].re), im = double(F[q].im);
-      if (m.C) { re -= double(C[q].re); im -= double(C[q].im); }
-      out[2 * q] = re;
-      out[2 * q + 1] = im;
-    }
+    // F − C in FP64 on the device, then one copy into the caller's array
+    double* dout = nullptr;
+    KH_CUDA(kh_host::dev_alloc((void**)&dout, cnt * 2 * sizeof(double), cudaStreamLegacy));
+    kh::launch_dft_read<T>(m.F, m.C, dout, (long long)cnt, cudaStreamLegacy);
+    ++launches;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(out, dout, cnt * 2 * sizeof(double), cudaMemcpyDeviceToHost);
+    kh_host::dev_free(dout, cudaStreamLegacy);
+    if (e != cudaSuccess) return fail(KH_ERR_CUDA, std::string("read_dft: ") + cudaGetErrorString(e));
     return KH_OK;
   }
 
@@ -1013,8 +1070,8 @@ class Sim : public SimBase {
   }
 
   void model_split(double& h_bytes, double& e_bytes, double& dft_bytes) const override {
-    const bool pervox_eps = eps_h_[0].size() > 0 || geo_set_;
-    const bool pervox_mu = mu_h_[0].size() > 0;
+    const bool pervox_eps = has_eps(0) || geo_set_;
+    const bool pervox_mu = has_mu(0);
     const long long cells = 1LL * n_[0] * n_[1] * n_[2];
     // H: E 3 rd + H 3 rd + H 3 wr (+ μ⁻¹ 3 rd); E: H 3 rd + E 3 rd + E 3 wr (+ ε⁻¹ 3 rd)
     double hw = (9 + (pervox_mu ? 3 : 0)) * double(cells);
@@ -1208,20 +1265,37 @@ class Sim : public SimBase {
     return KH_OK;
   }
 
-  // Center-range host array (x fastest) → padded device layout.
-  kh_status upload_center(const std::vector<T>& h, T** out, bool is_state) {
-    std::vector<T> pad(static_cast<size_t>(total_), T(0));
-    for (int k = 0; k < n_[2]; ++k)
-      for (int j = 0; j < n_[1]; ++j)
-        std::memcpy(&pad[origin_ + (long long)k * plane_ + (long long)j * pitch_],
-                    &h[(size_t(k) * n_[1] + j) * n_[0]], sizeof(T) * n_[0]);
+  // Center-range host array (x fastest, float or double) → padded device
+  // layout in the run's precision: one compact host-to-device copy into a
+  // pool buffer, then a scatter kernel (the ring and row padding stay zero).
+  kh_status upload_center(const void* src, int src_dtype, T** out) {
     void* p = nullptr;
-    kh_status st = alloc_raw(pad.size() * sizeof(T), &p, is_state);
+    kh_status st = alloc_raw(size_t(total_) * sizeof(T), &p, false);
     if (st != KH_OK) return st;
-    KH_CUDA(cudaMemcpy(p, pad.data(), pad.size() * sizeof(T), cudaMemcpyHostToDevice));
     *out = static_cast<T*>(p);
+    const size_t cnt = size_t(n_[0]) * n_[1] * n_[2];
+    if (cnt == 0) return KH_OK;
+    const size_t bytes = cnt * (src_dtype == KH_F32 ? sizeof(float) : sizeof(double));
+    void* tmp = nullptr;
+    KH_CUDA(kh_host::dev_alloc(&tmp, bytes, cudaStreamLegacy));
+    cudaError_t e = cudaMemcpyAsync(tmp, src, bytes, cudaMemcpyHostToDevice, cudaStreamLegacy);
+    if (e == cudaSuccess) {
+      if (src_dtype == KH_F32)
+        kh::launch_scatter_center<float, T>(static_cast<const float*>(tmp), *out, n_, pitch_, plane_, origin_,
+                                            cudaStreamLegacy);
+      else
+        kh::launch_scatter_center<double, T>(static_cast<const double*>(tmp), *out, n_, pitch_, plane_, origin_,
+                                             cudaStreamLegacy);
+      ++launches;
+      e = cudaGetLastError();
+    }
+    kh_host::dev_free(tmp, cudaStreamLegacy);
+    if (e != cudaSuccess) return fail(KH_ERR_CUDA, std::string("material upload: ") + cudaGetErrorString(e));
     return KH_OK;
   }
+
+  bool has_eps(int c) const { return !eps_h_[c].empty() || att_eps_[c].ptr; }
+  bool has_mu(int c) const { return !mu_h_[c].empty() || att_mu_[c].ptr; }
 
   // eval_time_source in the run's precision (TimeSources.jl:61-64, 123-132, 178-184)
   std::complex<T> eval_time(const SrcH& s, double t, int64_t step, bool h_half) const {
@@ -1359,7 +1433,7 @@ class Sim : public SimBase {
       ph.sources_active = P.sa ? 1 : 0;
       ph.f_now = dtab + P.fH;
       const bool src_h = P.sa && has_src_[1];
-      ph.full = (full_h_base || (src_h && !src_fix_ok_[1])) ? 1 : 0;
+      ph.full = (full_h_base || (src_h && !src_lean_ok_[1])) ? 1 : 0;
       mark(s, 0);
       if (use_tma_) kh::launch_half_step_tma<T>(true, ph, maps_h_, st);
       else kh::launch_half_step<T>(true, ph, st);
@@ -1380,7 +1454,7 @@ class Sim : public SimBase {
       pe.sources_active = P.sa ? 1 : 0;
       pe.f_now = dtab + P.fE;
       const bool src_e = P.sa && has_src_[0];
-      pe.full = (full_e_base || (src_e && !src_fix_ok_[0])) ? 1 : 0;
+      pe.full = (full_e_base || (src_e && !src_lean_ok_[0])) ? 1 : 0;
       if (use_tma_) kh::launch_half_step_tma<T>(false, pe, maps_e_, st);
       else kh::launch_half_step<T>(false, pe, st);
       ++launches;
@@ -1419,9 +1493,23 @@ class Sim : public SimBase {
       GraphEntry* g = nullptr;
       for (auto& ge : graphs_)
         if (ge.sig == sig) { g = &ge; break; }
-      if (g) ++graph_hits_;
-      else ++graph_misses_;
+      // A sequence is captured the second time it is seen: batches that occur
+      // once (a short run, the last partial batch) are issued directly rather
+      // than paying a capture and an instantiation they never amortise.
+      bool seen_before = false;
       if (!g) {
+        for (auto& sv : seen_)
+          if (sv == sig) { seen_before = true; break; }
+        if (!seen_before) {
+          if (seen_.size() >= kMaxGraphs) seen_.erase(seen_.begin());
+          seen_.push_back(sig);
+        }
+      }
+      if (g) ++graph_hits_;
+      else if (seen_before) ++graph_misses_;
+      if (!g && !seen_before) {
+        issue_all(ws);
+      } else if (!g) {
         if (graphs_.size() >= kMaxGraphs) {  // evict the least recently used
           size_t lru = 0;
           for (size_t q = 1; q < graphs_.size(); ++q)
@@ -1442,10 +1530,12 @@ class Sim : public SimBase {
         launches = l0;
         g = &graphs_.back();
       }
-      g->last_use = ++graph_clock_;
-      KH_CUDA(cudaGraphLaunch(g->exec, ws));
-      launches += g->nlaunch;
-      ++graph_replays_;
+      if (g) {
+        g->last_use = ++graph_clock_;
+        KH_CUDA(cudaGraphLaunch(g->exec, ws));
+        launches += g->nlaunch;
+        ++graph_replays_;
+      }
       KH_CUDA(cudaEventRecord(ev_out_, ws));
       KH_CUDA(cudaStreamWaitEvent(stream, ev_out_, 0));
       // batches that rarely repeat (irregular step counts) capture more than
@@ -1754,6 +1844,12 @@ class Sim : public SimBase {
   bool prepared_ = false;
 
   std::vector<T> sigb_h_[3], sigd_h_[3], eps_h_[3], mu_h_[3], msigd_h_[3], msigb_h_[3], chi3_h_;
+  // ε⁻¹ / μ⁻¹ attached with kh_sim_attach_material: the caller's array, read at prepare
+  struct Attached {
+    const void* ptr = nullptr;
+    int dtype = KH_F32;
+  };
+  Attached att_eps_[3], att_mu_[3];
   std::vector<PoleH> poles_;
   std::vector<PoleD> poles_d_;
   std::vector<SrcH> srcs_;
@@ -1769,11 +1865,12 @@ class Sim : public SimBase {
   cudaStream_t gstream_ = nullptr;
   cudaEvent_t ev_in_ = nullptr, ev_out_ = nullptr;
   std::vector<GraphEntry> graphs_;
+  std::vector<std::vector<int64_t>> seen_;  // signatures issued once, not yet captured
   uint64_t graph_clock_ = 0;
   int64_t graph_replays_ = 0;
   int nsrc_ = 0;
   bool has_src_[2] = {false, false};         // [E half, H half]
-  bool src_fix_ok_[2] = {true, true};
+  bool src_lean_ok_[2] = {true, true};
   bool special_in_region_[2] = {false, false};
   long long* slot_cell_ = nullptr;
   int nslots_ = 0;
@@ -1865,6 +1962,11 @@ const char* kh_last_error(const kh_sim* sim) {
 kh_status kh_sim_set_material(kh_sim* sim, int32_t kind, int32_t comp, const double* values) {
   if (!sim) return KH_ERR_INVALID;
   return sim->impl->set_material(kind, comp, values);
+}
+
+kh_status kh_sim_attach_material(kh_sim* sim, int32_t kind, int32_t comp, const void* values, int32_t dtype) {
+  if (!sim) return KH_ERR_INVALID;
+  return sim->impl->attach_material(kind, comp, values, dtype);
 }
 
 kh_status kh_sim_add_pole(kh_sim* sim, const kh_pole_coeffs* coeffs, const double* sigma) {

@@ -51,6 +51,7 @@ struct SimBase {
   std::string err;
   int64_t launches = 0;
   virtual kh_status set_material(int kind, int comp, const double* v) = 0;
+  virtual kh_status attach_material(int kind, int comp, const void* v, int dtype) = 0;
   virtual kh_status add_pole(const kh_pole_coeffs& c, const double* s) = 0;
   virtual kh_status add_source(const kh_source_desc& s) = 0;
   virtual kh_status add_monitor(int comp, const int32_t* st, const int32_t* dm, int nf,

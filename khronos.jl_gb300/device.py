@@ -15,6 +15,17 @@ def _dptr(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
 
+def _material_array(a: np.ndarray):
+    """A cell-indexed material array as the library reads it: x fastest,
+    contiguous, float32 or float64 kept as given (no copy when it already is,
+    e.g. a Fortran-ordered float32 array in pinned memory), with its KH_F* tag."""
+    a = np.asarray(a)
+    if a.dtype not in (np.float32, np.float64):
+        a = a.astype(np.float64)
+    flat = a.ravel(order="F")
+    return flat, (_abi.KH_F32 if flat.dtype == np.float32 else _abi.KH_F64)
+
+
 class GpuSim:
     """Device-resident simulation driven through the C ABI."""
 
@@ -42,10 +53,14 @@ class GpuSim:
         d.semantics = int(spec.semantics)
         d.periodic = int(spec.periodic)
         self._check(self.lib.kh_sim_create(C.byref(d), C.byref(self.handle)))
+        # material arrays the library reads at prepare (kh_sim_attach_material);
+        # held until then (for a request server, until the simulation is released)
+        self._materials = []
         try:
             for kind, comp, arr in spec.materials:
-                h = flat_f(arr)
-                self._check(self.lib.kh_sim_set_material(self.handle, kind, comp, _dptr(h)))
+                h, dt = _material_array(arr)
+                self._materials.append(h)
+                self._check(self.lib.kh_sim_attach_material(self.handle, kind, comp, h.ctypes.data, dt))
             for p in spec.poles:
                 pc = _abi.PoleCoeffs(**p.coeffs)
                 h = flat_f(p.sigma)
@@ -96,6 +111,7 @@ class GpuSim:
                 self.history_ids.append(hid.value)
             if prepare:
                 self._check(self.lib.kh_sim_prepare(self.handle))
+                self._materials = []
         except Exception:
             self.close()
             raise
@@ -189,9 +205,9 @@ class GpuSim:
         """DFT accumulator of a monitor, shape (Nx, Ny, Nz, Nf), complex128."""
         m = self.spec.monitors[monitor_index]
         cnt = int(np.prod(m.dims)) * len(m.freqs)
-        out = np.zeros(2 * cnt, dtype=np.float64)
-        self._check(self.lib.kh_sim_read_dft(self.handle, self.monitor_ids[monitor_index], _dptr(out)))
-        z = out[0::2] + 1j * out[1::2]
+        z = np.empty(cnt, dtype=np.complex128)  # interleaved (re, im) doubles
+        self._check(self.lib.kh_sim_read_dft(self.handle, self.monitor_ids[monitor_index],
+                                             z.ctypes.data_as(C.POINTER(C.c_double))))
         return z.reshape(tuple(m.dims) + (len(m.freqs),), order="F")
 
     def flux(self, monitor_indices: Sequence[int], normal_axis: int, dA: float) -> np.ndarray:

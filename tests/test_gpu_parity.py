@@ -290,7 +290,9 @@ def test_z_tiling_is_invisible(kh, oracle, gpu_lib, monkeypatch):
 @pytest.mark.parametrize("dtype", ["f32", "f64"])
 def test_step_graphs_are_invisible(kh, gpu_lib, dtype, monkeypatch):
     """Batches replayed from captured CUDA graphs give bit-identical fields and
-    DFT values to directly launched batches, across the source cutoff."""
+    DFT values to directly launched batches, across the source cutoff.  A
+    launch sequence is captured the second time it occurs, so the run ends
+    with full batches that repeat."""
     from khronos_gb300 import configs
     from khronos_gb300.device import GpuSim
 
@@ -300,7 +302,7 @@ def test_step_graphs_are_invisible(kh, gpu_lib, dtype, monkeypatch):
     for mode in ("0", "1"):
         monkeypatch.setenv("KHRONOS_GB300_GRAPHS", mode)
         g = GpuSim(spec, lib=gpu_lib)
-        for n in (7, 1500, 64, 64, 300):  # irregular calls across the cutoff (step ~400)
+        for n in (7, 1500, 64, 64, 300, 2500):  # irregular calls across the cutoff (step ~400)
             g.step(n)
         out[mode] = ([g.field(c) for c in range(6)], [g.dft(m) for m in range(len(spec.monitors))],
                      g.graph_replays)
