@@ -12,8 +12,15 @@ over the whole grid; the metric is cell-updates per second.
 
 Multi-GPU: replicas only (one independent simulation per GPU, no collective
 on the data path); value = all ranks' cell-updates / max-over-ranks time.
-The reference arm times the CPU restatement of the reference's CPU step loop
-(the reference is Julia and cannot run here) on the same workload.
+The reference arm times the CPU restatement of the reference's step loop (the
+reference is Julia and cannot run here) on the same workload and CPML stage
+logic, on all host threads.
+
+The default line also carries: `e2e` (the same run through the public API
+from pinned host arrays, set-up and flux read-back included), `flux_error`
+(full FP32 run against the FP64 run of the same inputs), `serve` (64-request
+serving stream against one-at-a-time runs under the same arrivals) and
+`cpu_baseline`.
 """
 from __future__ import annotations
 
@@ -45,60 +52,141 @@ def dist_env():
         os.environ.get("LOCAL_RANK", "0"))
 
 
+class _Nvml:
+    """Minimal NVML reader (ctypes on the driver's libnvidia-ml): SM clock,
+    its maximum and the active clock-event (throttle) reasons.  Read-only."""
+
+    REASONS = {0x8: "hw_slowdown", 0x40: "hw_thermal_slowdown", 0x20: "sw_thermal_slowdown",
+               0x4: "sw_power_cap"}
+
+    def __init__(self, uuid, index: int):
+        import ctypes as C
+
+        self.C = C
+        self.lib = C.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.h = C.c_void_p()
+        st = -1
+        if uuid:
+            st = self.lib.nvmlDeviceGetHandleByUUID(uuid.encode(), C.byref(self.h))
+        if st != 0:
+            st = self.lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(index), C.byref(self.h))
+        if st != 0:
+            raise OSError("no NVML handle for the device")
+        self.reasons_fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        v = C.c_uint()
+        self.lib.nvmlDeviceGetMaxClockInfo(self.h, 1, C.byref(v))  # NVML_CLOCK_SM
+        self.max_sm = float(v.value)
+
+    def sample(self):
+        C = self.C
+        v, r = C.c_uint(), C.c_ulonglong()
+        self.lib.nvmlDeviceGetClockInfo(self.h, 1, C.byref(v))
+        self.reasons_fn(self.h, C.byref(r))
+        return float(v.value), int(r.value)
+
+
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """SM clock and throttle reasons sampled every millisecond (NVML) from
+    __enter__ to __exit__; mark() brackets the timed region, and summary()
+    reports the samples taken inside it.  Falls back to nvidia-smi polling
+    when NVML cannot be opened."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index: int, period_ms: int = 100):
-        self.cmd = ["nvidia-smi", "-i", str(gpu_index), f"--query-gpu={self.FIELDS}",
-                    "--format=csv,noheader,nounits", f"-lms", str(period_ms)]
+    def __init__(self, gpu_index: int, period_ms: float = 1.0):
+        self.index = gpu_index
+        self.period = period_ms / 1e3
+        self.samples = []  # (time, sm_mhz, max_mhz, reasons set)
+        self.window = None
+        self._stop = threading.Event()
         self.proc = None
-        self.lines = []
+        self.thread = None
+        self.source = "nvml"
 
     def __enter__(self):
+        uuid = None
         try:
-            self.proc = subprocess.Popen(self.cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.thread = threading.Thread(target=self._read, daemon=True)
-            self.thread.start()
+            import torch
+
+            u = getattr(torch.cuda.get_device_properties(self.index), "uuid", None)
+            if u is not None:
+                uuid = "GPU-" + str(u)
+        except Exception:
+            pass
+        try:
+            self.nvml = _Nvml(uuid, self.index)
+            self.thread = threading.Thread(target=self._poll_nvml, daemon=True)
         except OSError:
-            self.proc = None
+            self.nvml = None
+            self.source = "nvidia-smi"
+            try:
+                self.proc = subprocess.Popen(
+                    ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                     "--format=csv,noheader,nounits", "-lms", "20"],
+                    stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            except OSError:
+                self.proc = None
+                return self
+            self.thread = threading.Thread(target=self._read_smi, daemon=True)
+        self.thread.start()
         return self
 
-    def _read(self):
+    def _poll_nvml(self):
+        names = _Nvml.REASONS
+        while not self._stop.is_set():
+            try:
+                sm, r = self.nvml.sample()
+            except Exception:
+                break
+            self.samples.append((time.perf_counter(), sm, self.nvml.max_sm,
+                                 {n for bit, n in names.items() if r & bit}))
+            time.sleep(self.period)
+
+    def _read_smi(self):
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm, smax = float(parts[0]), float(parts[1])
+            except ValueError:
+                continue
+            self.samples.append((time.perf_counter(), sm, smax,
+                                 {nm for nm, v in zip(names, parts[4:8]) if v.lower().startswith("active")}))
+
+    def mark(self, t0: float, t1: float):
+        self.window = (t0, t1)
 
     def __exit__(self, *exc):
+        self._stop.set()
         if self.proc is not None:
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
             except subprocess.TimeoutExpired:
                 self.proc.kill()
+        if self.thread is not None:
             self.thread.join(timeout=5)
 
     def summary(self):
-        sm, smax, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
-            parts = [p.strip() for p in ln.split(",")]
-            if len(parts) < 8:
-                continue
-            try:
-                sm.append(float(parts[0]))
-                smax.append(float(parts[1]))
-            except ValueError:
-                continue
-            for nm, v in zip(names, parts[4:8]):
-                if v.lower().startswith("active"):
-                    reasons.add(nm)
-        if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
-                "samples": len(sm)}
+        inside = self.samples
+        scope = "sampler lifetime"
+        if self.window is not None:
+            w = [s for s in self.samples if self.window[0] <= s[0] <= self.window[1]]
+            if w:
+                inside, scope = w, "timed region"
+        if not inside:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0, "source": self.source}
+        reasons = set().union(*(s[3] for s in inside))
+        return {"sm_mhz": statistics.median(s[1] for s in inside), "sm_max_mhz": max(s[2] for s in inside),
+                "reasons": sorted(reasons), "samples": len(inside), "scope": scope, "source": self.source,
+                "period_ms": self.period * 1e3}
 
 
 def measured_peaks():
@@ -140,7 +228,7 @@ def build_workload(dtype="f32", semantics="cpml"):
 def cpu_baseline(spec, budget_s=12.0):
     """The CPU restatement on the host cores, on a bounded number of full-grid steps."""
     orc = __graft_entry__._oracle()
-    o = orc.OracleSim(spec)
+    o = orc.OracleSim(spec, timed=True)
     t0 = time.perf_counter()
     o.step(2)
     per = max((time.perf_counter() - t0) / 2, 1e-6)
@@ -152,39 +240,59 @@ def cpu_baseline(spec, budget_s=12.0):
     cells = spec.cells
     return {"value": cells * n / dt / 1e9, "unit": UNIT, "cores": orc.num_threads(), "kind": "port",
             "sample": f"{n} full-grid steps of the same workload after 2 warm-up steps "
-                      f"({cells} cells, FP32, C++ restatement of the reference CPU step loop, OpenMP)"}
+                      f"({cells} cells, FP32, C++ restatement of the reference step loop, OpenMP, "
+                      f"-O3 with FMA contraction)"}
 
 
 def run_reference(args, world, rank):
+    """The reference arm: the C++ restatement of the reference's step loop
+    (the reference is Julia and cannot run here) on the host cores, on the
+    same workload and CPML stage logic as the GPU arm; the reference CPU
+    path's own stage dispatch is timed beside it on a short sample."""
     if rank != 0:
         return 0
-    w, spec = build_workload("f32", "reference_cpu")
     orc = __graft_entry__._oracle()
-    o = orc.OracleSim(spec)
-    o.step(max(args.warmup, 1))
-    # each timed step is one full-grid step; bound the run to about a minute
-    t0 = time.perf_counter()
-    o.step(1)
-    per = max(time.perf_counter() - t0, 1e-6)
-    k = int(max(1, min(args.steps, 60.0 / per)))
-    t0 = time.perf_counter()
-    o.step(k)
-    dt = time.perf_counter() - t0
+
+    def timed(semantics, steps, warmup, budget_s):
+        w, spec = build_workload("f32", semantics)
+        o = orc.OracleSim(spec, timed=True)
+        o.step(max(warmup, 1))
+        t0 = time.perf_counter()
+        o.step(1)
+        per = max(time.perf_counter() - t0, 1e-6)
+        k = int(max(1, min(steps, budget_s / per)))
+        t0 = time.perf_counter()
+        o.step(k)
+        dt = time.perf_counter() - t0
+        o.close()
+        return spec, k, dt
+
+    spec, k, dt = timed("cpml", args.steps, args.warmup, 60.0)
     value = spec.cells * k / dt / 1e9
+    _, k2, dt2 = timed("reference_cpu", min(args.steps, 10), 1, 10.0)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": k, "warmup": args.warmup, "ms_per_step": dt / k * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOADS[_workload_name].replace("CUDA-path semantics",
-                                                                  "reference CPU-path semantics"),
-                   "grid": list(spec.n), "note": "reference is Julia (absent); timed: its CPU step loop "
-                                                 "restated in C++ (oracle/), all host threads"},
+        "config": workload_config(spec, 1),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": orc.num_threads(), "kind": "port",
-                         "sample": f"{k} full-grid steps (requested {args.steps}) after {args.warmup} warm-up"},
+                         "sample": f"{k} full-grid steps (requested {args.steps}) after {args.warmup} warm-up; "
+                                   "C++ restatement of the reference step loop (Julia is absent), OpenMP over "
+                                   "all host threads, -O3 with FMA contraction"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "reference_cpu_path_stages": {
+            "value": spec.cells * k2 / dt2 / 1e9, "unit": UNIT, "steps": k2,
+            "note": "same grid with the reference CPU path's own CPML stage dispatch (generic_curl!, "
+                    "Helpers.jl:39-270), which this arm's CUDA-path stage logic replaces"},
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def workload_config(spec, world):
+    return {"workload": WORKLOADS[_workload_name], "grid": list(spec.n), "cells": spec.cells,
+            "l2": "inputs larger than L2 (fields+materials+CPML state ~0.9 GB per replica vs 129 MB L2); no flush",
+            "parallelism": f"replicas{world}" if world > 1 else "single"}
 
 
 def run_ours(args, world, rank, local_rank):
@@ -206,23 +314,30 @@ def run_ours(args, world, rank, local_rank):
 
     # ---- device-resident run: inputs already in HBM --------------------------
     gpu = GpuSim(spec)
-    gpu.step(args.warmup, sh)
-    torch.cuda.synchronize()
-    h_bytes, e_bytes, dft_bytes = gpu.model_bytes_split()
-    launches0 = gpu.launches
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local_rank) as clk:
+        gpu.step(args.warmup, sh)
+        torch.cuda.synchronize()
+        h_bytes, e_bytes, dft_bytes = gpu.model_bytes_split()
+        launches0 = gpu.launches
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
         start.record(stream)
-        h_ms, e_ms, dft_ms = gpu.step_timed(args.steps, sh)
+        gpu.step(args.steps, sh)
         end.record(stream)
         torch.cuda.synchronize()
+        clk.mark(t0, time.perf_counter())
     if dist:
         dist.barrier()
     ms = start.elapsed_time(end)
     launches = gpu.launches - launches0
+    # Per-kernel split for the roofline: a separate pass after the timed
+    # region, with CUDA events around the launches of every 8th step (events
+    # inside the timed region would cost it ~4 %).
+    rsteps = max(args.steps, 64)
+    h_ms, e_ms, dft_ms = gpu.step_timed(rsteps, sh)
     from khronos_gb300.replicas import aggregate_rate, max_over_ranks
 
     ms_max = max_over_ranks(ms, dist, device="cuda")
@@ -241,22 +356,23 @@ def run_ours(args, world, rank, local_rank):
     peak, peak_kind = measured_peaks()
     simt = os.environ.get("KHRONOS_GB300_KERNEL") == "simt"
     e_kernel = "half_step_kernel<float,E>" if simt else "half_step_tma_kernel<float,E>"
-    e_launch_ms = e_ms / args.steps
+    e_launch_ms = e_ms / rsteps
     achieved = e_bytes / (e_launch_ms / 1e3) / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOADS[_workload_name], "grid": list(spec.n), "cells": cells,
-                   "l2": "inputs larger than L2 (fields+materials+CPML state ~0.9 GB per replica vs 129 MB L2); no flush",
-                   "parallelism": f"replicas{world}" if world > 1 else "single"},
+        "config": workload_config(spec, world),
         "roofline": {"bound": "hbm", "kernel": e_kernel, "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "algorithmic_bytes_per_launch": e_bytes,
                      "traffic": ncu_traffic(e_kernel) if _workload_name == "waveguide" else None,
-                     "h_kernel": {"achieved": h_bytes / (h_ms / args.steps / 1e3) / 1e9,
-                                  "algorithmic_bytes_per_launch": h_bytes, "ms_per_launch": h_ms / args.steps},
-                     "e_ms_per_launch": e_launch_ms, "dft_ms_per_step": dft_ms / args.steps,
+                     "h_kernel": {"achieved": h_bytes / (h_ms / rsteps / 1e3) / 1e9,
+                                  "algorithmic_bytes_per_launch": h_bytes, "ms_per_launch": h_ms / rsteps,
+                                  "frac": h_bytes / (h_ms / rsteps / 1e3) / 1e9 / peak},
+                     "e_ms_per_launch": e_launch_ms, "dft_ms_per_step": dft_ms / rsteps,
+                     "timing": f"CUDA events around the launches of every 8th step of a {rsteps}-step pass "
+                               "after the timed region",
                      "step_model_bytes": h_bytes + e_bytes + dft_bytes,
                      "step_achieved": (h_bytes + e_bytes + dft_bytes) / (ms_max / args.steps / 1e3) / 1e9},
         "clocks": clk.summary(),
@@ -266,6 +382,8 @@ def run_ours(args, world, rank, local_rank):
         line["e2e"] = e2e
     if not args.no_flux_check:
         line["flux_error"] = flux_accuracy(w, sh)
+    if world == 1 and not args.no_serve and _workload_name == "waveguide":
+        line["serve"] = serving_leg(args.serve_requests_default, compact=True)
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(spec)
     print(json.dumps(line), flush=True)
@@ -296,31 +414,52 @@ def flux_accuracy(w, sh):
 
 
 def end_to_end(args, spec, w, sh, world, dist, cells):
-    """Same metric through the C ABI from host buffers: create + upload, K steps,
-    DFT arrays and fluxes read back to the host, all inside the timed region."""
+    """Same metric through the public API from host buffers: the simulation
+    created from material arrays in pinned host memory in the run's precision
+    (FP32), prepared (uploads, device classification), K steps, and the flux
+    spectra of both planes (the run's result) read back to the host, all inside
+    the timed region."""
+    import dataclasses
+
     import torch
     from khronos_gb300.device import GpuSim
 
+    # inputs staged in pinned host memory before the timed region, as a caller
+    # that keeps its GeometryData arrays in page-locked memory would hold them
+    pinned, mats = [], []
+    for kind, comp, arr in spec.materials:
+        buf = torch.empty(int(arr.size), dtype=torch.float32, pin_memory=True)
+        h = buf.numpy().reshape(arr.shape, order="F")
+        h[...] = arr
+        pinned.append(buf)
+        mats.append((kind, comp, h))
+    spec_h = dataclasses.replace(spec, materials=mats)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    g2 = GpuSim(spec)  # host arrays -> device (materials, σ, sources, monitors)
+    g2 = GpuSim(spec_h)  # create, attach the pinned arrays, prepare
+    t1 = time.perf_counter()
     g2.step(args.steps, sh)
-    dft_host = [g2.dft(m) for m in range(len(spec.monitors))]
+    g2.synchronize()
+    t2 = time.perf_counter()
     fluxes = [g2.flux(list(range(4 * i, 4 * i + 4)), fm.normal_axis, fm.dA)
               for i, fm in enumerate(w.flux_monitors)]
+    t3 = time.perf_counter()
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     g2.close()
-    h2d = sum(a.nbytes for _, _, a in spec.materials) // 2  # values cross as the run's FP32
+    h2d = sum(a.nbytes for _, _, a in mats)
     h2d += sum(s.amp.size * 16 for s in spec.sources) + sum(x.size * 8 for x in spec.sigma_b + spec.sigma_d
                                                             if x is not None)
-    d2h = sum(d.size * 16 for d in dft_host) + sum(f.size * 8 for f in fluxes)
+    d2h = sum(f.size * 8 for f in fluxes)
     from khronos_gb300.replicas import aggregate_rate, max_over_ranks
 
     e2e_max = max_over_ranks(e2e_s, dist, device="cuda")
     return {"value": aggregate_rate(cells * args.steps, e2e_max, world) / 1e9, "unit": UNIT,
             "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
-            "scope": "GpuSim(spec) from host arrays + K steps + DFT arrays and flux read back to host"}
+            "breakdown_ms": {"create_prepare": (t1 - t0) * 1e3, "steps": (t2 - t1) * 1e3,
+                             "flux_readback": (t3 - t2) * 1e3},
+            "scope": "GpuSim(spec) from FP32 material arrays in pinned host memory (create, attach, prepare: "
+                     "uploads + device classification) + K steps + both planes' flux spectra read back to host"}
 
 
 def _pct(v, q):
@@ -329,11 +468,15 @@ def _pct(v, q):
     return float(np.percentile(np.asarray(v, dtype=np.float64), q)) if len(v) else None
 
 
-def serving_leg(n_requests, seed=2024, budget_gb=150.0, max_resident=16, quantum=64, load=1.5, world=1, rank=0):
-    """The serving stream twice: one plain simulation at a time (the
-    reference's run_batch), then through the request server with Poisson
-    arrivals at `load` × the sequential throughput.  Latency = result read
-    back on the host − scheduled arrival."""
+def serving_leg(n_requests, seed=2024, budget_gb=150.0, max_resident=16, quantum=64, load=1.5, world=1, rank=0,
+                compact=False):
+    """The serving stream under Poisson arrivals, twice: one plain simulation
+    at a time in arrival order (the reference's run_batch, src/Batch.jl:103-145,
+    fed by the same arrivals), then through the request server.  Latency =
+    flux read back on the host − scheduled arrival.  The offered load is
+    `load` × the sequential throughput measured on the first few requests.
+    Without `compact`, the saturated capacity (whole stream submitted at
+    once) is measured too."""
     import threading
 
     import numpy as np
@@ -350,110 +493,118 @@ def serving_leg(n_requests, seed=2024, budget_gb=150.0, max_resident=16, quantum
         mine = set(shard([r.work for r in stream], world, rank))
         stream = [r for i, r in enumerate(stream) if i in mine]
     work = [r.work for r in stream]
+    # each request's host-side Simulation → spec, built before the clocks start
+    made = [r.make() for r in stream]
+    specs = [m.sim.spec() for m in made]
 
     def flux_of(g, w):
         fm = w.flux_monitors[0]
         return g.flux([0, 1, 2, 3], fm.normal_axis, fm.dA)
 
-    # 1) sequential, back to back: per-request service time
-    torch.cuda.synchronize()
-    service, seq_flux = [], []
-    for r in stream:
-        t0 = time.perf_counter()
-        w = r.make()
-        g = GpuSim(w.sim.spec())
-        g.step(r.steps)
-        seq_flux.append(flux_of(g, w))
+    def run_plain(i):
+        g = GpuSim(specs[i])
+        g.step(stream[i].steps)
+        f = flux_of(g, made[i])
         g.close()
-        service.append(time.perf_counter() - t0)
-    seq_rate = sum(work) / sum(service) / 1e9
-    gap = float(np.mean(service)) / load
+        return f
+
+    # 0) calibration: sequential throughput on the first requests
+    torch.cuda.synchronize()
+    ncal = min(8, len(stream))
+    t0 = time.perf_counter()
+    for i in range(ncal):
+        run_plain(i)
+    cal_rate = sum(work[:ncal]) / (time.perf_counter() - t0)
+    gap = float(np.mean(work)) / (load * cal_rate)
     arrivals = [r.arrival_unit * gap for r in stream]
-    # sequential latencies under the same arrivals (a FIFO single server)
-    finish, seq_lat = 0.0, []
-    for a, sv in zip(arrivals, service):
-        finish = max(finish, a) + sv
-        seq_lat.append(finish - a)
-    seq_span = finish - arrivals[0]
+
+    # 1) sequential: one plain simulation at a time, each started no earlier
+    #    than its arrival
+    seq_flux, seq_done = [], []
+    t_start = time.perf_counter()
+    for i, a in enumerate(arrivals):
+        delay = t_start + a - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        seq_flux.append(run_plain(i))
+        seq_done.append(time.perf_counter() - t_start)
+    seq_lat = [d - a for d, a in zip(seq_done, arrivals)]
+    seq_span = max(seq_done) - arrivals[0]
 
     # 2) the request server, requests submitted at their arrival times
     srv = Server(int(budget_gb * 1e9), max_resident=max_resident, quantum_steps=quantum)
     srv_flux = [None] * len(stream)
     done_at = [0.0] * len(stream)
-    t_start = time.perf_counter()
     index = {}
     lock = threading.Lock()
     errors = []
+    t_start = time.perf_counter()
 
     def submitter():
         try:
-            for r, a in zip(stream, arrivals):
+            for i, a in enumerate(arrivals):
                 delay = t_start + a - time.perf_counter()
                 if delay > 0:
                     time.sleep(delay)
-                w = r.make()
-                req = srv.submit(w.sim.spec(), r.steps)
+                req = srv.submit(specs[i], stream[i].steps)
                 with lock:
-                    index[req.ticket] = (r.index, w)
+                    index[req.ticket] = i
         except Exception as e:  # surfaced below
             errors.append(e)
 
     th = threading.Thread(target=submitter)
     th.start()
-    peak_resident = 0
     for _ in range(len(stream)):
         req = srv.next_done(timeout=600.0)
         if req is None:
             raise RuntimeError("serving leg: no request finished within 600 s")
         req.wait()
         with lock:
-            i, w = index[req.ticket]
-        srv_flux[i] = flux_of(req.sim, w)
+            i = index[req.ticket]
+        srv_flux[i] = flux_of(req.sim, made[i])
         done_at[i] = time.perf_counter() - t_start
         req.release()
-        peak_resident = max(peak_resident, srv.stats()["resident"])
     th.join()
     srv.close()
     if errors:
         raise errors[0]
-    # 3) sustained capacity: the whole stream submitted at once
-    model_bytes = 0.0
-    srv = Server(int(budget_gb * 1e9), max_resident=max_resident, quantum_steps=quantum)
-    t0 = time.perf_counter()
-    pending = []
-    for r in stream:
-        spec = r.make().sim.spec()
-        pending.append(srv.submit(spec, r.steps))
-    for _ in stream:
-        req = srv.next_done(timeout=600.0)
-        if req is None:
-            raise RuntimeError("serving leg: no request finished within 600 s")
-        req.wait()
-        model_bytes += req.sim.model_bytes_per_step() * req.steps
-        req.release()
-    sat_span = time.perf_counter() - t0
-    srv.close()
-    peak_gbs, _ = measured_peaks()
     srv_lat = [d - a for d, a in zip(done_at, arrivals)]
     srv_span = max(done_at) - arrivals[0]
     diff = max(float(np.max(np.abs(a - b)) / max(float(np.max(np.abs(b))), 1e-300))
                for a, b in zip(srv_flux, seq_flux))
     lat = lambda v: {"p50": _pct(v, 50), "p95": _pct(v, 95), "p99": _pct(v, 99), "max": max(v)}
-    return {
+    total = float(sum(work))
+    out = {
         "requests": len(stream), "seed": seed, "budget_gb": budget_gb, "max_resident": max_resident,
         "quantum_steps": quantum, "offered_load_vs_sequential": load, "mean_interarrival_s": gap,
-        "cell_updates": int(sum(work)),
-        "server": {"gcell_per_s": sum(work) / srv_span / 1e9, "latency_s": lat(srv_lat), "makespan_s": srv_span},
-        "sequential": {"gcell_per_s": sum(work) / seq_span / 1e9, "busy_gcell_per_s": seq_rate,
-                       "latency_s": lat(seq_lat), "makespan_s": seq_span,
-                       "mean_service_s": float(np.mean(service))},
-        "saturated": {"gcell_per_s": sum(work) / sat_span / 1e9, "makespan_s": sat_span,
-                      "model_bytes": model_bytes, "achieved_gbs": model_bytes / sat_span / 1e9,
-                      "hbm_frac": model_bytes / sat_span / 1e9 / peak_gbs},
-        "speedup_aggregate": (sum(work) / srv_span) / (sum(work) / seq_span),
-        "capacity_vs_sequential": (sum(work) / sat_span) / (sum(work) / sum(service)),
+        "cell_updates": int(total), "calibration_gcell_per_s": cal_rate / 1e9,
+        "server": {"gcell_per_s": total / srv_span / 1e9, "latency_s": lat(srv_lat), "makespan_s": srv_span},
+        "sequential": {"gcell_per_s": total / seq_span / 1e9, "latency_s": lat(seq_lat), "makespan_s": seq_span,
+                       "how": "one GpuSim at a time in arrival order, started at max(arrival, previous done)"},
+        "speedup_aggregate": seq_span / srv_span,
         "flux_max_rel_diff_served_vs_solo": diff,
     }
+    if not compact:
+        model_bytes = 0.0
+        srv = Server(int(budget_gb * 1e9), max_resident=max_resident, quantum_steps=quantum)
+        t0 = time.perf_counter()
+        for i in range(len(stream)):
+            srv.submit(specs[i], stream[i].steps)
+        for _ in stream:
+            req = srv.next_done(timeout=600.0)
+            if req is None:
+                raise RuntimeError("serving leg: no request finished within 600 s")
+            req.wait()
+            model_bytes += req.sim.model_bytes_per_step() * req.steps
+            req.release()
+        sat_span = time.perf_counter() - t0
+        srv.close()
+        peak_gbs, _ = measured_peaks()
+        out["saturated"] = {"gcell_per_s": total / sat_span / 1e9, "makespan_s": sat_span,
+                            "model_bytes": model_bytes, "achieved_gbs": model_bytes / sat_span / 1e9,
+                            "hbm_frac": model_bytes / sat_span / 1e9 / peak_gbs}
+        out["capacity_vs_sequential"] = (total / sat_span) / (total / seq_span)
+    return out
 
 
 def run_serving(args, world=1, rank=0, local_rank=0):
@@ -476,6 +627,8 @@ def run_serving(args, world=1, rank=0, local_rank=0):
 
         total = {}
         for leg in ("server", "sequential", "saturated"):
+            if leg not in res:
+                continue
             span = max_over_ranks(res[leg]["makespan_s"], dist)
             t = torch.tensor([float(res["cell_updates"])], dtype=torch.float64)
             dist.all_reduce(t)
@@ -586,6 +739,9 @@ def main(argv=None):
     ap.add_argument("--no-flux-check", action="store_true", help="skip the FP32-vs-FP64 flux leg")
     ap.add_argument("--serve-only", action="store_true", help="run only the serving-stream leg")
     ap.add_argument("--serve-requests", type=int, default=512)
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving leg of the default line")
+    ap.add_argument("--serve-requests-default", type=int, default=64,
+                    help="requests of the serving leg in the default line")
     ap.add_argument("--adjoint-only", action="store_true", help="run only the waveguide-bend adjoint leg")
     ap.add_argument("--adjoint-steps", type=int, default=6000)
     ap.add_argument("--adjoint-scale", type=float, default=1.0)
