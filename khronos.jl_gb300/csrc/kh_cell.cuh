@@ -87,6 +87,152 @@ __device__ __forceinline__ void wrap_pre_chi3(const HalfStepParams<T>& p, long l
   }
 }
 
+// Source term S of one cell for this half-step (update_source!,
+// Sources.jl:346-357): S_c = Σ real(f(t)·amplitude) over the cell's entries of
+// component c, in entry order; hasS[c] marks components with an entry.
+template <typename T, bool H>
+__device__ __forceinline__ void source_terms(const HalfStepParams<T>& p, uint32_t cls, T (&S)[3],
+                                             bool (&hasS)[3]) {
+  S[0] = S[1] = S[2] = T(0);
+  hasS[0] = hasS[1] = hasS[2] = false;
+  if (!p.sources_active || !(cls & (H ? kHasSrcH : kHasSrcE))) return;
+  const int slot = int(cls >> kSlotShift);
+  const bool slot_ok = KH_IN(slot + 1, p.n_slots + 1, 1001);
+  const int e1 = slot_ok ? p.slot_off[slot + 1] : 0;
+  for (int e = slot_ok ? p.slot_off[slot] : 0; e < e1; ++e) {
+    if (!KH_IN(e, p.n_ent, 1002)) break;
+    const int c = p.ent_comp[e] - (H ? 3 : 0);  // entries carry components 0..5
+    const Cplx<T> am = p.ent_amp[e];
+    if (!KH_IN(p.ent_src[e], p.n_src, 1003)) continue;
+    const Cplx<T> fv = p.f_now[p.ent_src[e]];
+    const T v = fv.re * am.re - fv.im * am.im;  // real(f(t) · amplitude)
+    if (c == 0) { S[0] += v; hasS[0] = true; }
+    else if (c == 1) { S[1] += v; hasS[1] = true; }
+    else if (c == 2) { S[2] += v; hasS[2] = true; }
+  }
+}
+
+// Source cell q of a LEAN launch, after the kernel stored its B|D update T
+// (the cell has no W stage for a sourced component, which the host checks
+// before choosing LEAN): O = m⁻¹·(T + S) as update_field_generic forms it
+// (net = T; net += S; A = m⁻¹·net, Helpers.jl:329-347).  T is read back from
+// the state array this thread just wrote; m⁻¹ of component c from *m[c]
+// (per-voxel values, in shared or global memory) or the scalar (m[c] null).
+// The general case: any number of entries per cell.
+template <typename T, bool H>
+__device__ __noinline__ void lean_source_cell(const HalfStepParams<T>& p, long long q, uint32_t cls,
+                                              const T* m0, const T* m1, const T* m2) {
+  T S[3];
+  bool hasS[3];
+  source_terms<T, H>(p, cls, S, hasS);
+  if (!KH_IN(q, p.total, 1009)) return;
+  const T* m[3] = {m0, m1, m2};
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    if (hasS[c] && p.Ts[c]) {
+      T net = p.Ts[c][q];
+      net += S[c];
+      const T mc = m[c] ? *m[c] : p.m_scalar;
+      p.O[c][q] = mc * net;
+    }
+}
+
+// Source cell q of a LEAN launch whose slot has a single entry (the common
+// case): one load of the packed entry (prefetched into L1 a plane ahead) and
+// the time factor from shared memory (`fsm`, or global memory when null);
+// O = m⁻¹·(T + S) with T = t0..t2, the cell's B|D state just computed, exactly
+// as lean_source_cell forms it.  Returns false, writing nothing, when the slot
+// has several entries.
+template <typename T, bool H>
+__device__ __noinline__ bool lean_source_packed(const HalfStepParams<T>& p, long long q, uint32_t cls, T t0, T t1,
+                                                T t2, const T* m0, const T* m1, const T* m2, const Cplx<T>* fsm) {
+  const int slot = int(cls >> kSlotShift);
+  if (!KH_IN(slot, p.n_slots, 1011)) return true;
+  const SlotPack<T> pk = p.slot_pack[slot];
+  const int c = pk.comp - (H ? 3 : 0);
+  if (pk.src < 0) return false;
+  if (c < 0 || c > 2 || !KH_IN(pk.src, p.n_src, 1012) || !KH_IN(q, p.total, 1013)) return true;
+  const Cplx<T> f = fsm ? fsm[pk.src] : p.f_now[pk.src];
+  T S = T(0);
+  S += f.re * pk.amp.re - f.im * pk.amp.im;  // real(f(t) · amplitude)
+  T net = c == 0 ? t0 : (c == 1 ? t1 : t2);
+  net += S;
+  const T* mp = c == 0 ? m0 : (c == 1 ? m1 : m2);
+  const T mc = mp ? *mp : p.m_scalar;
+  p.O[c][q] = mc * net;
+  return true;
+}
+
+// Kahan-compensated DFT accumulation of one value into one accumulator
+// (update_dft_monitor!, Monitors.jl:361-379: F += Δt·exp(i2πft)·field; the
+// phase `ph` carries Δt).  Every product and sum is separately rounded
+// (no contraction into FMAs), so the separate DFT kernel and the pass folded
+// into the half-step kernel give identical bits.
+__device__ __forceinline__ void dft_accumulate(Cplx<float>* F, Cplx<float>* C, long long t, Cplx<float> ph,
+                                               float v) {
+  Cplx<float> acc = F[t];
+  if (C) {
+    Cplx<float> c = C[t];
+    const float yr = __fsub_rn(__fmul_rn(ph.re, v), c.re);
+    const float yi = __fsub_rn(__fmul_rn(ph.im, v), c.im);
+    const float tr = __fadd_rn(acc.re, yr);
+    const float ti = __fadd_rn(acc.im, yi);
+    c.re = __fsub_rn(__fsub_rn(tr, acc.re), yr);
+    c.im = __fsub_rn(__fsub_rn(ti, acc.im), yi);
+    acc.re = tr;
+    acc.im = ti;
+    C[t] = c;
+  } else {
+    acc.re = __fadd_rn(acc.re, __fmul_rn(ph.re, v));
+    acc.im = __fadd_rn(acc.im, __fmul_rn(ph.im, v));
+  }
+  F[t] = acc;
+}
+
+__device__ __forceinline__ void dft_accumulate(Cplx<double>* F, Cplx<double>* C, long long t, Cplx<double> ph,
+                                               double v) {
+  Cplx<double> acc = F[t];
+  if (C) {
+    Cplx<double> c = C[t];
+    const double yr = __dsub_rn(__dmul_rn(ph.re, v), c.re);
+    const double yi = __dsub_rn(__dmul_rn(ph.im, v), c.im);
+    const double tr = __dadd_rn(acc.re, yr);
+    const double ti = __dadd_rn(acc.im, yi);
+    c.re = __dsub_rn(__dsub_rn(tr, acc.re), yr);
+    c.im = __dsub_rn(__dsub_rn(ti, acc.im), yi);
+    acc.re = tr;
+    acc.im = ti;
+    C[t] = c;
+  } else {
+    acc.re = __dadd_rn(acc.re, __dmul_rn(ph.re, v));
+    acc.im = __dadd_rn(acc.im, __dmul_rn(ph.im, v));
+  }
+  F[t] = acc;
+}
+
+// DFT monitors folded into a half-step (update_dft_monitor!,
+// Monitors.jl:361-379): cell (i, j, k), whose updated components are o0..o2,
+// accumulates into every monitor of `mask` whose box holds it, at the index
+// the separate DFT kernel would use.
+template <typename T>
+__device__ __noinline__ void dft_fold_cell(const HalfStepParams<T>& p, uint32_t mask, int i, int j, int k,
+                                           T o0, T o1, T o2) {
+  while (mask) {
+    const int m = __ffs(mask) - 1;
+    mask &= mask - 1;
+    const FoldMonitor<T>& fm = p.fold[m];
+    if (i < fm.lo[0] || i >= fm.hi[0] || j < fm.lo[1] || j >= fm.hi[1] || k < fm.lo[2] || k >= fm.hi[2]) continue;
+    const long long d0 = fm.hi[0] - fm.lo[0], d1 = fm.hi[1] - fm.lo[1], d2 = fm.hi[2] - fm.lo[2];
+    const long long ncell = d0 * d1 * d2;
+    const long long cell = ((long long)(k - fm.lo[2]) * d1 + (j - fm.lo[1])) * d0 + (i - fm.lo[0]);
+    const T v = fm.comp == 0 ? o0 : (fm.comp == 1 ? o1 : o2);
+    for (int f = 0; f < fm.nf; ++f) {
+      if (!KH_IN(f * ncell + cell, ncell * fm.nf, 1010)) break;
+      dft_accumulate(fm.F, fm.C, f * ncell + cell, fm.phase[f], v);
+    }
+  }
+}
+
 // Update of one cell that carries a source, χ3, a pole or a material
 // conductivity (and may also sit in a CPML region).  t/u/w are the cell's B|D
 // state and CPML U/W values (loaded and stored by the caller), m its μ⁻¹|ε⁻¹,
@@ -291,12 +437,4 @@ __device__ __forceinline__ void pml_cell(const bool (&f)[3], const AxisCoef<T> (
   }
 }
 
-// One fused half-step.  H = true: B/H from curl E; H = false: D/E from curl H.
-// FULL = false (LEAN) compiles only plain and CPML cells; cells marked special
-// there are source cells, updated as B|D-keeping cells (O = m⁻¹·T) and given
-// their source term by source_fix_kernel when sources are active.
-//
-// The z march is software-pipelined: every load of plane k+1 (fields,
-// neighbours, CPML state, cell classes) is issued before plane k is computed
-// and stored, so each warp keeps two planes of memory traffic in flight.
 }  // namespace kh

@@ -236,6 +236,17 @@ __device__ __forceinline__ void compute_plane(const HalfStepParams<T>& p, PlaneL
         }
       }
     }
+    if constexpr (!FULL) {
+      // LEAN source cells: the term is added after the stores (lean_source_cell)
+      if (p.sources_active) {
+        const bool pervox = p.m_inv[0] != nullptr;
+#pragma unroll
+        for (int v = 0; v < VN; ++v)
+          if ((L.cls[v] & (H ? kHasSrcH : kHasSrcE)) && x0 + v < p.nx)
+            lean_source_cell<T, H>(p, q + v, L.cls[v], pervox ? p.m_inv[0] + q + v : nullptr,
+                                   pervox ? p.m_inv[1] + q + v : nullptr, pervox ? p.m_inv[2] + q + v : nullptr);
+      }
+    }
   }
   // rotate: H half keeps A(k+1) as the next plane's A(k); E half keeps
   // A(k) as the next plane's A(k-1)
@@ -245,8 +256,8 @@ __device__ __forceinline__ void compute_plane(const HalfStepParams<T>& p, PlaneL
 
 // One fused half-step.  H = true: B/H from curl E; H = false: D/E from curl H.
 // FULL = false (LEAN) compiles only plain and CPML cells; cells marked special
-// there are source cells, updated as B|D-keeping cells (O = m⁻¹·T) and given
-// their source term by source_fix_kernel when sources are active.
+// there are source cells, updated as B|D-keeping cells with their source term
+// added after the stores of each plane (lean_source_cell).
 //
 // The z march is double-buffered with a prefetch distance of two planes: the
 // loads of plane k+2 are issued as soon as plane k has been consumed, so each
@@ -325,47 +336,6 @@ void launch_half_step(bool h_half, const HalfStepParams<T>& p, void* stream) {
   }
 }
 
-// Source term of the cells a LEAN half-step updated as B|D-keeping cells:
-// O = m⁻¹·(T + S), the same arithmetic update_field_generic performs
-// (net = T; net += S; A = m⁻¹·net, Helpers.jl:329-347).
-template <typename T>
-__global__ void source_fix_kernel(const SourceFixParams<T> p) {
-  const int slot = blockIdx.x * blockDim.x + threadIdx.x;
-  if (slot >= p.nslots) return;
-  const long long q = p.slot_cell[slot];
-  if (!KH_IN(q, p.total, 3022)) return;
-  const int base = p.h_half ? 3 : 0;
-  T S[3] = {T(0), T(0), T(0)};
-  bool has[3] = {false, false, false};
-  for (int e = p.slot_off[slot]; e < p.slot_off[slot + 1]; ++e) {
-    if (!KH_IN(e, p.n_ent, 3023)) break;
-    const int c = p.ent_comp[e] - base;
-    if (c < 0 || c > 2) continue;
-    const Cplx<T> a = p.ent_amp[e];
-    if (!KH_IN(p.ent_src[e], p.n_src, 3024)) continue;
-    const Cplx<T> f = p.f_now[p.ent_src[e]];
-    const T v = f.re * a.re - f.im * a.im;
-    if (c == 0) { S[0] += v; has[0] = true; }
-    else if (c == 1) { S[1] += v; has[1] = true; }
-    else { S[2] += v; has[2] = true; }
-  }
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    if (!has[c]) continue;
-    const T m = p.m_inv[c] ? p.m_inv[c][q] : p.m_scalar;
-    T net = p.Ts[c][q];
-    net += S[c];
-    p.O[c][q] = m * net;
-  }
-}
-
-template <typename T>
-void launch_source_fix(const SourceFixParams<T>& p, void* stream) {
-  if (p.nslots <= 0) return;
-  const int threads = 128;
-  source_fix_kernel<T><<<(p.nslots + threads - 1) / threads, threads, 0, static_cast<cudaStream_t>(stream)>>>(p);
-}
-
 // ---------------------------------------------------------------------------
 // Periodic wrap.  blockIdx.y = 3·axis + component; threads stride over the
 // face's (n_t1 × n_t2) cells; each copies both directions of one cell.
@@ -420,25 +390,7 @@ __global__ void dft_kernel(const DftParams<T> p) {
     const long long q = p.origin + (long long)(p.start[2] + kk) * p.plane +
                         (long long)(p.start[1] + jj) * p.pitch + (p.start[0] + i);
     if (!KH_IN(q, p.total, 3025)) continue;
-    const T v = p.field[q];
-    const Cplx<T> ph = p.phase[f];
-    Cplx<T> acc = p.F[t];
-    if (p.comp) {
-      Cplx<T> c = p.comp[t];
-      const T yr = ph.re * v - c.re;
-      const T yi = ph.im * v - c.im;
-      const T tr = acc.re + yr;
-      const T ti = acc.im + yi;
-      c.re = (tr - acc.re) - yr;
-      c.im = (ti - acc.im) - yi;
-      acc.re = tr;
-      acc.im = ti;
-      p.comp[t] = c;
-    } else {
-      acc.re = acc.re + ph.re * v;
-      acc.im = acc.im + ph.im * v;
-    }
-    p.F[t] = acc;
+    dft_accumulate(p.F, p.comp, t, p.phase[f], p.field[q]);
   }
 }
 
@@ -578,8 +530,6 @@ template void launch_half_step<float>(bool, const HalfStepParams<float>&, void*)
 template void launch_half_step<double>(bool, const HalfStepParams<double>&, void*);
 template void launch_wrap<float>(const WrapParams<float>&, void*);
 template void launch_wrap<double>(const WrapParams<double>&, void*);
-template void launch_source_fix<float>(const SourceFixParams<float>&, void*);
-template void launch_source_fix<double>(const SourceFixParams<double>&, void*);
 template void launch_record<float>(const RecordParams<float>&, void*);
 template void launch_record<double>(const RecordParams<double>&, void*);
 template void launch_dft<float>(const DftParams<float>&, void*);

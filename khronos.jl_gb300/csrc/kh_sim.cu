@@ -591,6 +591,11 @@ class Sim : public SimBase {
       ent_amp_h_ = ent_amp;
       KH_TRY(upload_raw(slot_cell.data(), slot_cell.size() * sizeof(long long), (void**)&slot_cell_));
       nslots_ = int(slot_cell.size());
+      slot_off_h_ = slot_off;
+      ent_src_h_ = ent_src;
+      ent_comp_h_ = ent_comp;
+      std::vector<kh::SlotPack<T>> pack = pack_slots();
+      KH_TRY(upload_raw(pack.data(), pack.size() * sizeof(kh::SlotPack<T>), (void**)&slot_pack_));
     }
     // Cell classes and the per-row-segment plane bitmasks (word (k/64, j, xb),
     // bit k%64), computed on the device from the material arrays and the
@@ -701,6 +706,8 @@ class Sim : public SimBase {
     // register-pipelined one.
     const char* kv = std::getenv("KHRONOS_GB300_KERNEL");
     use_tma_ = !(kv && std::string(kv) == "simt");
+    const char* fv = std::getenv("KHRONOS_GB300_DFT_FOLD");
+    dft_fold_ = !(fv && std::string(fv) == "0");
     if (use_tma_) KH_TRY(build_tma_maps());
     zplanes_ = choose_zplanes();
     if (const char* sv = std::getenv("KHRONOS_GB300_TEST_STALL")) stall_tx_ = std::string(sv) == "1" ? 16u : 0u;
@@ -956,6 +963,10 @@ class Sim : public SimBase {
       if (!amp_new.empty())
         KH_CUDA(cudaMemcpy(ent_amp_, amp_new.data(), amp_new.size() * sizeof(Cplx<T>), cudaMemcpyHostToDevice));
       ent_amp_h_.swap(amp_new);
+      if (slot_pack_) {
+        std::vector<kh::SlotPack<T>> pack = pack_slots();
+        KH_CUDA(cudaMemcpy(slot_pack_, pack.data(), pack.size() * sizeof(kh::SlotPack<T>), cudaMemcpyHostToDevice));
+      }
     }
     if (table) {
       s.table.assign(size_t(2 * table_len), std::complex<T>(T(0), T(0)));
@@ -1294,6 +1305,17 @@ class Sim : public SimBase {
     return KH_OK;
   }
 
+  // Single-entry slots packed for one load (src = -1: several entries).
+  std::vector<kh::SlotPack<T>> pack_slots() const {
+    std::vector<kh::SlotPack<T>> pack(slot_off_h_.empty() ? 0 : slot_off_h_.size() - 1);
+    for (size_t sl = 0; sl < pack.size(); ++sl) {
+      const int e0 = slot_off_h_[sl], e1 = slot_off_h_[sl + 1];
+      if (e1 - e0 == 1) pack[sl] = {ent_src_h_[e0], ent_comp_h_[e0], ent_amp_h_[e0]};
+      else pack[sl] = {-1, -1, {T(0), T(0)}};
+    }
+    return pack;
+  }
+
   bool has_eps(int c) const { return !eps_h_[c].empty() || att_eps_[c].ptr; }
   bool has_mu(int c) const { return !mu_h_[c].empty() || att_mu_[c].ptr; }
 
@@ -1425,8 +1447,31 @@ class Sim : public SimBase {
     const bool ref_cpu = d_.semantics == KH_SEM_REFERENCE_CPU;
     const bool full_h_base = msb || (ref_cpu && special_in_region_[1]);
     const bool full_e_base = msd || chi3_ != nullptr || !poles_d_.empty() || (ref_cpu && special_in_region_[0]);
-    kh::SourceFixParams<T> fh = fix_params(true), fe = fix_params(false);
     const kh::WrapParams<T> wh = wrap_params(true), we = wrap_params(false);
+    // DFT monitors of one half-step: those foldable into the launch go into
+    // its monitor table, the rest get the separate DFT kernel afterwards.
+    std::vector<std::pair<int, size_t>> rest;
+    auto fold_dft = [&](kh::HalfStepParams<T>& hp, const std::vector<std::pair<int, size_t>>& dms) {
+      hp.n_fold = 0;
+      rest.clear();
+      for (auto& dm : dms) {
+        if (fold_ok(dm.first) && hp.n_fold < kh::kMaxFoldMonitors) {
+          const Mon& m = mons_[dm.first];
+          kh::FoldMonitor<T>& fm = hp.fold[hp.n_fold++];
+          fm.comp = m.comp % 3;
+          for (int a = 0; a < 3; ++a) {
+            fm.lo[a] = m.start[a];
+            fm.hi[a] = m.start[a] + m.dims[a];
+          }
+          fm.nf = m.nf;
+          fm.phase = dtab + dm.second;
+          fm.F = m.F;
+          fm.C = m.C;
+        } else {
+          rest.push_back(dm);
+        }
+      }
+    };
     auto issue_all = [&](cudaStream_t st) {
     for (int s = 0; s < nb; ++s) {
       const StepPlan& P = plan[s];
@@ -1434,41 +1479,33 @@ class Sim : public SimBase {
       ph.f_now = dtab + P.fH;
       const bool src_h = P.sa && has_src_[1];
       ph.full = (full_h_base || (src_h && !src_lean_ok_[1])) ? 1 : 0;
+      fold_dft(ph, P.dftH);
       mark(s, 0);
       if (use_tma_) kh::launch_half_step_tma<T>(true, ph, maps_h_, st);
       else kh::launch_half_step<T>(true, ph, st);
       ++launches;
-      if (src_h && !ph.full) {
-        fh.f_now = dtab + P.fH;
-        kh::launch_source_fix<T>(fh, st);
-        ++launches;
-      }
       if (d_.periodic) {
         kh::launch_wrap<T>(wh, st);
         ++launches;
       }
       mark(s, 1);
-      for (auto& dm : P.dftH) launch_dft_for(dm.first, dtab + dm.second, st);
+      for (auto& dm : rest) launch_dft_for(dm.first, dtab + dm.second, st);
       record_histories(true, timestep_ + s, st);
       mark(s, 2);
       pe.sources_active = P.sa ? 1 : 0;
       pe.f_now = dtab + P.fE;
       const bool src_e = P.sa && has_src_[0];
       pe.full = (full_e_base || (src_e && !src_lean_ok_[0])) ? 1 : 0;
+      fold_dft(pe, P.dftE);
       if (use_tma_) kh::launch_half_step_tma<T>(false, pe, maps_e_, st);
       else kh::launch_half_step<T>(false, pe, st);
       ++launches;
-      if (src_e && !pe.full) {
-        fe.f_now = dtab + P.fE;
-        kh::launch_source_fix<T>(fe, st);
-        ++launches;
-      }
       if (d_.periodic) {
         kh::launch_wrap<T>(we, st);
         ++launches;
       }
       mark(s, 3);
-      for (auto& dm : P.dftE) launch_dft_for(dm.first, dtab + dm.second, st);
+      for (auto& dm : rest) launch_dft_for(dm.first, dtab + dm.second, st);
       record_histories(false, timestep_ + s, st);
       mark(s, 4);
     }
@@ -1627,6 +1664,19 @@ class Sim : public SimBase {
     return st;
   }
 
+  // A monitor is accumulated inside the TMA half-step launch when its box
+  // lies in the computed range 0..n-1 of every axis (a box reaching the
+  // staggered wall layer n keeps the separate kernel, which reads that layer
+  // after the periodic wrap has filled it).  KHRONOS_GB300_DFT_FOLD=0 keeps
+  // every monitor on the separate kernel.
+  bool fold_ok(int mi) const {
+    if (!use_tma_ || !dft_fold_) return false;
+    const Mon& m = mons_[mi];
+    for (int a = 0; a < 3; ++a)
+      if (m.start[a] < 0 || m.start[a] + m.dims[a] > n_[a]) return false;
+    return true;
+  }
+
   void launch_dft_for(int mi, const Cplx<T>* phase, cudaStream_t stream) {
     const Mon& m = mons_[mi];
     kh::DftParams<T> p;
@@ -1731,28 +1781,6 @@ class Sim : public SimBase {
     return KH_OK;
   }
 
-  kh::SourceFixParams<T> fix_params(bool h) const {
-    kh::SourceFixParams<T> f;
-    std::memset(&f, 0, sizeof(f));
-    f.nslots = nslots_;
-    f.n_ent = int(ent_amp_h_.size());
-    f.n_src = nsrc_;
-    f.total = total_;
-    f.slot_cell = slot_cell_;
-    f.slot_off = slot_off_;
-    f.ent_src = ent_src_;
-    f.ent_comp = ent_comp_;
-    f.ent_amp = ent_amp_;
-    for (int c = 0; c < 3; ++c) {
-      f.O[c] = h ? H_[c] : E_[c];
-      f.Ts[c] = h ? B_[c] : D_[c];
-      f.m_inv[c] = h ? mu_[c] : eps_[c];
-    }
-    f.m_scalar = h ? T(d_.mu_inv) : T(d_.eps_inv);
-    f.h_half = h ? 1 : 0;
-    return f;
-  }
-
   kh::WrapParams<T> wrap_params(bool h) const {
     kh::WrapParams<T> w;
     std::memset(&w, 0, sizeof(w));
@@ -1810,6 +1838,7 @@ class Sim : public SimBase {
     p.stall_tx = stall_tx_;
     p.periodic = h ? 0u : uint32_t(d_.periodic);
     p.slot_off = slot_off_;
+    p.slot_pack = slot_pack_;
     p.ent_src = ent_src_;
     p.ent_comp = ent_comp_;
     p.ent_amp = ent_amp_;
@@ -1879,6 +1908,7 @@ class Sim : public SimBase {
   // bytes that never arrive and give up (tests of the timeout status only)
   uint32_t stall_tx_ = 0;
   bool use_tma_ = true;
+  bool dft_fold_ = true;
   int zplanes_ = 10;
   int tma_slots_ = 0;  // SMs × resident TMA-kernel CTAs per SM
   kh::TmaMaps maps_h_, maps_e_;
@@ -1893,6 +1923,8 @@ class Sim : public SimBase {
   uint64_t *tbits_e_ = nullptr, *tbits_h_ = nullptr;
   int *slot_off_ = nullptr, *ent_src_ = nullptr, *ent_comp_ = nullptr;
   Cplx<T>* ent_amp_ = nullptr;
+  kh::SlotPack<T>* slot_pack_ = nullptr;
+  std::vector<int> slot_off_h_, ent_src_h_, ent_comp_h_;  // host copies of the source table
   std::vector<Cplx<T>> ent_amp_h_;  // host copy of ent_amp_
   // per source: (amplitude element index, entry index) of every injected cell
   std::vector<std::vector<std::pair<long long, int>>> src_ent_;

@@ -171,6 +171,9 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
     for (int st = 0; st < kTmaStages; ++st) mbar_init(&bars[st], 1);
     mbar_fence_init();
   }
+  // LEAN launches with sources: this half-step's time factors in shared memory
+  __shared__ Cplx<T> s_fnow[kSmemSources];
+  if (!FULL && p.sources_active && p.n_src <= kSmemSources && tid < p.n_src) s_fnow[tid] = p.f_now[tid];
   __syncthreads();
   // tile-wide CPML flags along x and y: which CPML state tiles a plane needs
   const bool tfx = x_tile < p.pml_lo[0] || x_tile + kTmaX > p.nx - p.pml_hi[0];
@@ -436,6 +439,49 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
             for (int cc = 0; cc < 3; ++cc) p.O[cc][q + v] = O[cc][v];
           }
       }
+      if constexpr (!FULL) {
+        // LEAN source cells: O = m⁻¹·(T + S) (update_field_generic,
+        // Helpers.jl:329-347), applied after the stores so the rare source
+        // path adds nothing to the registers of the update above: one load of
+        // the cell's packed entry (prefetched into L1 a plane ahead) and its
+        // time factor from shared memory; cells with several entries take the
+        // general entry loop.
+        if (p.sources_active) {
+#pragma unroll
+          for (int v = 0; v < VN; ++v) {
+            if (!((cur.cls[v] & (H ? kHasSrcH : kHasSrcE)) && x0 + v < p.nx)) continue;
+            const T* m0 = pervox ? Ms + ob + v : nullptr;
+            const T* m1 = pervox ? Ms + G::O_ELEMS + ob + v : nullptr;
+            const T* m2 = pervox ? Ms + 2 * G::O_ELEMS + ob + v : nullptr;
+            if (!lean_source_packed<T, H>(p, q + v, cur.cls[v], cur.t[0][v], cur.t[1][v], cur.t[2][v], m0, m1, m2,
+                                          p.n_src <= kSmemSources ? s_fnow : nullptr))
+              lean_source_cell<T, H>(p, q + v, cur.cls[v], m0, m1, m2);
+          }
+        }
+      }
+      // DFT monitors of this step (decimation steps only) whose box meets this
+      // row segment of plane k, on the values just stored (a LEAN source
+      // cell's final value is the one its source pass wrote)
+      uint32_t fold_mask = 0;
+      for (int m = 0; m < p.n_fold; ++m) {
+        const FoldMonitor<T>& fm = p.fold[m];
+        if (fm.lo[0] < x_tile + kTmaX && fm.hi[0] > x_tile && fm.lo[1] <= j && fm.hi[1] > j && fm.lo[2] <= k &&
+            fm.hi[2] > k)
+          fold_mask |= 1u << m;
+      }
+      if (fold_mask) {
+#pragma unroll
+        for (int v = 0; v < VN; ++v) {
+          const int i = x0 + v;
+          if (i >= p.nx) continue;
+          T o[3] = {O[0][v], O[1][v], O[2][v]};
+          if (!FULL && p.sources_active && (cur.cls[v] & (H ? kHasSrcH : kHasSrcE)) && KH_IN(q + v, p.total, 2021)) {
+#pragma unroll
+            for (int cc = 0; cc < 3; ++cc) o[cc] = p.O[cc][q + v];
+          }
+          dft_fold_cell<T>(p, fold_mask, i, j, k, o[0], o[1], o[2]);
+        }
+      }
     }
     // every thread is done with load c (H: current, E: z neighbour); its
     // stage takes load c + kTmaStages
@@ -450,6 +496,18 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
     if (tid == 0 && c + kTmaStages <= N) {
       fence_proxy_async();
       issue(c + kTmaStages);
+    }
+    if constexpr (!FULL) {
+      // the next plane's packed source entries into L1 (its cell classes
+      // arrived during this plane)
+      if (p.sources_active && c + 1 < N) {
+#pragma unroll
+        for (int v = 0; v < VN; ++v)
+          if (nxt.cls[v] & (H ? kHasSrcH : kHasSrcE)) {
+            const int slot = int(nxt.cls[v] >> kSlotShift);
+            if (KH_IN(slot, p.n_slots, 2025)) asm volatile("prefetch.global.L1 [%0];" ::"l"(p.slot_pack + slot));
+          }
+      }
     }
     cur = nxt;
   }

@@ -314,6 +314,32 @@ def test_step_graphs_are_invisible(kh, gpu_lib, dtype, monkeypatch):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("dtype,semantics", [("f32", "cpml"), ("f64", "cpml"), ("f32", "reference_cpu")])
+def test_dft_fold_is_invisible(kh, gpu_lib, dtype, semantics, monkeypatch):
+    """DFT monitors accumulated inside the half-step launch give the same bits
+    as the separate DFT kernel (KHRONOS_GB300_DFT_FOLD=0): the waveguide's two
+    flux planes (Ey, Ez, Hy, Hz), with the source active and after its cutoff,
+    in both CPML semantics."""
+    from khronos_gb300 import configs
+    from khronos_gb300.device import GpuSim
+
+    w = configs.waveguide(dtype=dtype, scale=0.25)
+    w.sim.semantics = semantics
+    spec = w.sim.spec()
+    steps = 700 if semantics == "cpml" else 60
+    out = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("KHRONOS_GB300_DFT_FOLD", mode)
+        g = GpuSim(spec, lib=gpu_lib)
+        g.step(steps)
+        out[mode] = [g.field(c) for c in range(6)] + [g.dft(m) for m in range(len(spec.monitors))]
+        g.close()
+    assert any(np.any(d != 0) for d in out["1"][6:])
+    for a, b in zip(out["0"], out["1"]):
+        assert np.array_equal(a, b)
+
+
+@pytest.mark.gpu
 def test_run_benchmark(kh, gpu_lib):
     """run_benchmark(sim, until) mirrors the reference: steps until times and
     returns a positive MCells/s rate."""
