@@ -137,29 +137,29 @@ __device__ __noinline__ void lean_source_cell(const HalfStepParams<T>& p, long l
     }
 }
 
-// Source cell q of a LEAN launch whose slot has a single entry (the common
-// case): one load of the packed entry (prefetched into L1 a plane ahead) and
-// the time factor from shared memory (`fsm`, or global memory when null);
-// O = m⁻¹·(T + S) with T = t0..t2, the cell's B|D state just computed, exactly
-// as lean_source_cell forms it.  Returns false, writing nothing, when the slot
-// has several entries.
+// Source term of a single-entry LEAN source cell, in place on its freshly
+// updated values: O_c = m⁻¹_c·(T_c + S) for the entry's component c, the
+// arithmetic of lean_source_cell.  One load of the packed entry and the time
+// factor from shared memory (`fsm`, or global memory when null).  Returns
+// false, changing nothing, when the cell's slot has several entries.
 template <typename T, bool H>
-__device__ __noinline__ bool lean_source_packed(const HalfStepParams<T>& p, long long q, uint32_t cls, T t0, T t1,
-                                                T t2, const T* m0, const T* m1, const T* m2, const Cplx<T>* fsm) {
+__device__ __forceinline__ bool lean_source_inline(const HalfStepParams<T>& p, uint32_t cls, const T (&m)[3],
+                                                   const T (&t)[3], T (&O)[3], const Cplx<T>* fsm) {
   const int slot = int(cls >> kSlotShift);
-  if (!KH_IN(slot, p.n_slots, 1011)) return true;
+  if (!KH_IN(slot, p.n_slots, 1014)) return true;
   const SlotPack<T> pk = p.slot_pack[slot];
-  const int c = pk.comp - (H ? 3 : 0);
   if (pk.src < 0) return false;
-  if (c < 0 || c > 2 || !KH_IN(pk.src, p.n_src, 1012) || !KH_IN(q, p.total, 1013)) return true;
+  const int c = pk.comp - (H ? 3 : 0);
+  if (c < 0 || c > 2 || !KH_IN(pk.src, p.n_src, 1015)) return true;
   const Cplx<T> f = fsm ? fsm[pk.src] : p.f_now[pk.src];
   T S = T(0);
   S += f.re * pk.amp.re - f.im * pk.amp.im;  // real(f(t) · amplitude)
-  T net = c == 0 ? t0 : (c == 1 ? t1 : t2);
+  T net = c == 0 ? t[0] : (c == 1 ? t[1] : t[2]);
   net += S;
-  const T* mp = c == 0 ? m0 : (c == 1 ? m1 : m2);
-  const T mc = mp ? *mp : p.m_scalar;
-  p.O[c][q] = mc * net;
+  const T val = (c == 0 ? m[0] : (c == 1 ? m[1] : m[2])) * net;
+  if (c == 0) O[0] = val;
+  else if (c == 1) O[1] = val;
+  else O[2] = val;
   return true;
 }
 

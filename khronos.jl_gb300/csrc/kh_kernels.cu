@@ -264,7 +264,7 @@ __device__ __forceinline__ void compute_plane(const HalfStepParams<T>& p, PlaneL
 // warp keeps about two planes of memory traffic in flight.
 template <typename T, int VN, bool H, bool CPML, bool FULL>
 __global__ void __launch_bounds__(32 * kBlockY, sizeof(T) == 4 ? kMinBlocks : 2)
-    half_step_kernel(const HalfStepParams<T> p) {
+    half_step_kernel(const __grid_constant__ HalfStepParams<T> p) {
   const int lane = threadIdx.x;
   const int j = blockIdx.y * kBlockY + threadIdx.y;
   if (j >= p.ny) return;  // warp-uniform: blockDim.x == 32

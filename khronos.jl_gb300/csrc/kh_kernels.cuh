@@ -193,6 +193,9 @@ struct HalfStepParams {
   // exchanges E before the Kerr correction); the wrap kernel skips those cells.
   uint32_t periodic;
 
+  // Work beyond the update in this launch (TMA-staged kernel): 1 selects the
+  // instantiation with LEAN source cells and the folded DFT monitors below.
+  int ex;
   // DFT monitors of this half folded into the launch (TMA-staged kernel)
   int n_fold;
   FoldMonitor<T> fold[kMaxFoldMonitors];

@@ -1480,6 +1480,7 @@ class Sim : public SimBase {
       const bool src_h = P.sa && has_src_[1];
       ph.full = (full_h_base || (src_h && !src_lean_ok_[1])) ? 1 : 0;
       fold_dft(ph, P.dftH);
+      ph.ex = ((src_h && !ph.full) || ph.n_fold > 0) ? 1 : 0;
       mark(s, 0);
       if (use_tma_) kh::launch_half_step_tma<T>(true, ph, maps_h_, st);
       else kh::launch_half_step<T>(true, ph, st);
@@ -1497,6 +1498,7 @@ class Sim : public SimBase {
       const bool src_e = P.sa && has_src_[0];
       pe.full = (full_e_base || (src_e && !src_lean_ok_[0])) ? 1 : 0;
       fold_dft(pe, P.dftE);
+      pe.ex = ((src_e && !pe.full) || pe.n_fold > 0) ? 1 : 0;
       if (use_tma_) kh::launch_half_step_tma<T>(false, pe, maps_e_, st);
       else kh::launch_half_step<T>(false, pe, st);
       ++launches;

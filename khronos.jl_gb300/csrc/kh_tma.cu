@@ -141,9 +141,12 @@ constexpr int tma_min_blocks() {
   return sizeof(T) == 4 ? (FULL ? kTmaMinBlocks - 1 : kTmaMinBlocks) : 2;
 }
 
-template <typename T, bool H, bool CPML, bool FULL, bool STALL = false>
+// EX: the launch also carries work beyond the half-step update, compiled
+// only into this instantiation so the other launches keep the lean code path:
+// LEAN source cells (O = m⁻¹·(T + S)) and DFT monitors folded into the pass.
+template <typename T, bool H, bool CPML, bool FULL, bool EX, bool STALL = false>
 __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
-    half_step_tma_kernel(const HalfStepParams<T> p, const __grid_constant__ TmaMaps maps) {
+    half_step_tma_kernel(const __grid_constant__ HalfStepParams<T> p, const __grid_constant__ TmaMaps maps) {
   using G = TmaGeom<T>;
   constexpr int VN = 2;
   constexpr int s = H ? 1 : -1;
@@ -172,8 +175,10 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
     mbar_fence_init();
   }
   // LEAN launches with sources: this half-step's time factors in shared memory
-  __shared__ Cplx<T> s_fnow[kSmemSources];
-  if (!FULL && p.sources_active && p.n_src <= kSmemSources && tid < p.n_src) s_fnow[tid] = p.f_now[tid];
+  __shared__ Cplx<T> s_fnow[EX && !FULL ? kSmemSources : 1];
+  if constexpr (EX && !FULL) {
+    if (p.sources_active && p.n_src <= kSmemSources && tid < p.n_src) s_fnow[tid] = p.f_now[tid];
+  }
   __syncthreads();
   // tile-wide CPML flags along x and y: which CPML state tiles a plane needs
   const bool tfx = x_tile < p.pml_lo[0] || x_tile + kTmaX > p.nx - p.pml_hi[0];
@@ -348,6 +353,7 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
       // this thread's two cells have no CPML flag and no special class
       // (measured faster than a warp-uniform decision per row segment)
       bool plain = !(anyfx || fy || fz);
+      uint32_t multi = 0;  // EX: bit v set when cell v's source slot has several entries
 #pragma unroll
       for (int v = 0; v < VN; ++v) plain = plain && !(cur.cls[v] & (H ? kSpecialH : kSpecialE));
       if (plain) {
@@ -357,6 +363,7 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
           for (int v = 0; v < VN; ++v) O[cc][v] = O[cc][v] + m[cc][v] * K[cc][v];
       } else {
         const AxisCoef<T> az = KH_IN(k, p.nz, 2020) ? p.ax[2][k] : AxisCoef<T>{T(0), T(1), T(1), T(1)};
+        multi = 0;
 #pragma unroll
         for (int v = 0; v < VN; ++v) {
           const int i = x0 + v;
@@ -405,6 +412,13 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
                 Oc[cc] = mc[cc] * tc[cc];
               }
             }
+            if constexpr (EX) {
+              // source term of a single-entry cell in place; several entries
+              // after the stores (lean_source_cell)
+              if (special && p.sources_active && (cur.cls[v] & (H ? kHasSrcH : kHasSrcE)) &&
+                  !lean_source_inline<T, H>(p, cur.cls[v], mc, tc, Oc, p.n_src <= kSmemSources ? s_fnow : nullptr))
+                multi |= 1u << v;
+            }
           }
 #pragma unroll
           for (int cc = 0; cc < 3; ++cc) {
@@ -439,47 +453,37 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
             for (int cc = 0; cc < 3; ++cc) p.O[cc][q + v] = O[cc][v];
           }
       }
-      if constexpr (!FULL) {
-        // LEAN source cells: O = m⁻¹·(T + S) (update_field_generic,
-        // Helpers.jl:329-347), applied after the stores so the rare source
-        // path adds nothing to the registers of the update above: one load of
-        // the cell's packed entry (prefetched into L1 a plane ahead) and its
-        // time factor from shared memory; cells with several entries take the
-        // general entry loop.
-        if (p.sources_active) {
+      if constexpr (EX && !FULL) {
+        // source cells whose slot has several entries: the general entry loop,
+        // from the B|D state just stored
+        if (multi) {
 #pragma unroll
-          for (int v = 0; v < VN; ++v) {
-            if (!((cur.cls[v] & (H ? kHasSrcH : kHasSrcE)) && x0 + v < p.nx)) continue;
-            const T* m0 = pervox ? Ms + ob + v : nullptr;
-            const T* m1 = pervox ? Ms + G::O_ELEMS + ob + v : nullptr;
-            const T* m2 = pervox ? Ms + 2 * G::O_ELEMS + ob + v : nullptr;
-            if (!lean_source_packed<T, H>(p, q + v, cur.cls[v], cur.t[0][v], cur.t[1][v], cur.t[2][v], m0, m1, m2,
-                                          p.n_src <= kSmemSources ? s_fnow : nullptr))
-              lean_source_cell<T, H>(p, q + v, cur.cls[v], m0, m1, m2);
-          }
+          for (int v = 0; v < VN; ++v)
+            if (((multi >> v) & 1u) && x0 + v < p.nx) {
+              lean_source_cell<T, H>(p, q + v, cur.cls[v], pervox ? Ms + ob + v : nullptr,
+                                     pervox ? Ms + G::O_ELEMS + ob + v : nullptr,
+                                     pervox ? Ms + 2 * G::O_ELEMS + ob + v : nullptr);
+              if (KH_IN(q + v, p.total, 2021)) {
+#pragma unroll
+                for (int cc = 0; cc < 3; ++cc) O[cc][v] = p.O[cc][q + v];
+              }
+            }
         }
       }
-      // DFT monitors of this step (decimation steps only) whose box meets this
-      // row segment of plane k, on the values just stored (a LEAN source
-      // cell's final value is the one its source pass wrote)
-      uint32_t fold_mask = 0;
-      for (int m = 0; m < p.n_fold; ++m) {
-        const FoldMonitor<T>& fm = p.fold[m];
-        if (fm.lo[0] < x_tile + kTmaX && fm.hi[0] > x_tile && fm.lo[1] <= j && fm.hi[1] > j && fm.lo[2] <= k &&
-            fm.hi[2] > k)
-          fold_mask |= 1u << m;
-      }
-      if (fold_mask) {
+      if constexpr (EX) {
+        // DFT monitors of this step (decimation steps) whose box meets this
+        // row segment of plane k, on the final values of its cells
+        uint32_t fold_mask = 0;
+        for (int m = 0; m < p.n_fold; ++m) {
+          const FoldMonitor<T>& fm = p.fold[m];
+          if (fm.lo[0] < x_tile + kTmaX && fm.hi[0] > x_tile && fm.lo[1] <= j && fm.hi[1] > j && fm.lo[2] <= k &&
+              fm.hi[2] > k)
+            fold_mask |= 1u << m;
+        }
+        if (fold_mask) {
 #pragma unroll
-        for (int v = 0; v < VN; ++v) {
-          const int i = x0 + v;
-          if (i >= p.nx) continue;
-          T o[3] = {O[0][v], O[1][v], O[2][v]};
-          if (!FULL && p.sources_active && (cur.cls[v] & (H ? kHasSrcH : kHasSrcE)) && KH_IN(q + v, p.total, 2021)) {
-#pragma unroll
-            for (int cc = 0; cc < 3; ++cc) o[cc] = p.O[cc][q + v];
-          }
-          dft_fold_cell<T>(p, fold_mask, i, j, k, o[0], o[1], o[2]);
+          for (int v = 0; v < VN; ++v)
+            if (x0 + v < p.nx) dft_fold_cell<T>(p, fold_mask, x0 + v, j, k, O[0][v], O[1][v], O[2][v]);
         }
       }
     }
@@ -497,7 +501,7 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
       fence_proxy_async();
       issue(c + kTmaStages);
     }
-    if constexpr (!FULL) {
+    if constexpr (EX && !FULL) {
       // the next plane's packed source entries into L1 (its cell classes
       // arrived during this plane)
       if (p.sources_active && c + 1 < N) {
@@ -526,13 +530,18 @@ static void launch_tma_variant(bool h_half, const HalfStepParams<T>& p, const Tm
   const size_t smem = TmaGeom<T>::SMEM;
   if constexpr (sizeof(T) == 4 && !FULL) {
     if (p.stall_tx) {  // failure-detection test instantiation (FP32 LEAN only)
-      if (h_half) half_step_tma_kernel<T, true, CPML, FULL, true><<<grid, block, smem, st>>>(p, maps);
-      else half_step_tma_kernel<T, false, CPML, FULL, true><<<grid, block, smem, st>>>(p, maps);
+      if (h_half) half_step_tma_kernel<T, true, CPML, FULL, false, true><<<grid, block, smem, st>>>(p, maps);
+      else half_step_tma_kernel<T, false, CPML, FULL, false, true><<<grid, block, smem, st>>>(p, maps);
       return;
     }
   }
-  if (h_half) half_step_tma_kernel<T, true, CPML, FULL><<<grid, block, smem, st>>>(p, maps);
-  else half_step_tma_kernel<T, false, CPML, FULL><<<grid, block, smem, st>>>(p, maps);
+  if (p.ex) {
+    if (h_half) half_step_tma_kernel<T, true, CPML, FULL, true><<<grid, block, smem, st>>>(p, maps);
+    else half_step_tma_kernel<T, false, CPML, FULL, true><<<grid, block, smem, st>>>(p, maps);
+  } else {
+    if (h_half) half_step_tma_kernel<T, true, CPML, FULL, false><<<grid, block, smem, st>>>(p, maps);
+    else half_step_tma_kernel<T, false, CPML, FULL, false><<<grid, block, smem, st>>>(p, maps);
+  }
 }
 
 template <typename T>
@@ -547,28 +556,34 @@ void launch_half_step_tma(bool h_half, const HalfStepParams<T>& p, const TmaMaps
   }
 }
 
-template <typename T, bool H, bool CPML, bool FULL, bool STALL = false>
+template <typename T, bool H, bool CPML, bool FULL, bool EX, bool STALL = false>
 static int set_smem_attr() {
-  return int(cudaFuncSetAttribute(half_step_tma_kernel<T, H, CPML, FULL, STALL>,
+  return int(cudaFuncSetAttribute(half_step_tma_kernel<T, H, CPML, FULL, EX, STALL>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, int(TmaGeom<T>::SMEM)));
+}
+
+template <typename T, bool EX>
+static int set_smem_attrs() {
+  int e = 0;
+  e |= set_smem_attr<T, true, true, true, EX>();
+  e |= set_smem_attr<T, true, true, false, EX>();
+  e |= set_smem_attr<T, true, false, true, EX>();
+  e |= set_smem_attr<T, true, false, false, EX>();
+  e |= set_smem_attr<T, false, true, true, EX>();
+  e |= set_smem_attr<T, false, true, false, EX>();
+  e |= set_smem_attr<T, false, false, true, EX>();
+  e |= set_smem_attr<T, false, false, false, EX>();
+  return e;
 }
 
 template <typename T>
 int prepare_tma_kernels() {
-  int e = 0;
-  e |= set_smem_attr<T, true, true, true>();
-  e |= set_smem_attr<T, true, true, false>();
-  e |= set_smem_attr<T, true, false, true>();
-  e |= set_smem_attr<T, true, false, false>();
-  e |= set_smem_attr<T, false, true, true>();
-  e |= set_smem_attr<T, false, true, false>();
-  e |= set_smem_attr<T, false, false, true>();
-  e |= set_smem_attr<T, false, false, false>();
+  int e = set_smem_attrs<T, false>() | set_smem_attrs<T, true>();
   if constexpr (sizeof(T) == 4) {
-    e |= set_smem_attr<T, true, true, false, true>();
-    e |= set_smem_attr<T, true, false, false, true>();
-    e |= set_smem_attr<T, false, true, false, true>();
-    e |= set_smem_attr<T, false, false, false, true>();
+    e |= set_smem_attr<T, true, true, false, false, true>();
+    e |= set_smem_attr<T, true, false, false, false, true>();
+    e |= set_smem_attr<T, false, true, false, false, true>();
+    e |= set_smem_attr<T, false, false, false, false, true>();
   }
   return e;
 }
@@ -576,7 +591,7 @@ int prepare_tma_kernels() {
 template <typename T>
 int tma_resident_ctas() {
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, half_step_tma_kernel<T, true, true, false>, 32 * kTmaY,
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, half_step_tma_kernel<T, true, true, false, false>, 32 * kTmaY,
                                                     TmaGeom<T>::SMEM) != cudaSuccess)
     return 1;
   return n > 0 ? n : 1;
