@@ -220,7 +220,8 @@ __device__ __noinline__ void dft_fold_cell(const HalfStepParams<T>& p, uint32_t 
   while (mask) {
     const int m = __ffs(mask) - 1;
     mask &= mask - 1;
-    const FoldMonitor<T>& fm = p.fold[m];
+    const FoldMonitor<T>& fm = p.fold[p.fold_mon[m]];
+    const Cplx<T>* phase = p.fold_phase + p.fold_off[m];
     if (i < fm.lo[0] || i >= fm.hi[0] || j < fm.lo[1] || j >= fm.hi[1] || k < fm.lo[2] || k >= fm.hi[2]) continue;
     const long long d0 = fm.hi[0] - fm.lo[0], d1 = fm.hi[1] - fm.lo[1], d2 = fm.hi[2] - fm.lo[2];
     const long long ncell = d0 * d1 * d2;
@@ -228,7 +229,7 @@ __device__ __noinline__ void dft_fold_cell(const HalfStepParams<T>& p, uint32_t 
     const T v = fm.comp == 0 ? o0 : (fm.comp == 1 ? o1 : o2);
     for (int f = 0; f < fm.nf; ++f) {
       if (!KH_IN(f * ncell + cell, ncell * fm.nf, 1010)) break;
-      dft_accumulate(fm.F, fm.C, f * ncell + cell, fm.phase[f], v);
+      dft_accumulate(fm.F, fm.C, f * ncell + cell, phase[f], v);
     }
   }
 }

@@ -115,17 +115,17 @@ struct AxisCoef {
   T op;   // 1 + σ
 };
 
-// A DFT monitor accumulated inside a half-step launch (decimation steps):
-// component `comp` (0..2 within the half) over the cell box [lo, hi), which
-// lies inside the computed range 0..n-1; accumulators F[f·ncell + cell], cell
-// x fastest over the box, as the separate DFT kernel lays them out.
+// A DFT monitor that half-step launches can accumulate (device array, one
+// entry per such monitor, built at prepare): component `comp` (0..2 within
+// its half) over the cell box [lo, hi), which lies inside the computed range
+// 0..n-1; accumulators F[f·ncell + cell], cell x fastest over the box, as the
+// separate DFT kernel lays them out.
 constexpr int kMaxFoldMonitors = 16;
 template <typename T>
 struct FoldMonitor {
   int comp;
   int lo[3], hi[3];
   int nf;
-  const Cplx<T>* phase;  // nf entries of this step: Δt·exp(i 2π f t)
   Cplx<T>* F;
   Cplx<T>* C;            // Kahan compensation (FP32) or nullptr
 };
@@ -196,9 +196,15 @@ struct HalfStepParams {
   // Work beyond the update in this launch (TMA-staged kernel): 1 selects the
   // instantiation with LEAN source cells and the folded DFT monitors below.
   int ex;
-  // DFT monitors of this half folded into the launch (TMA-staged kernel)
+  // DFT monitors of this half folded into the launch (TMA-staged kernel):
+  // descriptor fold[fold_mon[m]] with its nf phases of this step (Δt·exp(i 2π f t))
+  // at fold_phase + fold_off[m], m < n_fold.  Kept small: the whole launch's
+  // parameters stay under 4 KB.
+  const FoldMonitor<T>* fold;
+  const Cplx<T>* fold_phase;
   int n_fold;
-  FoldMonitor<T> fold[kMaxFoldMonitors];
+  int fold_mon[kMaxFoldMonitors];
+  int fold_off[kMaxFoldMonitors];
 
   int* err;  // set to KH_ERR_TIMEOUT by a kernel whose bounded wait gave up
   // Failure-detection test hook (0 in normal runs): nonzero launches the FP32

@@ -709,6 +709,27 @@ class Sim : public SimBase {
     const char* fv = std::getenv("KHRONOS_GB300_DFT_FOLD");
     dft_fold_ = !(fv && std::string(fv) == "0");
     if (use_tma_) KH_TRY(build_tma_maps());
+    // descriptors of the monitors the TMA launches accumulate
+    fold_idx_.assign(mons_.size(), -1);
+    {
+      std::vector<kh::FoldMonitor<T>> fd;
+      for (size_t mi = 0; mi < mons_.size(); ++mi) {
+        if (!fold_ok(int(mi))) continue;
+        const Mon& m = mons_[mi];
+        kh::FoldMonitor<T> fm;
+        fm.comp = m.comp % 3;
+        for (int a = 0; a < 3; ++a) {
+          fm.lo[a] = m.start[a];
+          fm.hi[a] = m.start[a] + m.dims[a];
+        }
+        fm.nf = m.nf;
+        fm.F = m.F;
+        fm.C = m.C;
+        fold_idx_[mi] = int(fd.size());
+        fd.push_back(fm);
+      }
+      if (!fd.empty()) KH_TRY(upload_raw(fd.data(), fd.size() * sizeof(kh::FoldMonitor<T>), (void**)&fold_dev_));
+    }
     zplanes_ = choose_zplanes();
     if (const char* sv = std::getenv("KHRONOS_GB300_TEST_STALL")) stall_tx_ = std::string(sv) == "1" ? 16u : 0u;
     // the zeroing and uploads above ran on the legacy default stream; wait for
@@ -1453,20 +1474,14 @@ class Sim : public SimBase {
     std::vector<std::pair<int, size_t>> rest;
     auto fold_dft = [&](kh::HalfStepParams<T>& hp, const std::vector<std::pair<int, size_t>>& dms) {
       hp.n_fold = 0;
+      hp.fold = fold_dev_;
+      hp.fold_phase = dtab;
       rest.clear();
       for (auto& dm : dms) {
-        if (fold_ok(dm.first) && hp.n_fold < kh::kMaxFoldMonitors) {
-          const Mon& m = mons_[dm.first];
-          kh::FoldMonitor<T>& fm = hp.fold[hp.n_fold++];
-          fm.comp = m.comp % 3;
-          for (int a = 0; a < 3; ++a) {
-            fm.lo[a] = m.start[a];
-            fm.hi[a] = m.start[a] + m.dims[a];
-          }
-          fm.nf = m.nf;
-          fm.phase = dtab + dm.second;
-          fm.F = m.F;
-          fm.C = m.C;
+        if (fold_idx_[dm.first] >= 0 && hp.n_fold < kh::kMaxFoldMonitors) {
+          hp.fold_mon[hp.n_fold] = fold_idx_[dm.first];
+          hp.fold_off[hp.n_fold] = int(dm.second);
+          ++hp.n_fold;
         } else {
           rest.push_back(dm);
         }
@@ -1911,6 +1926,8 @@ class Sim : public SimBase {
   uint32_t stall_tx_ = 0;
   bool use_tma_ = true;
   bool dft_fold_ = true;
+  kh::FoldMonitor<T>* fold_dev_ = nullptr;  // descriptors of the foldable monitors
+  std::vector<int> fold_idx_;               // monitor → descriptor index, −1: separate DFT kernel
   int zplanes_ = 10;
   int tma_slots_ = 0;  // SMs × resident TMA-kernel CTAs per SM
   kh::TmaMaps maps_h_, maps_e_;

@@ -475,7 +475,7 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
         // row segment of plane k, on the final values of its cells
         uint32_t fold_mask = 0;
         for (int m = 0; m < p.n_fold; ++m) {
-          const FoldMonitor<T>& fm = p.fold[m];
+          const FoldMonitor<T>& fm = p.fold[p.fold_mon[m]];
           if (fm.lo[0] < x_tile + kTmaX && fm.hi[0] > x_tile && fm.lo[1] <= j && fm.hi[1] > j && fm.lo[2] <= k &&
               fm.hi[2] > k)
             fold_mask |= 1u << m;
