@@ -211,25 +211,37 @@ __device__ __forceinline__ void dft_accumulate(Cplx<double>* F, Cplx<double>* C,
 }
 
 // DFT monitors folded into a half-step (update_dft_monitor!,
-// Monitors.jl:361-379): cell (i, j, k), whose updated components are o0..o2,
-// accumulates into every monitor of `mask` whose box holds it, at the index
-// the separate DFT kernel would use.
+// Monitors.jl:361-379), for the cells of plane k inside this CTA's x–y tile
+// [x_tile, x_tile + tx) × [y_tile, y_tile + ty): the (cell, frequency) items of
+// every monitor of the launch are spread over the CTA's `nthreads` threads
+// (cells fastest), each reading the field value the CTA stored for this
+// plane (visible after the barrier that ends the plane) and updating its
+// accumulator at the index the separate DFT kernel uses.  Called by every
+// thread of the CTA.
 template <typename T>
-__device__ __noinline__ void dft_fold_cell(const HalfStepParams<T>& p, uint32_t mask, int i, int j, int k,
-                                           T o0, T o1, T o2) {
-  while (mask) {
-    const int m = __ffs(mask) - 1;
-    mask &= mask - 1;
+__device__ __noinline__ void dft_fold_plane(const HalfStepParams<T>& p, int x_tile, int tx, int y_tile, int ty,
+                                            int k, int tid, int nthreads) {
+  for (int m = 0; m < p.n_fold; ++m) {
     const FoldMonitor<T>& fm = p.fold[p.fold_mon[m]];
-    const Cplx<T>* phase = p.fold_phase + p.fold_off[m];
-    if (i < fm.lo[0] || i >= fm.hi[0] || j < fm.lo[1] || j >= fm.hi[1] || k < fm.lo[2] || k >= fm.hi[2]) continue;
+    if (k < fm.lo[2] || k >= fm.hi[2]) continue;
+    const int i0 = max(fm.lo[0], x_tile), i1 = min(fm.hi[0], min(x_tile + tx, p.nx));
+    const int j0 = max(fm.lo[1], y_tile), j1 = min(fm.hi[1], min(y_tile + ty, p.ny));
+    if (i0 >= i1 || j0 >= j1) continue;
+    const int ni = i1 - i0;
+    const int ncells = ni * (j1 - j0);
     const long long d0 = fm.hi[0] - fm.lo[0], d1 = fm.hi[1] - fm.lo[1], d2 = fm.hi[2] - fm.lo[2];
-    const long long ncell = d0 * d1 * d2;
-    const long long cell = ((long long)(k - fm.lo[2]) * d1 + (j - fm.lo[1])) * d0 + (i - fm.lo[0]);
-    const T v = fm.comp == 0 ? o0 : (fm.comp == 1 ? o1 : o2);
-    for (int f = 0; f < fm.nf; ++f) {
-      if (!KH_IN(f * ncell + cell, ncell * fm.nf, 1010)) break;
-      dft_accumulate(fm.F, fm.C, f * ncell + cell, phase[f], v);
+    const long long nbox = d0 * d1 * d2;
+    const Cplx<T>* phase = p.fold_phase + p.fold_off[m];
+    const T* field = p.O[fm.comp];
+    const long long items = (long long)ncells * fm.nf;
+    for (long long t = tid; t < items; t += nthreads) {
+      const int f = int(t / ncells);
+      const int c = int(t - (long long)f * ncells);
+      const int i = i0 + c % ni, j = j0 + c / ni;
+      const long long q = p.origin + (long long)k * p.plane + (long long)j * p.pitch + i;
+      const long long cell = ((long long)(k - fm.lo[2]) * d1 + (j - fm.lo[1])) * d0 + (i - fm.lo[0]);
+      if (!KH_IN(q, p.total, 1010) || !KH_IN(f * nbox + cell, nbox * fm.nf, 1016)) continue;
+      dft_accumulate(fm.F, fm.C, f * nbox + cell, phase[f], field[q]);
     }
   }
 }

@@ -463,27 +463,7 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
               lean_source_cell<T, H>(p, q + v, cur.cls[v], pervox ? Ms + ob + v : nullptr,
                                      pervox ? Ms + G::O_ELEMS + ob + v : nullptr,
                                      pervox ? Ms + 2 * G::O_ELEMS + ob + v : nullptr);
-              if (KH_IN(q + v, p.total, 2021)) {
-#pragma unroll
-                for (int cc = 0; cc < 3; ++cc) O[cc][v] = p.O[cc][q + v];
-              }
             }
-        }
-      }
-      if constexpr (EX) {
-        // DFT monitors of this step (decimation steps) whose box meets this
-        // row segment of plane k, on the final values of its cells
-        uint32_t fold_mask = 0;
-        for (int m = 0; m < p.n_fold; ++m) {
-          const FoldMonitor<T>& fm = p.fold[p.fold_mon[m]];
-          if (fm.lo[0] < x_tile + kTmaX && fm.hi[0] > x_tile && fm.lo[1] <= j && fm.hi[1] > j && fm.lo[2] <= k &&
-              fm.hi[2] > k)
-            fold_mask |= 1u << m;
-        }
-        if (fold_mask) {
-#pragma unroll
-          for (int v = 0; v < VN; ++v)
-            if (x0 + v < p.nx) dft_fold_cell<T>(p, fold_mask, x0 + v, j, k, O[0][v], O[1][v], O[2][v]);
         }
       }
     }
@@ -500,6 +480,11 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
     if (tid == 0 && c + kTmaStages <= N) {
       fence_proxy_async();
       issue(c + kTmaStages);
+    }
+    if constexpr (EX) {
+      // DFT monitors of this step (decimation steps), on the plane's values
+      // stored before the barrier above, shared by the whole CTA
+      if (p.n_fold > 0) dft_fold_plane<T>(p, x_tile, kTmaX, y_tile, kTmaY, k0 + c, tid, 32 * kTmaY);
     }
     if constexpr (EX && !FULL) {
       // the next plane's packed source entries into L1 (its cell classes
