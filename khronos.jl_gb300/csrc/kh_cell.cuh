@@ -165,14 +165,12 @@ __device__ __forceinline__ bool lean_source_inline(const HalfStepParams<T>& p, u
 
 // Kahan-compensated DFT accumulation of one value into one accumulator
 // (update_dft_monitor!, Monitors.jl:361-379: F += Δt·exp(i2πft)·field; the
-// phase `ph` carries Δt).  Every product and sum is separately rounded
-// (no contraction into FMAs), so the separate DFT kernel and the pass folded
-// into the half-step kernel give identical bits.
-__device__ __forceinline__ void dft_accumulate(Cplx<float>* F, Cplx<float>* C, long long t, Cplx<float> ph,
-                                               float v) {
-  Cplx<float> acc = F[t];
-  if (C) {
-    Cplx<float> c = C[t];
+// phase `ph` carries Δt), on values already loaded: `c` is the compensation
+// (FP32 runs; `comp` false in FP64 runs, which keep none).  Every product and
+// sum is separately rounded (no contraction into FMAs), so the separate DFT
+// kernel and the pass folded into the half-step kernel give identical bits.
+__device__ __forceinline__ void kahan_update(Cplx<float>& acc, Cplx<float>& c, bool comp, Cplx<float> ph, float v) {
+  if (comp) {
     const float yr = __fsub_rn(__fmul_rn(ph.re, v), c.re);
     const float yi = __fsub_rn(__fmul_rn(ph.im, v), c.im);
     const float tr = __fadd_rn(acc.re, yr);
@@ -181,19 +179,15 @@ __device__ __forceinline__ void dft_accumulate(Cplx<float>* F, Cplx<float>* C, l
     c.im = __fsub_rn(__fsub_rn(ti, acc.im), yi);
     acc.re = tr;
     acc.im = ti;
-    C[t] = c;
   } else {
     acc.re = __fadd_rn(acc.re, __fmul_rn(ph.re, v));
     acc.im = __fadd_rn(acc.im, __fmul_rn(ph.im, v));
   }
-  F[t] = acc;
 }
 
-__device__ __forceinline__ void dft_accumulate(Cplx<double>* F, Cplx<double>* C, long long t, Cplx<double> ph,
-                                               double v) {
-  Cplx<double> acc = F[t];
-  if (C) {
-    Cplx<double> c = C[t];
+__device__ __forceinline__ void kahan_update(Cplx<double>& acc, Cplx<double>& c, bool comp, Cplx<double> ph,
+                                             double v) {
+  if (comp) {
     const double yr = __dsub_rn(__dmul_rn(ph.re, v), c.re);
     const double yi = __dsub_rn(__dmul_rn(ph.im, v), c.im);
     const double tr = __dadd_rn(acc.re, yr);
@@ -202,46 +196,78 @@ __device__ __forceinline__ void dft_accumulate(Cplx<double>* F, Cplx<double>* C,
     c.im = __dsub_rn(__dsub_rn(ti, acc.im), yi);
     acc.re = tr;
     acc.im = ti;
-    C[t] = c;
   } else {
     acc.re = __dadd_rn(acc.re, __dmul_rn(ph.re, v));
     acc.im = __dadd_rn(acc.im, __dmul_rn(ph.im, v));
   }
+}
+
+template <typename T>
+__device__ __forceinline__ void dft_accumulate(Cplx<T>* F, Cplx<T>* C, long long t, Cplx<T> ph, T v) {
+  Cplx<T> acc = F[t];
+  Cplx<T> c = C ? C[t] : Cplx<T>{T(0), T(0)};
+  kahan_update(acc, c, C != nullptr, ph, v);
+  if (C) C[t] = c;
   F[t] = acc;
 }
 
 // DFT monitors folded into a half-step (update_dft_monitor!,
-// Monitors.jl:361-379), for the cells of plane k inside this CTA's x–y tile
-// [x_tile, x_tile + tx) × [y_tile, y_tile + ty): the (cell, frequency) items of
-// every monitor of the launch are spread over the CTA's `nthreads` threads
-// (cells fastest), each reading the field value the CTA stored for this
-// plane (visible after the barrier that ends the plane) and updating its
+// Monitors.jl:361-379), for the cells a CTA updated: planes [k0, k1) of its
+// x–y tile [x_tile, x_tile + tx) × [y_tile, y_tile + ty).  The (plane, cell,
+// frequency) items of every monitor of the launch are spread over the CTA's
+// `nthreads` threads, each reading a field value the CTA stored during its
+// march (visible after the barrier that ends each plane) and updating its
 // accumulator at the index the separate DFT kernel uses.  Called by every
-// thread of the CTA.
+// thread of the CTA once its march is done, when nothing else is live.
 template <typename T>
-__device__ __noinline__ void dft_fold_plane(const HalfStepParams<T>& p, int x_tile, int tx, int y_tile, int ty,
-                                            int k, int tid, int nthreads) {
+__device__ __noinline__ void dft_fold_tile(const HalfStepParams<T>& p, int x_tile, int tx, int y_tile, int ty,
+                                           int k0, int k1, int tid, int nthreads) {
   for (int m = 0; m < p.n_fold; ++m) {
     const FoldMonitor<T>& fm = p.fold[p.fold_mon[m]];
-    if (k < fm.lo[2] || k >= fm.hi[2]) continue;
     const int i0 = max(fm.lo[0], x_tile), i1 = min(fm.hi[0], min(x_tile + tx, p.nx));
     const int j0 = max(fm.lo[1], y_tile), j1 = min(fm.hi[1], min(y_tile + ty, p.ny));
-    if (i0 >= i1 || j0 >= j1) continue;
+    const int kk0 = max(fm.lo[2], k0), kk1 = min(fm.hi[2], k1);
+    if (i0 >= i1 || j0 >= j1 || kk0 >= kk1) continue;
     const int ni = i1 - i0;
-    const int ncells = ni * (j1 - j0);
+    const int ncells = ni * (j1 - j0) * (kk1 - kk0);
+    const int nij = ni * (j1 - j0);
     const long long d0 = fm.hi[0] - fm.lo[0], d1 = fm.hi[1] - fm.lo[1], d2 = fm.hi[2] - fm.lo[2];
     const long long nbox = d0 * d1 * d2;
     const Cplx<T>* phase = p.fold_phase + p.fold_off[m];
     const T* field = p.O[fm.comp];
     const long long items = (long long)ncells * fm.nf;
-    for (long long t = tid; t < items; t += nthreads) {
-      const int f = int(t / ncells);
-      const int c = int(t - (long long)f * ncells);
-      const int i = i0 + c % ni, j = j0 + c / ni;
-      const long long q = p.origin + (long long)k * p.plane + (long long)j * p.pitch + i;
-      const long long cell = ((long long)(k - fm.lo[2]) * d1 + (j - fm.lo[1])) * d0 + (i - fm.lo[0]);
-      if (!KH_IN(q, p.total, 1010) || !KH_IN(f * nbox + cell, nbox * fm.nf, 1016)) continue;
-      dft_accumulate(fm.F, fm.C, f * nbox + cell, phase[f], field[q]);
+    // kFold items per thread and round: every load of a round is issued
+    // before any of its stores, so their latencies overlap
+    constexpr int kFold = 4;
+    for (long long t0 = tid; t0 < items; t0 += (long long)kFold * nthreads) {
+      long long idx[kFold];
+      T val[kFold];
+      Cplx<T> ph[kFold], acc[kFold], cmp[kFold];
+#pragma unroll
+      for (int b = 0; b < kFold; ++b) {
+        const long long t = t0 + (long long)b * nthreads;
+        idx[b] = -1;
+        if (t >= items) continue;
+        const int f = int(t / ncells);
+        const int c = int(t - (long long)f * ncells);
+        const int k = kk0 + c / nij, cij = c % nij;
+        const int i = i0 + cij % ni, j = j0 + cij / ni;
+        const long long q = p.origin + (long long)k * p.plane + (long long)j * p.pitch + i;
+        const long long cell = ((long long)(k - fm.lo[2]) * d1 + (j - fm.lo[1])) * d0 + (i - fm.lo[0]);
+        if (!KH_IN(q, p.total, 1010) || !KH_IN(f * nbox + cell, nbox * fm.nf, 1016)) continue;
+        idx[b] = f * nbox + cell;
+        val[b] = field[q];
+        ph[b] = phase[f];
+        acc[b] = fm.F[idx[b]];
+        cmp[b] = fm.C ? fm.C[idx[b]] : Cplx<T>{T(0), T(0)};
+      }
+#pragma unroll
+      for (int b = 0; b < kFold; ++b) {
+        if (idx[b] < 0) continue;
+        kahan_update(acc[b], cmp[b], fm.C != nullptr, ph[b], val[b]);
+        fm.F[idx[b]] = acc[b];
+        if (fm.C) fm.C[idx[b]] = cmp[b];
+      }
     }
   }
 }

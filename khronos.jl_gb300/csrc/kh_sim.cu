@@ -1175,6 +1175,7 @@ class Sim : public SimBase {
 
  private:
   static constexpr int kBatch = 512;
+  static constexpr int kCaptureNow = 128;
 
   // Entries of the largest per-batch table: both halves' source factors on
   // every step, plus each monitor's phases on its decimation steps.
@@ -1547,11 +1548,13 @@ class Sim : public SimBase {
       GraphEntry* g = nullptr;
       for (auto& ge : graphs_)
         if (ge.sig == sig) { g = &ge; break; }
-      // A sequence is captured the second time it is seen: batches that occur
-      // once (a short run, the last partial batch) are issued directly rather
-      // than paying a capture and an instantiation they never amortise.
-      bool seen_before = false;
-      if (!g) {
+      // A short sequence is captured the second time it is seen: batches that
+      // occur once (a short run, the last partial batch) are issued directly
+      // rather than paying a capture and an instantiation they never
+      // amortise.  Batches of kCaptureNow steps or more are captured at once:
+      // one replay of them already repays the capture.
+      bool seen_before = nb >= kCaptureNow;
+      if (!g && !seen_before) {
         for (auto& sv : seen_)
           if (sv == sig) { seen_before = true; break; }
         if (!seen_before) {

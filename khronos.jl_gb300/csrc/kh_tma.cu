@@ -170,16 +170,6 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
   // the failure-detection test instantiation waits briefly for bytes that never come
   constexpr long long kLimit = STALL ? kStallWaitLimit : kWaitLimit;
 
-  if (tid == 0) {
-    for (int st = 0; st < kTmaStages; ++st) mbar_init(&bars[st], 1);
-    mbar_fence_init();
-  }
-  // LEAN launches with sources: this half-step's time factors in shared memory
-  __shared__ Cplx<T> s_fnow[EX && !FULL ? kSmemSources : 1];
-  if constexpr (EX && !FULL) {
-    if (p.sources_active && p.n_src <= kSmemSources && tid < p.n_src) s_fnow[tid] = p.f_now[tid];
-  }
-  __syncthreads();
   // tile-wide CPML flags along x and y: which CPML state tiles a plane needs
   const bool tfx = x_tile < p.pml_lo[0] || x_tile + kTmaX > p.nx - p.pml_hi[0];
   const bool tfy = y_tile < p.pml_lo[1] || y_tile + kTmaY > p.ny - p.pml_hi[1];
@@ -238,10 +228,22 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
       }
     }
   };
+  // The issuing thread initialises the ring's barriers and starts the first
+  // copies at once; the other threads meet the barriers only after the
+  // __syncthreads below, which the copies in flight do not wait for.
   if (tid == 0) {
+    for (int st = 0; st < kTmaStages; ++st) mbar_init(&bars[st], 1);
+    mbar_fence_init();
     const int first = min(kTmaStages, N + 1);
     for (int n = 0; n < first; ++n) issue(n);
   }
+  // LEAN launches with sources: this half-step's time factors in shared
+  // memory (loaded while the first planes are in flight)
+  __shared__ Cplx<T> s_fnow[EX && !FULL ? kSmemSources : 1];
+  if constexpr (EX && !FULL) {
+    if (p.sources_active && p.n_src <= kSmemSources && tid >= 32 && tid - 32 < p.n_src) s_fnow[tid - 32] = p.f_now[tid - 32];
+  }
+  __syncthreads();
 
   // static per-thread data along the march
   const long long row = p.origin + (long long)j * p.pitch + x0;
@@ -481,11 +483,6 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
       fence_proxy_async();
       issue(c + kTmaStages);
     }
-    if constexpr (EX) {
-      // DFT monitors of this step (decimation steps), on the plane's values
-      // stored before the barrier above, shared by the whole CTA
-      if (p.n_fold > 0) dft_fold_plane<T>(p, x_tile, kTmaX, y_tile, kTmaY, k0 + c, tid, 32 * kTmaY);
-    }
     if constexpr (EX && !FULL) {
       // the next plane's packed source entries into L1 (its cell classes
       // arrived during this plane)
@@ -499,6 +496,11 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
       }
     }
     cur = nxt;
+  }
+  if constexpr (EX) {
+    // DFT monitors of this step (decimation steps) on the values this CTA
+    // stored, shared by the whole CTA after its march
+    if (p.n_fold > 0) dft_fold_tile<T>(p, x_tile, kTmaX, y_tile, kTmaY, k0, k1, tid, 32 * kTmaY);
   }
 }
 
