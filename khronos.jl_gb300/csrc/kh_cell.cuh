@@ -87,191 +87,6 @@ __device__ __forceinline__ void wrap_pre_chi3(const HalfStepParams<T>& p, long l
   }
 }
 
-// Source term S of one cell for this half-step (update_source!,
-// Sources.jl:346-357): S_c = Σ real(f(t)·amplitude) over the cell's entries of
-// component c, in entry order; hasS[c] marks components with an entry.
-template <typename T, bool H>
-__device__ __forceinline__ void source_terms(const HalfStepParams<T>& p, uint32_t cls, T (&S)[3],
-                                             bool (&hasS)[3]) {
-  S[0] = S[1] = S[2] = T(0);
-  hasS[0] = hasS[1] = hasS[2] = false;
-  if (!p.sources_active || !(cls & (H ? kHasSrcH : kHasSrcE))) return;
-  const int slot = int(cls >> kSlotShift);
-  const bool slot_ok = KH_IN(slot + 1, p.n_slots + 1, 1001);
-  const int e1 = slot_ok ? p.slot_off[slot + 1] : 0;
-  for (int e = slot_ok ? p.slot_off[slot] : 0; e < e1; ++e) {
-    if (!KH_IN(e, p.n_ent, 1002)) break;
-    const int c = p.ent_comp[e] - (H ? 3 : 0);  // entries carry components 0..5
-    const Cplx<T> am = p.ent_amp[e];
-    if (!KH_IN(p.ent_src[e], p.n_src, 1003)) continue;
-    const Cplx<T> fv = p.f_now[p.ent_src[e]];
-    const T v = fv.re * am.re - fv.im * am.im;  // real(f(t) · amplitude)
-    if (c == 0) { S[0] += v; hasS[0] = true; }
-    else if (c == 1) { S[1] += v; hasS[1] = true; }
-    else if (c == 2) { S[2] += v; hasS[2] = true; }
-  }
-}
-
-// Source cell q of a LEAN launch, after the kernel stored its B|D update T
-// (the cell has no W stage for a sourced component, which the host checks
-// before choosing LEAN): O = m⁻¹·(T + S) as update_field_generic forms it
-// (net = T; net += S; A = m⁻¹·net, Helpers.jl:329-347).  T is read back from
-// the state array this thread just wrote; m⁻¹ of component c from *m[c]
-// (per-voxel values, in shared or global memory) or the scalar (m[c] null).
-// The general case: any number of entries per cell.
-template <typename T, bool H>
-__device__ __noinline__ void lean_source_cell(const HalfStepParams<T>& p, long long q, uint32_t cls,
-                                              const T* m0, const T* m1, const T* m2) {
-  T S[3];
-  bool hasS[3];
-  source_terms<T, H>(p, cls, S, hasS);
-  if (!KH_IN(q, p.total, 1009)) return;
-  const T* m[3] = {m0, m1, m2};
-#pragma unroll
-  for (int c = 0; c < 3; ++c)
-    if (hasS[c] && p.Ts[c]) {
-      T net = p.Ts[c][q];
-      net += S[c];
-      const T mc = m[c] ? *m[c] : p.m_scalar;
-      p.O[c][q] = mc * net;
-    }
-}
-
-// Source term of a single-entry LEAN source cell, in place on its freshly
-// updated values: O_c = m⁻¹_c·(T_c + S) for the entry's component c, the
-// arithmetic of lean_source_cell.  One load of the packed entry and the time
-// factor from shared memory (`fsm`, or global memory when null).  Returns
-// false, changing nothing, when the cell's slot has several entries.
-template <typename T, bool H>
-__device__ __forceinline__ bool lean_source_inline(const HalfStepParams<T>& p, uint32_t cls, const T (&m)[3],
-                                                   const T (&t)[3], T (&O)[3], const Cplx<T>* fsm) {
-  const int slot = int(cls >> kSlotShift);
-  if (!KH_IN(slot, p.n_slots, 1014)) return true;
-  const SlotPack<T> pk = p.slot_pack[slot];
-  if (pk.src < 0) return false;
-  const int c = pk.comp - (H ? 3 : 0);
-  if (c < 0 || c > 2 || !KH_IN(pk.src, p.n_src, 1015)) return true;
-  const Cplx<T> f = fsm ? fsm[pk.src] : p.f_now[pk.src];
-  T S = T(0);
-  S += f.re * pk.amp.re - f.im * pk.amp.im;  // real(f(t) · amplitude)
-  T net = c == 0 ? t[0] : (c == 1 ? t[1] : t[2]);
-  net += S;
-  const T val = (c == 0 ? m[0] : (c == 1 ? m[1] : m[2])) * net;
-  if (c == 0) O[0] = val;
-  else if (c == 1) O[1] = val;
-  else O[2] = val;
-  return true;
-}
-
-// Kahan-compensated DFT accumulation of one value into one accumulator
-// (update_dft_monitor!, Monitors.jl:361-379: F += Δt·exp(i2πft)·field; the
-// phase `ph` carries Δt), on values already loaded: `c` is the compensation
-// (FP32 runs; `comp` false in FP64 runs, which keep none).  Every product and
-// sum is separately rounded (no contraction into FMAs), so the separate DFT
-// kernel and the pass folded into the half-step kernel give identical bits.
-__device__ __forceinline__ void kahan_update(Cplx<float>& acc, Cplx<float>& c, bool comp, Cplx<float> ph, float v) {
-  if (comp) {
-    const float yr = __fsub_rn(__fmul_rn(ph.re, v), c.re);
-    const float yi = __fsub_rn(__fmul_rn(ph.im, v), c.im);
-    const float tr = __fadd_rn(acc.re, yr);
-    const float ti = __fadd_rn(acc.im, yi);
-    c.re = __fsub_rn(__fsub_rn(tr, acc.re), yr);
-    c.im = __fsub_rn(__fsub_rn(ti, acc.im), yi);
-    acc.re = tr;
-    acc.im = ti;
-  } else {
-    acc.re = __fadd_rn(acc.re, __fmul_rn(ph.re, v));
-    acc.im = __fadd_rn(acc.im, __fmul_rn(ph.im, v));
-  }
-}
-
-__device__ __forceinline__ void kahan_update(Cplx<double>& acc, Cplx<double>& c, bool comp, Cplx<double> ph,
-                                             double v) {
-  if (comp) {
-    const double yr = __dsub_rn(__dmul_rn(ph.re, v), c.re);
-    const double yi = __dsub_rn(__dmul_rn(ph.im, v), c.im);
-    const double tr = __dadd_rn(acc.re, yr);
-    const double ti = __dadd_rn(acc.im, yi);
-    c.re = __dsub_rn(__dsub_rn(tr, acc.re), yr);
-    c.im = __dsub_rn(__dsub_rn(ti, acc.im), yi);
-    acc.re = tr;
-    acc.im = ti;
-  } else {
-    acc.re = __dadd_rn(acc.re, __dmul_rn(ph.re, v));
-    acc.im = __dadd_rn(acc.im, __dmul_rn(ph.im, v));
-  }
-}
-
-template <typename T>
-__device__ __forceinline__ void dft_accumulate(Cplx<T>* F, Cplx<T>* C, long long t, Cplx<T> ph, T v) {
-  Cplx<T> acc = F[t];
-  Cplx<T> c = C ? C[t] : Cplx<T>{T(0), T(0)};
-  kahan_update(acc, c, C != nullptr, ph, v);
-  if (C) C[t] = c;
-  F[t] = acc;
-}
-
-// DFT monitors folded into a half-step (update_dft_monitor!,
-// Monitors.jl:361-379), for the cells a CTA updated: planes [k0, k1) of its
-// x–y tile [x_tile, x_tile + tx) × [y_tile, y_tile + ty).  The (plane, cell,
-// frequency) items of every monitor of the launch are spread over the CTA's
-// `nthreads` threads, each reading a field value the CTA stored during its
-// march (visible after the barrier that ends each plane) and updating its
-// accumulator at the index the separate DFT kernel uses.  Called by every
-// thread of the CTA once its march is done, when nothing else is live.
-template <typename T>
-__device__ __noinline__ void dft_fold_tile(const HalfStepParams<T>& p, int x_tile, int tx, int y_tile, int ty,
-                                           int k0, int k1, int tid, int nthreads) {
-  for (int m = 0; m < p.n_fold; ++m) {
-    const FoldMonitor<T>& fm = p.fold[p.fold_mon[m]];
-    const int i0 = max(fm.lo[0], x_tile), i1 = min(fm.hi[0], min(x_tile + tx, p.nx));
-    const int j0 = max(fm.lo[1], y_tile), j1 = min(fm.hi[1], min(y_tile + ty, p.ny));
-    const int kk0 = max(fm.lo[2], k0), kk1 = min(fm.hi[2], k1);
-    if (i0 >= i1 || j0 >= j1 || kk0 >= kk1) continue;
-    const int ni = i1 - i0;
-    const int ncells = ni * (j1 - j0) * (kk1 - kk0);
-    const int nij = ni * (j1 - j0);
-    const long long d0 = fm.hi[0] - fm.lo[0], d1 = fm.hi[1] - fm.lo[1], d2 = fm.hi[2] - fm.lo[2];
-    const long long nbox = d0 * d1 * d2;
-    const Cplx<T>* phase = p.fold_phase + p.fold_off[m];
-    const T* field = p.O[fm.comp];
-    const long long items = (long long)ncells * fm.nf;
-    // kFold items per thread and round: every load of a round is issued
-    // before any of its stores, so their latencies overlap
-    constexpr int kFold = 4;
-    for (long long t0 = tid; t0 < items; t0 += (long long)kFold * nthreads) {
-      long long idx[kFold];
-      T val[kFold];
-      Cplx<T> ph[kFold], acc[kFold], cmp[kFold];
-#pragma unroll
-      for (int b = 0; b < kFold; ++b) {
-        const long long t = t0 + (long long)b * nthreads;
-        idx[b] = -1;
-        if (t >= items) continue;
-        const int f = int(t / ncells);
-        const int c = int(t - (long long)f * ncells);
-        const int k = kk0 + c / nij, cij = c % nij;
-        const int i = i0 + cij % ni, j = j0 + cij / ni;
-        const long long q = p.origin + (long long)k * p.plane + (long long)j * p.pitch + i;
-        const long long cell = ((long long)(k - fm.lo[2]) * d1 + (j - fm.lo[1])) * d0 + (i - fm.lo[0]);
-        if (!KH_IN(q, p.total, 1010) || !KH_IN(f * nbox + cell, nbox * fm.nf, 1016)) continue;
-        idx[b] = f * nbox + cell;
-        val[b] = field[q];
-        ph[b] = phase[f];
-        acc[b] = fm.F[idx[b]];
-        cmp[b] = fm.C ? fm.C[idx[b]] : Cplx<T>{T(0), T(0)};
-      }
-#pragma unroll
-      for (int b = 0; b < kFold; ++b) {
-        if (idx[b] < 0) continue;
-        kahan_update(acc[b], cmp[b], fm.C != nullptr, ph[b], val[b]);
-        fm.F[idx[b]] = acc[b];
-        if (fm.C) fm.C[idx[b]] = cmp[b];
-      }
-    }
-  }
-}
-
 // Update of one cell that carries a source, χ3, a pole or a material
 // conductivity (and may also sit in a CPML region).  t/u/w are the cell's B|D
 // state and CPML U/W values (loaded and stored by the caller), m its μ⁻¹|ε⁻¹,
@@ -476,4 +291,12 @@ __device__ __forceinline__ void pml_cell(const bool (&f)[3], const AxisCoef<T> (
   }
 }
 
+// One fused half-step.  H = true: B/H from curl E; H = false: D/E from curl H.
+// FULL = false (LEAN) compiles only plain and CPML cells; cells marked special
+// there are source cells, updated as B|D-keeping cells (O = m⁻¹·T) and given
+// their source term by source_fix_kernel when sources are active.
+//
+// The z march is software-pipelined: every load of plane k+1 (fields,
+// neighbours, CPML state, cell classes) is issued before plane k is computed
+// and stored, so each warp keeps two planes of memory traffic in flight.
 }  // namespace kh

@@ -236,17 +236,6 @@ __device__ __forceinline__ void compute_plane(const HalfStepParams<T>& p, PlaneL
         }
       }
     }
-    if constexpr (!FULL) {
-      // LEAN source cells: the term is added after the stores (lean_source_cell)
-      if (p.sources_active) {
-        const bool pervox = p.m_inv[0] != nullptr;
-#pragma unroll
-        for (int v = 0; v < VN; ++v)
-          if ((L.cls[v] & (H ? kHasSrcH : kHasSrcE)) && x0 + v < p.nx)
-            lean_source_cell<T, H>(p, q + v, L.cls[v], pervox ? p.m_inv[0] + q + v : nullptr,
-                                   pervox ? p.m_inv[1] + q + v : nullptr, pervox ? p.m_inv[2] + q + v : nullptr);
-      }
-    }
   }
   // rotate: H half keeps A(k+1) as the next plane's A(k); E half keeps
   // A(k) as the next plane's A(k-1)
@@ -256,15 +245,15 @@ __device__ __forceinline__ void compute_plane(const HalfStepParams<T>& p, PlaneL
 
 // One fused half-step.  H = true: B/H from curl E; H = false: D/E from curl H.
 // FULL = false (LEAN) compiles only plain and CPML cells; cells marked special
-// there are source cells, updated as B|D-keeping cells with their source term
-// added after the stores of each plane (lean_source_cell).
+// there are source cells, updated as B|D-keeping cells (O = m⁻¹·T) and given
+// their source term by source_fix_kernel when sources are active.
 //
 // The z march is double-buffered with a prefetch distance of two planes: the
 // loads of plane k+2 are issued as soon as plane k has been consumed, so each
 // warp keeps about two planes of memory traffic in flight.
 template <typename T, int VN, bool H, bool CPML, bool FULL>
 __global__ void __launch_bounds__(32 * kBlockY, sizeof(T) == 4 ? kMinBlocks : 2)
-    half_step_kernel(const __grid_constant__ HalfStepParams<T> p) {
+    half_step_kernel(const HalfStepParams<T> p) {
   const int lane = threadIdx.x;
   const int j = blockIdx.y * kBlockY + threadIdx.y;
   if (j >= p.ny) return;  // warp-uniform: blockDim.x == 32
@@ -336,6 +325,60 @@ void launch_half_step(bool h_half, const HalfStepParams<T>& p, void* stream) {
   }
 }
 
+// Source term of the cells a LEAN half-step updated as B|D-keeping cells:
+// O = m⁻¹·(T + S), the same arithmetic update_field_generic performs
+// (net = T; net += S; A = m⁻¹·net, Helpers.jl:329-347).
+template <typename T>
+__global__ void source_fix_kernel(const SourceFixParams<T> p) {
+  const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= p.nslots) return;
+  const long long q = p.slot_cell[slot];
+  const SlotPack<T> pk = p.slot_pack[slot];
+  if (!KH_IN(q, p.total, 3022)) return;
+  const int base = p.h_half ? 3 : 0;
+  if (pk.src >= 0) {  // a single entry: one component, S = real(f(t)·amplitude)
+    const int c = pk.comp - base;
+    if (c < 0 || c > 2 || !KH_IN(pk.src, p.n_src, 3024)) return;
+    const Cplx<T> f = p.f_now[pk.src];
+    T S = T(0);
+    S += f.re * pk.amp.re - f.im * pk.amp.im;
+    const T m = p.m_inv[c] ? p.m_inv[c][q] : p.m_scalar;
+    T net = p.Ts[c][q];
+    net += S;
+    p.O[c][q] = m * net;
+    return;
+  }
+  T S[3] = {T(0), T(0), T(0)};
+  bool has[3] = {false, false, false};
+  for (int e = p.slot_off[slot]; e < p.slot_off[slot + 1]; ++e) {
+    if (!KH_IN(e, p.n_ent, 3023)) break;
+    const int c = p.ent_comp[e] - base;
+    if (c < 0 || c > 2) continue;
+    const Cplx<T> a = p.ent_amp[e];
+    if (!KH_IN(p.ent_src[e], p.n_src, 3024)) continue;
+    const Cplx<T> f = p.f_now[p.ent_src[e]];
+    const T v = f.re * a.re - f.im * a.im;
+    if (c == 0) { S[0] += v; has[0] = true; }
+    else if (c == 1) { S[1] += v; has[1] = true; }
+    else { S[2] += v; has[2] = true; }
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    if (!has[c]) continue;
+    const T m = p.m_inv[c] ? p.m_inv[c][q] : p.m_scalar;
+    T net = p.Ts[c][q];
+    net += S[c];
+    p.O[c][q] = m * net;
+  }
+}
+
+template <typename T>
+void launch_source_fix(const SourceFixParams<T>& p, void* stream) {
+  if (p.nslots <= 0) return;
+  const int threads = 128;
+  source_fix_kernel<T><<<(p.nslots + threads - 1) / threads, threads, 0, static_cast<cudaStream_t>(stream)>>>(p);
+}
+
 // ---------------------------------------------------------------------------
 // Periodic wrap.  blockIdx.y = 3·axis + component; threads stride over the
 // face's (n_t1 × n_t2) cells; each copies both directions of one cell.
@@ -374,7 +417,29 @@ void launch_wrap(const WrapParams<T>& p, void* stream) {
 // ---------------------------------------------------------------------------
 // DFT accumulation (update_dft_monitor!, Monitors.jl:361-379):
 //   F[cell, f] += Δt·exp(i2πf t)·field[cell]
-// FP32 accumulators carry a Kahan compensation term.
+// FP32 accumulators carry a Kahan compensation term.  One update, shared by
+// the per-monitor and the batched kernels so both give the same bits.
+template <typename T>
+__device__ __forceinline__ void dft_update(Cplx<T>* F, Cplx<T>* comp, long long t, Cplx<T> ph, T v) {
+  Cplx<T> acc = F[t];
+  if (comp) {
+    Cplx<T> c = comp[t];
+    const T yr = ph.re * v - c.re;
+    const T yi = ph.im * v - c.im;
+    const T tr = acc.re + yr;
+    const T ti = acc.im + yi;
+    c.re = (tr - acc.re) - yr;
+    c.im = (ti - acc.im) - yi;
+    acc.re = tr;
+    acc.im = ti;
+    comp[t] = c;
+  } else {
+    acc.re = acc.re + ph.re * v;
+    acc.im = acc.im + ph.im * v;
+  }
+  F[t] = acc;
+}
+
 template <typename T>
 __global__ void dft_kernel(const DftParams<T> p) {
   const long long ncell = (long long)p.dims[0] * p.dims[1] * p.dims[2];
@@ -390,8 +455,43 @@ __global__ void dft_kernel(const DftParams<T> p) {
     const long long q = p.origin + (long long)(p.start[2] + kk) * p.plane +
                         (long long)(p.start[1] + jj) * p.pitch + (p.start[0] + i);
     if (!KH_IN(q, p.total, 3025)) continue;
-    dft_accumulate(p.F, p.comp, t, p.phase[f], p.field[q]);
+    dft_update(p.F, p.comp, t, p.phase[f], p.field[q]);
   }
+}
+
+// All monitors of one half-step in one grid: item u < first[n] belongs to the
+// monitor m with first[m] <= u < first[m+1].
+template <typename T>
+__global__ void dft_batch_kernel(const DftBatchParams<T> p) {
+  const long long total = p.first[p.n];
+  for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < total;
+       u += (long long)gridDim.x * blockDim.x) {
+    int m = 0;
+    while (m + 1 < p.n && u >= p.first[m + 1]) ++m;
+    const auto& M = p.mon[m];
+    const long long t = u - p.first[m];
+    const long long ncell = (long long)M.dims[0] * M.dims[1] * M.dims[2];
+    const int f = int(t / ncell);
+    const long long cell = t - (long long)f * ncell;
+    const int i = int(cell % M.dims[0]);
+    const long long r = cell / M.dims[0];
+    const int jj = int(r % M.dims[1]);
+    const int kk = int(r / M.dims[1]);
+    const long long q = p.origin + (long long)(M.start[2] + kk) * p.plane +
+                        (long long)(M.start[1] + jj) * p.pitch + (M.start[0] + i);
+    if (!KH_IN(q, p.total, 3030)) continue;
+    dft_update(M.F, M.comp, t, M.phase[f], M.field[q]);
+  }
+}
+
+template <typename T>
+void launch_dft_batch(const DftBatchParams<T>& p, void* stream) {
+  if (p.n <= 0) return;
+  const long long total = p.first[p.n];
+  long long blocks = (total + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  if (blocks < 1) blocks = 1;
+  dft_batch_kernel<T><<<unsigned(blocks), 256, 0, static_cast<cudaStream_t>(stream)>>>(p);
 }
 
 template <typename T>
@@ -530,9 +630,13 @@ template void launch_half_step<float>(bool, const HalfStepParams<float>&, void*)
 template void launch_half_step<double>(bool, const HalfStepParams<double>&, void*);
 template void launch_wrap<float>(const WrapParams<float>&, void*);
 template void launch_wrap<double>(const WrapParams<double>&, void*);
+template void launch_source_fix<float>(const SourceFixParams<float>&, void*);
+template void launch_source_fix<double>(const SourceFixParams<double>&, void*);
 template void launch_record<float>(const RecordParams<float>&, void*);
 template void launch_record<double>(const RecordParams<double>&, void*);
 template void launch_dft<float>(const DftParams<float>&, void*);
+template void launch_dft_batch<float>(const DftBatchParams<float>&, void*);
+template void launch_dft_batch<double>(const DftBatchParams<double>&, void*);
 template void launch_dft<double>(const DftParams<double>&, void*);
 template void launch_flux<float>(const Cplx<float>*, const Cplx<float>*, const Cplx<float>*,
                                  const Cplx<float>*, const Cplx<float>*, const Cplx<float>*,

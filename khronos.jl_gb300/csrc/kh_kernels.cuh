@@ -115,21 +115,6 @@ struct AxisCoef {
   T op;   // 1 + σ
 };
 
-// A DFT monitor that half-step launches can accumulate (device array, one
-// entry per such monitor, built at prepare): component `comp` (0..2 within
-// its half) over the cell box [lo, hi), which lies inside the computed range
-// 0..n-1; accumulators F[f·ncell + cell], cell x fastest over the box, as the
-// separate DFT kernel lays them out.
-constexpr int kMaxFoldMonitors = 16;
-template <typename T>
-struct FoldMonitor {
-  int comp;
-  int lo[3], hi[3];
-  int nf;
-  Cplx<T>* F;
-  Cplx<T>* C;            // Kahan compensation (FP32) or nullptr
-};
-
 // Source slot with a single entry, packed for one load (src < 0: the slot
 // has several entries and takes the general entry loop).
 template <typename T>
@@ -138,8 +123,6 @@ struct alignas(16) SlotPack {
   int comp;      // component 0..5
   Cplx<T> amp;   // complex amplitude
 };
-// Time factors of up to this many sources are staged in shared memory.
-constexpr int kSmemSources = 64;
 
 // Parameters of one fused half-step launch.
 template <typename T>
@@ -180,7 +163,6 @@ struct HalfStepParams {
   const int* ent_comp;        // component 0..2 within this half
   const Cplx<T>* ent_amp;     // complex amplitude of entry
   const Cplx<T>* f_now;       // per source: time factor f(t) of this half-step
-  const SlotPack<T>* slot_pack;  // per slot: its entry when it has exactly one
   int n_slots, n_ent, n_src;  // extents of slot_off (n_slots + 1), ent_*, f_now
 
   // E half only
@@ -192,19 +174,6 @@ struct HalfStepParams {
   // its pre-correction E into the ghost layer the wrap fills (the reference
   // exchanges E before the Kerr correction); the wrap kernel skips those cells.
   uint32_t periodic;
-
-  // Work beyond the update in this launch (TMA-staged kernel): 1 selects the
-  // instantiation with LEAN source cells and the folded DFT monitors below.
-  int ex;
-  // DFT monitors of this half folded into the launch (TMA-staged kernel):
-  // descriptor fold[fold_mon[m]] with its nf phases of this step (Δt·exp(i 2π f t))
-  // at fold_phase + fold_off[m], m < n_fold.  Kept small: the whole launch's
-  // parameters stay under 4 KB.
-  const FoldMonitor<T>* fold;
-  const Cplx<T>* fold_phase;
-  int n_fold;
-  int fold_mon[kMaxFoldMonitors];
-  int fold_off[kMaxFoldMonitors];
 
   int* err;  // set to KH_ERR_TIMEOUT by a kernel whose bounded wait gave up
   // Failure-detection test hook (0 in normal runs): nonzero launches the FP32
@@ -310,6 +279,48 @@ struct DftParams {
 // FP64 vectors; a 320-cell row is 5 full warps).
 constexpr int kVN = 2;
 
+// Sparse source application for cells the LEAN kernel updated as B|D-keeping
+// cells: O = m⁻¹·(T + S) with S = Σ real(f(t)·amplitude) (Helpers.jl:329-332,
+// Sources.jl:346-357).  Exact when the cell has no W stage for the component
+// and no χ3/pole, which the host checks before choosing this path.  One
+// thread per source cell; a cell with a single entry reads it packed.
+template <typename T>
+struct SourceFixParams {
+  int nslots, n_ent, n_src;
+  long long total;
+  const long long* slot_cell;  // cell offset of each slot
+  const SlotPack<T>* slot_pack;
+  const int* slot_off;
+  const int* ent_src;
+  const int* ent_comp;         // 0..5
+  const Cplx<T>* ent_amp;
+  const Cplx<T>* f_now;
+  T* O[3];
+  const T* Ts[3];
+  const T* m_inv[3];
+  T m_scalar;
+  int h_half;
+};
+
+// DFT accumulation of every monitor of one half-step in one launch
+// (update_dft_monitor!, Monitors.jl:361-379, for all monitors updated at this
+// step): item t of monitor m (t < ncell·nf, cell fastest) is (cell, f).
+constexpr int kMaxDftBatch = 16;
+template <typename T>
+struct DftBatchParams {
+  int n;                             // monitors in this launch
+  long long pitch, plane, origin, total;
+  long long first[kMaxDftBatch + 1]; // prefix sums of the monitors' items
+  struct Mon {
+    const T* field;
+    int start[3], dims[3];
+    int nf;
+    const Cplx<T>* phase;            // nf entries: Δt·exp(i 2π f t)
+    Cplx<T>* F;
+    Cplx<T>* comp;                   // Kahan compensation (FP32) or nullptr
+  } mon[kMaxDftBatch];
+};
+
 // Periodic wrap of one field group after its half-step (_exchange_halos_local!
 // single-chunk connections, Chunking.jl:1751-1768, 2138-2172): for each axis a
 // in `periodic` and each component, layer n_a-1 → ghost layer -1 and layer 0 →
@@ -330,7 +341,13 @@ template <typename T>
 void launch_wrap(const WrapParams<T>& p, void* stream);
 
 template <typename T>
+void launch_source_fix(const SourceFixParams<T>& p, void* stream);
+
+template <typename T>
 void launch_dft(const DftParams<T>& p, void* stream);
+
+template <typename T>
+void launch_dft_batch(const DftBatchParams<T>& p, void* stream);
 
 // ---- set-up kernels (kh_setup.cu) ----
 // Compact Center-range array (x fastest) → padded layout, converted to T.

@@ -512,9 +512,9 @@ class Sim : public SimBase {
       e = e2;
     }
     // Which cells the LEAN kernels can take (see run_batch): a source cell's
-    // term is O = m⁻¹·(T + S) there, exact when its component has no W stage
-    // in that cell and the cell carries no χ3 or pole; CPU-path semantics keep
-    // B|D for every component of a special cell inside CPML, which LEAN does not.
+    // term can be added after the kernel when its component has no W stage
+    // there and the cell carries no χ3 or pole; CPU-path semantics keep B|D
+    // for every component of a special cell inside CPML, which LEAN does not.
     auto flag = [&](int a, int idx) { return idx < lo_[a] || idx >= n_[a] - hi_[a]; };
     has_src_[0] = has_src_[1] = false;
     src_lean_ok_[0] = src_lean_ok_[1] = true;
@@ -706,30 +706,9 @@ class Sim : public SimBase {
     // register-pipelined one.
     const char* kv = std::getenv("KHRONOS_GB300_KERNEL");
     use_tma_ = !(kv && std::string(kv) == "simt");
-    const char* fv = std::getenv("KHRONOS_GB300_DFT_FOLD");
-    dft_fold_ = !(fv && std::string(fv) == "0");
+    const char* bv = std::getenv("KHRONOS_GB300_DFT_BATCH");
+    dft_batch_ = !(bv && std::string(bv) == "0");
     if (use_tma_) KH_TRY(build_tma_maps());
-    // descriptors of the monitors the TMA launches accumulate
-    fold_idx_.assign(mons_.size(), -1);
-    {
-      std::vector<kh::FoldMonitor<T>> fd;
-      for (size_t mi = 0; mi < mons_.size(); ++mi) {
-        if (!fold_ok(int(mi))) continue;
-        const Mon& m = mons_[mi];
-        kh::FoldMonitor<T> fm;
-        fm.comp = m.comp % 3;
-        for (int a = 0; a < 3; ++a) {
-          fm.lo[a] = m.start[a];
-          fm.hi[a] = m.start[a] + m.dims[a];
-        }
-        fm.nf = m.nf;
-        fm.F = m.F;
-        fm.C = m.C;
-        fold_idx_[mi] = int(fd.size());
-        fd.push_back(fm);
-      }
-      if (!fd.empty()) KH_TRY(upload_raw(fd.data(), fd.size() * sizeof(kh::FoldMonitor<T>), (void**)&fold_dev_));
-    }
     zplanes_ = choose_zplanes();
     if (const char* sv = std::getenv("KHRONOS_GB300_TEST_STALL")) stall_tx_ = std::string(sv) == "1" ? 16u : 0u;
     // the zeroing and uploads above ran on the legacy default stream; wait for
@@ -1470,24 +1449,7 @@ class Sim : public SimBase {
     const bool full_h_base = msb || (ref_cpu && special_in_region_[1]);
     const bool full_e_base = msd || chi3_ != nullptr || !poles_d_.empty() || (ref_cpu && special_in_region_[0]);
     const kh::WrapParams<T> wh = wrap_params(true), we = wrap_params(false);
-    // DFT monitors of one half-step: those foldable into the launch go into
-    // its monitor table, the rest get the separate DFT kernel afterwards.
-    std::vector<std::pair<int, size_t>> rest;
-    auto fold_dft = [&](kh::HalfStepParams<T>& hp, const std::vector<std::pair<int, size_t>>& dms) {
-      hp.n_fold = 0;
-      hp.fold = fold_dev_;
-      hp.fold_phase = dtab;
-      rest.clear();
-      for (auto& dm : dms) {
-        if (fold_idx_[dm.first] >= 0 && hp.n_fold < kh::kMaxFoldMonitors) {
-          hp.fold_mon[hp.n_fold] = fold_idx_[dm.first];
-          hp.fold_off[hp.n_fold] = int(dm.second);
-          ++hp.n_fold;
-        } else {
-          rest.push_back(dm);
-        }
-      }
-    };
+    kh::SourceFixParams<T> fh = fix_params(true), fe = fix_params(false);
     auto issue_all = [&](cudaStream_t st) {
     for (int s = 0; s < nb; ++s) {
       const StepPlan& P = plan[s];
@@ -1495,35 +1457,41 @@ class Sim : public SimBase {
       ph.f_now = dtab + P.fH;
       const bool src_h = P.sa && has_src_[1];
       ph.full = (full_h_base || (src_h && !src_lean_ok_[1])) ? 1 : 0;
-      fold_dft(ph, P.dftH);
-      ph.ex = ((src_h && !ph.full) || ph.n_fold > 0) ? 1 : 0;
       mark(s, 0);
       if (use_tma_) kh::launch_half_step_tma<T>(true, ph, maps_h_, st);
       else kh::launch_half_step<T>(true, ph, st);
       ++launches;
+      if (src_h && !ph.full) {
+        fh.f_now = dtab + P.fH;
+        kh::launch_source_fix<T>(fh, st);
+        ++launches;
+      }
       if (d_.periodic) {
         kh::launch_wrap<T>(wh, st);
         ++launches;
       }
       mark(s, 1);
-      for (auto& dm : rest) launch_dft_for(dm.first, dtab + dm.second, st);
+      launch_dfts(P.dftH, dtab, st);
       record_histories(true, timestep_ + s, st);
       mark(s, 2);
       pe.sources_active = P.sa ? 1 : 0;
       pe.f_now = dtab + P.fE;
       const bool src_e = P.sa && has_src_[0];
       pe.full = (full_e_base || (src_e && !src_lean_ok_[0])) ? 1 : 0;
-      fold_dft(pe, P.dftE);
-      pe.ex = ((src_e && !pe.full) || pe.n_fold > 0) ? 1 : 0;
       if (use_tma_) kh::launch_half_step_tma<T>(false, pe, maps_e_, st);
       else kh::launch_half_step<T>(false, pe, st);
       ++launches;
+      if (src_e && !pe.full) {
+        fe.f_now = dtab + P.fE;
+        kh::launch_source_fix<T>(fe, st);
+        ++launches;
+      }
       if (d_.periodic) {
         kh::launch_wrap<T>(we, st);
         ++launches;
       }
       mark(s, 3);
-      for (auto& dm : rest) launch_dft_for(dm.first, dtab + dm.second, st);
+      launch_dfts(P.dftE, dtab, st);
       record_histories(false, timestep_ + s, st);
       mark(s, 4);
     }
@@ -1684,17 +1652,41 @@ class Sim : public SimBase {
     return st;
   }
 
-  // A monitor is accumulated inside the TMA half-step launch when its box
-  // lies in the computed range 0..n-1 of every axis (a box reaching the
-  // staggered wall layer n keeps the separate kernel, which reads that layer
-  // after the periodic wrap has filled it).  KHRONOS_GB300_DFT_FOLD=0 keeps
-  // every monitor on the separate kernel.
-  bool fold_ok(int mi) const {
-    if (!use_tma_ || !dft_fold_) return false;
-    const Mon& m = mons_[mi];
-    for (int a = 0; a < 3; ++a)
-      if (m.start[a] < 0 || m.start[a] + m.dims[a] > n_[a]) return false;
-    return true;
+  // The DFT monitors updated after one half-step of one step: one launch for
+  // all of them (KHRONOS_GB300_DFT_BATCH=0: one launch per monitor, the same
+  // arithmetic).
+  void launch_dfts(const std::vector<std::pair<int, size_t>>& dms, const Cplx<T>* dtab, cudaStream_t st) {
+    if (dms.empty()) return;
+    if (!dft_batch_) {
+      for (auto& dm : dms) launch_dft_for(dm.first, dtab + dm.second, st);
+      return;
+    }
+    for (size_t b0 = 0; b0 < dms.size(); b0 += kh::kMaxDftBatch) {
+      kh::DftBatchParams<T> bp;
+      std::memset(&bp, 0, sizeof(bp));
+      bp.pitch = pitch_;
+      bp.plane = plane_;
+      bp.origin = origin_;
+      bp.total = total_;
+      bp.first[0] = 0;
+      for (size_t q = b0; q < dms.size() && bp.n < kh::kMaxDftBatch; ++q) {
+        const Mon& m = mons_[dms[q].first];
+        auto& M = bp.mon[bp.n];
+        M.field = m.comp < 3 ? E_[m.comp] : H_[m.comp - 3];
+        for (int a = 0; a < 3; ++a) {
+          M.start[a] = m.start[a];
+          M.dims[a] = m.dims[a];
+        }
+        M.nf = m.nf;
+        M.phase = dtab + dms[q].second;
+        M.F = m.F;
+        M.comp = m.C;
+        bp.first[bp.n + 1] = bp.first[bp.n] + (long long)m.ncell * m.nf;
+        ++bp.n;
+      }
+      kh::launch_dft_batch<T>(bp, st);
+      ++launches;
+    }
   }
 
   void launch_dft_for(int mi, const Cplx<T>* phase, cudaStream_t stream) {
@@ -1801,6 +1793,29 @@ class Sim : public SimBase {
     return KH_OK;
   }
 
+  kh::SourceFixParams<T> fix_params(bool h) const {
+    kh::SourceFixParams<T> f;
+    std::memset(&f, 0, sizeof(f));
+    f.nslots = nslots_;
+    f.n_ent = int(ent_amp_h_.size());
+    f.n_src = nsrc_;
+    f.total = total_;
+    f.slot_cell = slot_cell_;
+    f.slot_pack = slot_pack_;
+    f.slot_off = slot_off_;
+    f.ent_src = ent_src_;
+    f.ent_comp = ent_comp_;
+    f.ent_amp = ent_amp_;
+    for (int c = 0; c < 3; ++c) {
+      f.O[c] = h ? H_[c] : E_[c];
+      f.Ts[c] = h ? B_[c] : D_[c];
+      f.m_inv[c] = h ? mu_[c] : eps_[c];
+    }
+    f.m_scalar = h ? T(d_.mu_inv) : T(d_.eps_inv);
+    f.h_half = h ? 1 : 0;
+    return f;
+  }
+
   kh::WrapParams<T> wrap_params(bool h) const {
     kh::WrapParams<T> w;
     std::memset(&w, 0, sizeof(w));
@@ -1858,7 +1873,6 @@ class Sim : public SimBase {
     p.stall_tx = stall_tx_;
     p.periodic = h ? 0u : uint32_t(d_.periodic);
     p.slot_off = slot_off_;
-    p.slot_pack = slot_pack_;
     p.ent_src = ent_src_;
     p.ent_comp = ent_comp_;
     p.ent_amp = ent_amp_;
@@ -1928,9 +1942,7 @@ class Sim : public SimBase {
   // bytes that never arrive and give up (tests of the timeout status only)
   uint32_t stall_tx_ = 0;
   bool use_tma_ = true;
-  bool dft_fold_ = true;
-  kh::FoldMonitor<T>* fold_dev_ = nullptr;  // descriptors of the foldable monitors
-  std::vector<int> fold_idx_;               // monitor → descriptor index, −1: separate DFT kernel
+  bool dft_batch_ = true;
   int zplanes_ = 10;
   int tma_slots_ = 0;  // SMs × resident TMA-kernel CTAs per SM
   kh::TmaMaps maps_h_, maps_e_;

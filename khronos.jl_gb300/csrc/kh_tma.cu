@@ -141,12 +141,9 @@ constexpr int tma_min_blocks() {
   return sizeof(T) == 4 ? (FULL ? kTmaMinBlocks - 1 : kTmaMinBlocks) : 2;
 }
 
-// EX: the launch also carries work beyond the half-step update, compiled
-// only into this instantiation so the other launches keep the lean code path:
-// LEAN source cells (O = m⁻¹·(T + S)) and DFT monitors folded into the pass.
-template <typename T, bool H, bool CPML, bool FULL, bool EX, bool STALL = false>
+template <typename T, bool H, bool CPML, bool FULL, bool STALL = false>
 __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
-    half_step_tma_kernel(const __grid_constant__ HalfStepParams<T> p, const __grid_constant__ TmaMaps maps) {
+    half_step_tma_kernel(const HalfStepParams<T> p, const __grid_constant__ TmaMaps maps) {
   using G = TmaGeom<T>;
   constexpr int VN = 2;
   constexpr int s = H ? 1 : -1;
@@ -170,6 +167,11 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
   // the failure-detection test instantiation waits briefly for bytes that never come
   constexpr long long kLimit = STALL ? kStallWaitLimit : kWaitLimit;
 
+  if (tid == 0) {
+    for (int st = 0; st < kTmaStages; ++st) mbar_init(&bars[st], 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
   // tile-wide CPML flags along x and y: which CPML state tiles a plane needs
   const bool tfx = x_tile < p.pml_lo[0] || x_tile + kTmaX > p.nx - p.pml_hi[0];
   const bool tfy = y_tile < p.pml_lo[1] || y_tile + kTmaY > p.ny - p.pml_hi[1];
@@ -228,22 +230,10 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
       }
     }
   };
-  // The issuing thread initialises the ring's barriers and starts the first
-  // copies at once; the other threads meet the barriers only after the
-  // __syncthreads below, which the copies in flight do not wait for.
   if (tid == 0) {
-    for (int st = 0; st < kTmaStages; ++st) mbar_init(&bars[st], 1);
-    mbar_fence_init();
     const int first = min(kTmaStages, N + 1);
     for (int n = 0; n < first; ++n) issue(n);
   }
-  // LEAN launches with sources: this half-step's time factors in shared
-  // memory (loaded while the first planes are in flight)
-  __shared__ Cplx<T> s_fnow[EX && !FULL ? kSmemSources : 1];
-  if constexpr (EX && !FULL) {
-    if (p.sources_active && p.n_src <= kSmemSources && tid >= 32 && tid - 32 < p.n_src) s_fnow[tid - 32] = p.f_now[tid - 32];
-  }
-  __syncthreads();
 
   // static per-thread data along the march
   const long long row = p.origin + (long long)j * p.pitch + x0;
@@ -355,7 +345,6 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
       // this thread's two cells have no CPML flag and no special class
       // (measured faster than a warp-uniform decision per row segment)
       bool plain = !(anyfx || fy || fz);
-      uint32_t multi = 0;  // EX: bit v set when cell v's source slot has several entries
 #pragma unroll
       for (int v = 0; v < VN; ++v) plain = plain && !(cur.cls[v] & (H ? kSpecialH : kSpecialE));
       if (plain) {
@@ -365,7 +354,6 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
           for (int v = 0; v < VN; ++v) O[cc][v] = O[cc][v] + m[cc][v] * K[cc][v];
       } else {
         const AxisCoef<T> az = KH_IN(k, p.nz, 2020) ? p.ax[2][k] : AxisCoef<T>{T(0), T(1), T(1), T(1)};
-        multi = 0;
 #pragma unroll
         for (int v = 0; v < VN; ++v) {
           const int i = x0 + v;
@@ -414,13 +402,6 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
                 Oc[cc] = mc[cc] * tc[cc];
               }
             }
-            if constexpr (EX) {
-              // source term of a single-entry cell in place; several entries
-              // after the stores (lean_source_cell)
-              if (special && p.sources_active && (cur.cls[v] & (H ? kHasSrcH : kHasSrcE)) &&
-                  !lean_source_inline<T, H>(p, cur.cls[v], mc, tc, Oc, p.n_src <= kSmemSources ? s_fnow : nullptr))
-                multi |= 1u << v;
-            }
           }
 #pragma unroll
           for (int cc = 0; cc < 3; ++cc) {
@@ -455,19 +436,6 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
             for (int cc = 0; cc < 3; ++cc) p.O[cc][q + v] = O[cc][v];
           }
       }
-      if constexpr (EX && !FULL) {
-        // source cells whose slot has several entries: the general entry loop,
-        // from the B|D state just stored
-        if (multi) {
-#pragma unroll
-          for (int v = 0; v < VN; ++v)
-            if (((multi >> v) & 1u) && x0 + v < p.nx) {
-              lean_source_cell<T, H>(p, q + v, cur.cls[v], pervox ? Ms + ob + v : nullptr,
-                                     pervox ? Ms + G::O_ELEMS + ob + v : nullptr,
-                                     pervox ? Ms + 2 * G::O_ELEMS + ob + v : nullptr);
-            }
-        }
-      }
     }
     // every thread is done with load c (H: current, E: z neighbour); its
     // stage takes load c + kTmaStages
@@ -483,24 +451,7 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
       fence_proxy_async();
       issue(c + kTmaStages);
     }
-    if constexpr (EX && !FULL) {
-      // the next plane's packed source entries into L1 (its cell classes
-      // arrived during this plane)
-      if (p.sources_active && c + 1 < N) {
-#pragma unroll
-        for (int v = 0; v < VN; ++v)
-          if (nxt.cls[v] & (H ? kHasSrcH : kHasSrcE)) {
-            const int slot = int(nxt.cls[v] >> kSlotShift);
-            if (KH_IN(slot, p.n_slots, 2025)) asm volatile("prefetch.global.L1 [%0];" ::"l"(p.slot_pack + slot));
-          }
-      }
-    }
     cur = nxt;
-  }
-  if constexpr (EX) {
-    // DFT monitors of this step (decimation steps) on the values this CTA
-    // stored, shared by the whole CTA after its march
-    if (p.n_fold > 0) dft_fold_tile<T>(p, x_tile, kTmaX, y_tile, kTmaY, k0, k1, tid, 32 * kTmaY);
   }
 }
 
@@ -517,18 +468,13 @@ static void launch_tma_variant(bool h_half, const HalfStepParams<T>& p, const Tm
   const size_t smem = TmaGeom<T>::SMEM;
   if constexpr (sizeof(T) == 4 && !FULL) {
     if (p.stall_tx) {  // failure-detection test instantiation (FP32 LEAN only)
-      if (h_half) half_step_tma_kernel<T, true, CPML, FULL, false, true><<<grid, block, smem, st>>>(p, maps);
-      else half_step_tma_kernel<T, false, CPML, FULL, false, true><<<grid, block, smem, st>>>(p, maps);
+      if (h_half) half_step_tma_kernel<T, true, CPML, FULL, true><<<grid, block, smem, st>>>(p, maps);
+      else half_step_tma_kernel<T, false, CPML, FULL, true><<<grid, block, smem, st>>>(p, maps);
       return;
     }
   }
-  if (p.ex) {
-    if (h_half) half_step_tma_kernel<T, true, CPML, FULL, true><<<grid, block, smem, st>>>(p, maps);
-    else half_step_tma_kernel<T, false, CPML, FULL, true><<<grid, block, smem, st>>>(p, maps);
-  } else {
-    if (h_half) half_step_tma_kernel<T, true, CPML, FULL, false><<<grid, block, smem, st>>>(p, maps);
-    else half_step_tma_kernel<T, false, CPML, FULL, false><<<grid, block, smem, st>>>(p, maps);
-  }
+  if (h_half) half_step_tma_kernel<T, true, CPML, FULL><<<grid, block, smem, st>>>(p, maps);
+  else half_step_tma_kernel<T, false, CPML, FULL><<<grid, block, smem, st>>>(p, maps);
 }
 
 template <typename T>
@@ -543,34 +489,28 @@ void launch_half_step_tma(bool h_half, const HalfStepParams<T>& p, const TmaMaps
   }
 }
 
-template <typename T, bool H, bool CPML, bool FULL, bool EX, bool STALL = false>
+template <typename T, bool H, bool CPML, bool FULL, bool STALL = false>
 static int set_smem_attr() {
-  return int(cudaFuncSetAttribute(half_step_tma_kernel<T, H, CPML, FULL, EX, STALL>,
+  return int(cudaFuncSetAttribute(half_step_tma_kernel<T, H, CPML, FULL, STALL>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, int(TmaGeom<T>::SMEM)));
-}
-
-template <typename T, bool EX>
-static int set_smem_attrs() {
-  int e = 0;
-  e |= set_smem_attr<T, true, true, true, EX>();
-  e |= set_smem_attr<T, true, true, false, EX>();
-  e |= set_smem_attr<T, true, false, true, EX>();
-  e |= set_smem_attr<T, true, false, false, EX>();
-  e |= set_smem_attr<T, false, true, true, EX>();
-  e |= set_smem_attr<T, false, true, false, EX>();
-  e |= set_smem_attr<T, false, false, true, EX>();
-  e |= set_smem_attr<T, false, false, false, EX>();
-  return e;
 }
 
 template <typename T>
 int prepare_tma_kernels() {
-  int e = set_smem_attrs<T, false>() | set_smem_attrs<T, true>();
+  int e = 0;
+  e |= set_smem_attr<T, true, true, true>();
+  e |= set_smem_attr<T, true, true, false>();
+  e |= set_smem_attr<T, true, false, true>();
+  e |= set_smem_attr<T, true, false, false>();
+  e |= set_smem_attr<T, false, true, true>();
+  e |= set_smem_attr<T, false, true, false>();
+  e |= set_smem_attr<T, false, false, true>();
+  e |= set_smem_attr<T, false, false, false>();
   if constexpr (sizeof(T) == 4) {
-    e |= set_smem_attr<T, true, true, false, false, true>();
-    e |= set_smem_attr<T, true, false, false, false, true>();
-    e |= set_smem_attr<T, false, true, false, false, true>();
-    e |= set_smem_attr<T, false, false, false, false, true>();
+    e |= set_smem_attr<T, true, true, false, true>();
+    e |= set_smem_attr<T, true, false, false, true>();
+    e |= set_smem_attr<T, false, true, false, true>();
+    e |= set_smem_attr<T, false, false, false, true>();
   }
   return e;
 }
@@ -578,7 +518,7 @@ int prepare_tma_kernels() {
 template <typename T>
 int tma_resident_ctas() {
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, half_step_tma_kernel<T, true, true, false, false>, 32 * kTmaY,
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, half_step_tma_kernel<T, true, true, false>, 32 * kTmaY,
                                                     TmaGeom<T>::SMEM) != cudaSuccess)
     return 1;
   return n > 0 ? n : 1;

@@ -315,9 +315,9 @@ def test_step_graphs_are_invisible(kh, gpu_lib, dtype, monkeypatch):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("dtype,semantics", [("f32", "cpml"), ("f64", "cpml"), ("f32", "reference_cpu")])
-def test_dft_fold_is_invisible(kh, gpu_lib, dtype, semantics, monkeypatch):
-    """DFT monitors accumulated inside the half-step launch give the same bits
-    as the separate DFT kernel (KHRONOS_GB300_DFT_FOLD=0): the waveguide's two
+def test_dft_batch_is_invisible(kh, gpu_lib, dtype, semantics, monkeypatch):
+    """All monitors of a half-step accumulated by one launch give the same bits
+    as one launch per monitor (KHRONOS_GB300_DFT_BATCH=0): the waveguide's two
     flux planes (Ey, Ez, Hy, Hz), with the source active and after its cutoff,
     in both CPML semantics."""
     from khronos_gb300 import configs
@@ -329,7 +329,7 @@ def test_dft_fold_is_invisible(kh, gpu_lib, dtype, semantics, monkeypatch):
     steps = 700 if semantics == "cpml" else 60
     out = {}
     for mode in ("0", "1"):
-        monkeypatch.setenv("KHRONOS_GB300_DFT_FOLD", mode)
+        monkeypatch.setenv("KHRONOS_GB300_DFT_BATCH", mode)
         g = GpuSim(spec, lib=gpu_lib)
         g.step(steps)
         out[mode] = [g.field(c) for c in range(6)] + [g.dft(m) for m in range(len(spec.monitors))]
