@@ -11,8 +11,7 @@ which can move a flux plane by one cell, so they measure a different plane.)
 * Si-strip waveguide at half resolution (160×96×64), the full physical run
   (2000 steps): FP32 GPU against the FP64 oracle;
 * the same waveguide at full size (320×192×128, 4000 steps): FP32 GPU
-  against the promoted FP64 GPU run, which the parity tests hold to 1e-10 of
-  the FP64 oracle on smaller grids.
+  against the FP64 oracle (about 3·10¹⁰ cell-updates on the host cores).
 """
 import pytest
 
@@ -75,9 +74,9 @@ def test_waveguide_half_resolution_fp32_flux_vs_fp64_oracle(kh, oracle, gpu_lib)
     _check(_gpu_fluxes(w32, 2000, gpu_lib), _oracle_fluxes(w32, 2000, oracle))
 
 
-def test_waveguide_full_size_fp32_flux_vs_fp64(kh, gpu_lib):
+def test_waveguide_full_size_fp32_flux_vs_fp64_oracle(kh, oracle, gpu_lib):
     from khronos_gb300 import configs
 
     w32 = configs.waveguide(dtype="f32")
     assert tuple(w32.sim.spec().n) == (320, 192, 128)
-    _check(_gpu_fluxes(w32, 4000, gpu_lib), _gpu_fluxes(w32, 4000, gpu_lib, promote=True))
+    _check(_gpu_fluxes(w32, 4000, gpu_lib), _oracle_fluxes(w32, 4000, oracle))

@@ -152,3 +152,85 @@ def test_promoted_spec_keeps_inputs(kh):
     assert pp.n == sp.n and pp.dt == sp.dt and pp.delta == sp.delta
     assert [m.start for m in pp.monitors] == [m.start for m in sp.monitors]
     assert all(np.array_equal(a.amp, b.amp) for a, b in zip(pp.sources, sp.sources))
+
+
+def _absorber_sigma(n, delta, layers=20, order=3):
+    """_apply_absorbers! (Geometry.jl:708-790) for one absorber on the high y
+    side: σ = σ_max·(d/L)^p over the last `layers` entries of each component's
+    own y extent (ny + 1 for Ex, Ez, Hy; ny for Ey, Hx, Hz), σ_max =
+    −(p+1)·ln(1e-6)/(2L), on the cells 0..ny−1 this library's arrays hold."""
+    L = layers * delta
+    smax = -(order + 1) * np.log(1e-6) / (2.0 * L)
+
+    def comp(ny_c):
+        a = np.zeros(n)
+        for layer in range(1, min(layers, ny_c) + 1):
+            j = ny_c - layer  # 0-based index of this layer
+            if j < n[1]:
+                a[:, j, :] += smax * ((layers - layer + 1) / layers) ** order
+        return a
+
+    ny = n[1]
+    sd = [comp(ny + 1), comp(ny), comp(ny + 1)]   # Ex, Ey, Ez
+    sb = [comp(ny), comp(ny + 1), comp(ny)]       # Hx, Hy, Hz
+    return sd, sb
+
+
+def _absorber_case(kh, semantics):
+    """The reference's absorber run (test/test_absorber.jl:84-121): a 4 µm cube
+    at resolution 10 filled by an ε = 1 object, 1 µm PML on both x sides, the
+    low y side and both z sides, a 20-layer absorber on the high y side, a CW
+    Ez point source (fcen 1) at the centre."""
+    src = kh.UniformSource(time_profile=kh.ContinuousWaveSource(fcen=1.0), component=kh.EZ)
+    probe = kh.Simulation(cell_size=(4.0,) * 3, resolution=10, sources=[src], dtype="f64")
+    n, delta = probe.grid.n, probe.grid.delta
+    sd, sb = _absorber_sigma(n, delta[1])
+    ones = [np.ones(n) for _ in range(3)]
+    return kh.Simulation(cell_size=(4.0,) * 3, resolution=10, sources=[src], dtype="f64",
+                         boundaries=[[1.0, 1.0], [1.0, 0.0], [1.0, 1.0]], eps_inv=ones,
+                         sigma_d=sd, sigma_b=sb, semantics=semantics)
+
+
+def test_reference_absorber_run_reaches_a_missing_dispatch(kh, oracle):
+    """The reference's only multi-step test of a PML run on its CPU path,
+    restated.  The absorber marks every region it overlaps as conductive
+    (classify_region_physics, Chunking.jl:219-241), so the chunk with PML
+    along x next to the high-y absorber allocates C_y (PML on prev(y) = x) but
+    no U_y (no PML on next(y) = z); its σ arrays are zero-filled scalars
+    (_slice_or_zero, Chunking.jl:1359-1366), and generic_curl! has no method
+    for C without U with a scalar σ_next (Helpers.jl:39-270), so that run
+    stops with a MethodError on the reference's CPU path.  The oracle, which
+    restates the same dispatch, refuses the configuration at prepare."""
+    sim = _absorber_case(kh, "reference_cpu")
+    spec = sim.spec()
+    assert tuple(spec.n) == (40, 40, 40)
+    assert int(round(2.0 / spec.dt)) == 40  # run(until = 2.0)
+    with pytest.raises(RuntimeError, match="status 6"):
+        oracle.OracleSim(spec)
+
+
+def test_cpu_path_growth_onset_on_the_dipole_grid(kh, oracle):
+    """64³ dipole grid (10-cell CPML, Gaussian Ez dipole), FP64: the CPU-path
+    fields leave the CUDA-path ones between steps 60 and 80 (energy ratio
+    above 1.01), pass a ratio of 1e6 by step 140 and stay finite through step
+    1000.  Mechanism: in a slab with PML along a only, the a-component's own
+    W stage adds (1+σ)W_new − (1−σ)W_old, a gain that the σ_a damping of the
+    other components' T and U stages cancels; the CPU path's method for a
+    component without U (C, U and σD absent, Helpers.jl:208-223) drops its
+    σ_prev = σ_a stage, so the gain is left uncancelled."""
+    from khronos_gb300 import configs
+
+    sims = {}
+    for sem in ("cpml", "reference_cpu"):
+        w = configs.dipole(dtype="f64", steps=1000)
+        w.sim.semantics = sem
+        sims[sem] = oracle.OracleSim(w.sim.spec())
+    ratio = {}
+    for step in range(10, 1001, 10):
+        for o in sims.values():
+            o.step(10)
+        if step in (60, 80, 140, 1000):
+            ratio[step] = _energy(sims["reference_cpu"]) / _energy(sims["cpml"])
+    assert ratio[60] < 1.01 < ratio[80]
+    assert ratio[140] > 1e6
+    assert np.isfinite(ratio[1000]) and ratio[1000] > 1e100
