@@ -858,18 +858,26 @@ class Sim : public SimBase {
       m[q] = &mons_[ids[q]];
       if (m[q]->nf != m[0]->nf) return fail(KH_ERR_INVALID, "flux monitors differ in frequencies");
     }
-    if (kh_status es = wait_idle(); es != KH_OK) return es;
+    // Ordered after this simulation's last batch on its own stream: the
+    // per-frequency buffer comes from the memory pool, the result is copied
+    // into a recycled pinned buffer, and only that stream is waited for.
+    cudaStream_t st = last_stream_;
+    const size_t bytes = sizeof(double) * m[0]->nf;
     double* dout = nullptr;
-    KH_CUDA(kh_host::dev_alloc((void**)&dout, sizeof(double) * m[0]->nf, cudaStreamLegacy));
+    KH_CUDA(kh_host::dev_alloc((void**)&dout, bytes, st));
     kh::launch_flux<T>(m[0]->F, m[1]->F, m[2]->F, m[3]->F, m[0]->C, m[1]->C, m[2]->C, m[3]->C,
-                       m[0]->dims, m[1]->dims, m[2]->dims, m[3]->dims, normal, m[0]->nf, dA, dout,
-                       nullptr);
+                       m[0]->dims, m[1]->dims, m[2]->dims, m[3]->dims, normal, m[0]->nf, dA, dout, st);
     ++launches;
+    double* host = static_cast<double*>(kh_host::pinned_get(bytes));
     cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaMemcpy(out, dout, sizeof(double) * m[0]->nf, cudaMemcpyDeviceToHost);
-    kh_host::dev_free(dout, cudaStreamLegacy);
+    if (e == cudaSuccess && !host) e = cudaErrorMemoryAllocation;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(host, dout, bytes, cudaMemcpyDeviceToHost, st);
+    kh_host::dev_free(dout, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) std::memcpy(out, host, bytes);
+    if (host) kh_host::pinned_put(host, bytes);
     if (e != cudaSuccess) return fail(KH_ERR_CUDA, cudaGetErrorString(e));
-    return KH_OK;
+    return check_device_error();
   }
 
   // flux() with the per-frequency sums in the static device scratch instead of
