@@ -380,6 +380,105 @@ void launch_source_fix(const SourceFixParams<T>& p, void* stream) {
 }
 
 // ---------------------------------------------------------------------------
+// Dispersive and Kerr cells after a LEAN E half-step (DispFixParams).  One
+// thread per cell of planes [k0, k1), x fastest; cells without χ3 or a pole
+// only read their class word.
+template <typename T>
+__global__ void disp_fix_kernel(const DispFixParams<T> p) {
+  const long long nxy = (long long)p.nx * p.ny;
+  const long long total = nxy * (p.k1 - p.k0);
+  for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < total;
+       u += (long long)gridDim.x * blockDim.x) {
+    const int k = p.k0 + int(u / nxy);
+    const long long r = u % nxy;
+    const int j = int(r / p.nx), i = int(r % p.nx);
+    const long long q = p.origin + (long long)k * p.plane + (long long)j * p.pitch + i;
+    if (!KH_IN(q, p.total, 3040)) continue;
+    const uint32_t cls = p.cell_class[q];
+    if (!(cls & (kHasChi3 | kHasPole))) continue;
+    T O[3];
+    if (cls & kHasPole) {
+      // E = ε⁻¹·(D + S − Σ P) (update_field_generic: net = T; net += S; net -= P)
+      T S[3] = {T(0), T(0), T(0)};
+      bool hasS[3] = {false, false, false};
+      if (p.sources_active && (cls & kHasSrcE)) {
+        const int slot = int(cls >> kSlotShift);
+        if (KH_IN(slot + 1, p.n_slots + 1, 3041)) {
+          for (int e = p.slot_off[slot]; e < p.slot_off[slot + 1]; ++e) {
+            if (!KH_IN(e, p.n_ent, 3042) || !KH_IN(p.ent_src[e], p.n_src, 3043)) continue;
+            const int c = p.ent_comp[e];
+            const Cplx<T> am = p.ent_amp[e];
+            const Cplx<T> fv = p.f_now[p.ent_src[e]];
+            const T v = fv.re * am.re - fv.im * am.im;  // real(f(t) · amplitude)
+            if (c >= 0 && c < 3) {
+              S[c] += v;
+              hasS[c] = true;
+            }
+          }
+        }
+      }
+      T Ptot[3] = {T(0), T(0), T(0)};
+      for (int pp = 0; pp < p.npoles; ++pp) {
+        Ptot[0] += p.poles[pp].P[0][q];
+        Ptot[1] += p.poles[pp].P[1][q];
+        Ptot[2] += p.poles[pp].P[2][q];
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        T net = p.D[c][q];
+        if (hasS[c]) net += S[c];
+        net -= Ptot[c];
+        const T m = p.m_inv[c] ? p.m_inv[c][q] : p.m_scalar;
+        O[c] = m * net;
+      }
+    } else {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) O[c] = p.E[c][q];
+    }
+    // χ3 Kerr correction (Dispersive.jl:127-147)
+    if (cls & kHasChi3) {
+      const T c3 = p.chi3[q];
+      if (c3 != T(0)) {
+        const T esq = (O[0] * O[0] + O[1] * O[1]) + O[2] * O[2];
+        const T corr = T(1) / (T(1) + c3 * esq);
+        O[0] = O[0] * corr;
+        O[1] = O[1] * corr;
+        O[2] = O[2] * corr;
+      }
+    }
+    // ADE poles with E^{n+1} (Dispersive.jl:25-88)
+    if (cls & kHasPole) {
+      for (int pp = 0; pp < p.npoles; ++pp) {
+        const PoleParams<T>& P = p.poles[pp];
+        const T s = P.sigma[q];
+        if (s == T(0)) continue;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const T px = P.P[c][q];
+          const T pprev = P.Pprev[c][q];
+          T pn;
+          if (P.is_drude) pn = P.gamma1_inv * ((T(2) * px - P.gamma1 * pprev) + (P.drive * s) * O[c]);
+          else pn = P.gamma1_inv * ((P.coeff_p * px - P.gamma1 * pprev) + (P.drive * s) * O[c]);
+          P.P[c][q] = pn;
+          P.Pprev[c][q] = px;
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) p.E[c][q] = O[c];
+  }
+}
+
+template <typename T>
+void launch_disp_fix(const DispFixParams<T>& p, void* stream) {
+  const long long total = (long long)p.nx * p.ny * (p.k1 - p.k0);
+  if (total <= 0) return;
+  long long blocks = (total + 255) / 256;
+  if (blocks > 152 * 32) blocks = 152 * 32;
+  disp_fix_kernel<T><<<unsigned(blocks), 256, 0, static_cast<cudaStream_t>(stream)>>>(p);
+}
+
+// ---------------------------------------------------------------------------
 // Periodic wrap.  blockIdx.y = 3·axis + component; threads stride over the
 // face's (n_t1 × n_t2) cells; each copies both directions of one cell.
 template <typename T>
@@ -636,6 +735,8 @@ template void launch_record<float>(const RecordParams<float>&, void*);
 template void launch_record<double>(const RecordParams<double>&, void*);
 template void launch_dft<float>(const DftParams<float>&, void*);
 template void launch_dft_batch<float>(const DftBatchParams<float>&, void*);
+template void launch_disp_fix<float>(const DispFixParams<float>&, void*);
+template void launch_disp_fix<double>(const DispFixParams<double>&, void*);
 template void launch_dft_batch<double>(const DftBatchParams<double>&, void*);
 template void launch_dft<double>(const DftParams<double>&, void*);
 template void launch_flux<float>(const Cplx<float>*, const Cplx<float>*, const Cplx<float>*,

@@ -302,6 +302,36 @@ struct SourceFixParams {
   int h_half;
 };
 
+// Dispersive and Kerr cells of a LEAN E half-step (the launch kept their D
+// state, E = ε⁻¹·D): over the z planes [k0, k1) that hold such cells, a pole
+// cell gets E = ε⁻¹·(D − Σ_p P_p), a χ3 cell the Kerr correction, then every
+// pole its ADE update with E^{n+1} — the order and arithmetic of the general
+// cell update (step_curl_and_update!, step_chi3_correction!,
+// step_polarization!; Kernels.jl:76-83).  Pole cells lie outside the CPML
+// (the ADE σ is zeroed there), χ3 cells may lie inside it.
+template <typename T>
+struct DispFixParams {
+  int nx, ny, k0, k1;
+  long long pitch, plane, origin, total;
+  const uint32_t* cell_class;
+  const T* chi3;
+  const T* D[3];
+  T* E[3];
+  const T* m_inv[3];
+  T m_scalar;
+  int npoles;
+  PoleParams<T> poles[kMaxPoles];
+  // source terms of pole cells that are also source cells (a χ3-only source
+  // cell already holds ε⁻¹·(D + S) from the source kernel, which runs first)
+  int sources_active;
+  const int* slot_off;
+  const int* ent_src;
+  const int* ent_comp;
+  const Cplx<T>* ent_amp;
+  const Cplx<T>* f_now;
+  int n_slots, n_ent, n_src;
+};
+
 // DFT accumulation of every monitor of one half-step in one launch
 // (update_dft_monitor!, Monitors.jl:361-379, for all monitors updated at this
 // step): item t of monitor m (t < ncell·nf, cell fastest) is (cell, f).
@@ -348,6 +378,9 @@ void launch_dft(const DftParams<T>& p, void* stream);
 
 template <typename T>
 void launch_dft_batch(const DftBatchParams<T>& p, void* stream);
+
+template <typename T>
+void launch_disp_fix(const DispFixParams<T>& p, void* stream);
 
 // ---- set-up kernels (kh_setup.cu) ----
 // Compact Center-range array (x fastest) → padded layout, converted to T.

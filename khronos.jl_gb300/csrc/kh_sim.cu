@@ -518,6 +518,7 @@ class Sim : public SimBase {
     auto flag = [&](int a, int idx) { return idx < lo_[a] || idx >= n_[a] - hi_[a]; };
     has_src_[0] = has_src_[1] = false;
     src_lean_ok_[0] = src_lean_ok_[1] = true;
+    src_on_dispersive_ = false;
     for (const Ent& e : ents) {
       const int half = e.comp >= 3 ? 1 : 0;
       has_src_[half] = true;
@@ -528,7 +529,7 @@ class Sim : public SimBase {
         const size_t ci = center(e.i, e.j, e.k);
         bool dispersive = !chi3_h_.empty() && chi3_h_[ci] != T(0);
         for (auto& p : poles_) dispersive = dispersive || p.sigma[ci] != T(0);
-        if (dispersive) src_lean_ok_[0] = false;
+        if (dispersive) src_on_dispersive_ = true;
       }
     }
 
@@ -720,6 +721,37 @@ class Sim : public SimBase {
       KH_CUDA(cudaMemcpy(&rf, region_flags, sizeof(rf), cudaMemcpyDeviceToHost));
       special_in_region_[0] = (rf & 1u) != 0;
       special_in_region_[1] = (rf & 2u) != 0;
+    }
+    // χ3 and pole cells updated by the LEAN E launch plus the dispersive-cell
+    // pass, unless something else needs the FULL launch anyway (material
+    // conductivity, the CPU-path semantics with special cells in CPML, or a
+    // periodic axis, whose wrap must see E before the Kerr correction).
+    // KHRONOS_GB300_DISP_FIX=0 keeps them in the FULL launch.
+    {
+      const char* dv = std::getenv("KHRONOS_GB300_DISP_FIX");
+      const bool dispersive = chi3_ != nullptr || !poles_d_.empty();
+      const bool msd_any = msigd_[0] || msigd_[1] || msigd_[2];
+      disp_fix_ = dispersive && !(dv && std::string(dv) == "0") && !msd_any && d_.periodic == 0 &&
+                  !(d_.semantics == KH_SEM_REFERENCE_CPU && special_in_region_[0]) && cls_ != nullptr;
+      if (disp_fix_) {
+        // planes holding χ3 or pole cells
+        int k0 = n_[2], k1 = 0;
+        auto scan = [&](const std::vector<T>& a) {
+          const size_t per = size_t(n_[0]) * n_[1];
+          for (int k = 0; k < n_[2]; ++k) {
+            const T* pl = a.data() + size_t(k) * per;
+            for (size_t q = 0; q < per; ++q)
+              if (pl[q] != T(0)) { k0 = std::min(k0, k); k1 = std::max(k1, k + 1); break; }
+          }
+        };
+        if (!chi3_h_.empty()) scan(chi3_h_);
+        for (auto& pl : poles_) scan(pl.sigma);
+        disp_k0_ = k0 < k1 ? k0 : 0;
+        disp_k1_ = k0 < k1 ? k1 : 0;
+      }
+      // a source on a χ3 or pole cell: LEAN with the dispersive-cell pass,
+      // else the FULL launch while sources are active
+      if (src_on_dispersive_ && !disp_fix_) src_lean_ok_[0] = false;
     }
     prepared_ = true;
     return KH_OK;
@@ -1455,9 +1487,13 @@ class Sim : public SimBase {
     const bool msd = msigd_[0] || msigd_[1] || msigd_[2];
     const bool ref_cpu = d_.semantics == KH_SEM_REFERENCE_CPU;
     const bool full_h_base = msb || (ref_cpu && special_in_region_[1]);
-    const bool full_e_base = msd || chi3_ != nullptr || !poles_d_.empty() || (ref_cpu && special_in_region_[0]);
+    // χ3 and pole cells: in the LEAN E launch plus the dispersive-cell pass
+    // (disp_fix_), or in the FULL launch
+    const bool dispersive = chi3_ != nullptr || !poles_d_.empty();
+    const bool full_e_base = msd || (dispersive && !disp_fix_) || (ref_cpu && special_in_region_[0]);
     const kh::WrapParams<T> wh = wrap_params(true), we = wrap_params(false);
     kh::SourceFixParams<T> fh = fix_params(true), fe = fix_params(false);
+    kh::DispFixParams<T> dfix = disp_params(pe);
     auto issue_all = [&](cudaStream_t st) {
     for (int s = 0; s < nb; ++s) {
       const StepPlan& P = plan[s];
@@ -1492,6 +1528,12 @@ class Sim : public SimBase {
       if (src_e && !pe.full) {
         fe.f_now = dtab + P.fE;
         kh::launch_source_fix<T>(fe, st);
+        ++launches;
+      }
+      if (disp_fix_ && !pe.full) {
+        dfix.sources_active = P.sa ? 1 : 0;
+        dfix.f_now = dtab + P.fE;
+        kh::launch_disp_fix<T>(dfix, st);
         ++launches;
       }
       if (d_.periodic) {
@@ -1824,6 +1866,37 @@ class Sim : public SimBase {
     return f;
   }
 
+  kh::DispFixParams<T> disp_params(const kh::HalfStepParams<T>& pe) const {
+    kh::DispFixParams<T> d;
+    std::memset(&d, 0, sizeof(d));
+    d.nx = n_[0];
+    d.ny = n_[1];
+    d.k0 = disp_k0_;
+    d.k1 = disp_k1_;
+    d.pitch = pitch_;
+    d.plane = plane_;
+    d.origin = origin_;
+    d.total = total_;
+    d.cell_class = cls_;
+    d.chi3 = chi3_;
+    for (int c = 0; c < 3; ++c) {
+      d.D[c] = D_[c];
+      d.E[c] = E_[c];
+      d.m_inv[c] = eps_[c];
+    }
+    d.m_scalar = T(d_.eps_inv);
+    d.npoles = pe.npoles;
+    for (int q = 0; q < kh::kMaxPoles; ++q) d.poles[q] = pe.poles[q];
+    d.slot_off = slot_off_;
+    d.ent_src = ent_src_;
+    d.ent_comp = ent_comp_;
+    d.ent_amp = ent_amp_;
+    d.n_slots = nslots_;
+    d.n_ent = int(ent_amp_h_.size());
+    d.n_src = nsrc_;
+    return d;
+  }
+
   kh::WrapParams<T> wrap_params(bool h) const {
     kh::WrapParams<T> w;
     std::memset(&w, 0, sizeof(w));
@@ -1942,6 +2015,7 @@ class Sim : public SimBase {
   int nsrc_ = 0;
   bool has_src_[2] = {false, false};         // [E half, H half]
   bool src_lean_ok_[2] = {true, true};
+  bool src_on_dispersive_ = false;  // an E source cell carries χ3 or a pole
   bool special_in_region_[2] = {false, false};
   long long* slot_cell_ = nullptr;
   int nslots_ = 0;
@@ -1951,6 +2025,8 @@ class Sim : public SimBase {
   uint32_t stall_tx_ = 0;
   bool use_tma_ = true;
   bool dft_batch_ = true;
+  bool disp_fix_ = false;      // χ3 / pole cells by the dispersive-cell pass after a LEAN E launch
+  int disp_k0_ = 0, disp_k1_ = 0;  // planes that hold them
   int zplanes_ = 10;
   int tma_slots_ = 0;  // SMs × resident TMA-kernel CTAs per SM
   kh::TmaMaps maps_h_, maps_e_;

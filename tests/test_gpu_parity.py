@@ -82,6 +82,31 @@ def test_dispersive_scaled(kh, oracle, gpu_lib, dtype):
     compare(w.sim.spec(), 150, oracle, gpu_lib, TOL[dtype])
 
 
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_dispersive_cells_pass_matches_full_launch(kh, oracle, gpu_lib, dtype, monkeypatch):
+    """χ3 and pole cells updated by the LEAN E launch plus the dispersive-cell
+    pass agree with the FULL launch (KHRONOS_GB300_DISP_FIX=0), which does
+    them in the cell loop, across the source cutoff; both match the oracle."""
+    from khronos_gb300 import configs
+    from khronos_gb300.device import GpuSim
+
+    w = configs.dispersive(dtype=dtype, scale=0.25)
+    spec = w.sim.spec()
+    out = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("KHRONOS_GB300_DISP_FIX", mode)
+        g = GpuSim(spec, lib=gpu_lib)
+        g.step(400)
+        out[mode] = ([g.field(c) for c in range(6)], [g.dft(m) for m in range(len(spec.monitors))])
+        g.close()
+    tol = 1e-13 if dtype == "f64" else 1e-6
+    for a, b in zip(field_errors(out["1"][0], out["0"][0]), [0] * 6):
+        assert a <= tol
+    assert max(dft_errors(out["1"][1], out["0"][1])) <= tol
+    monkeypatch.setenv("KHRONOS_GB300_DISP_FIX", "1")
+    compare(spec, 150, oracle, gpu_lib, TOL[dtype])
+
+
 def _odd_sim(kh, semantics="cpml", dtype="f64", boundaries=((0.3, 0.2), (0.2, 0.4), (0.4, 0.3)), **kw):
     srcs = [
         kh.UniformSource(time_profile=kh.GaussianPulseSource(fcen=0.8, fwidth=0.3), component=kh.EZ,
