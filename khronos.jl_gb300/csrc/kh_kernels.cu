@@ -328,6 +328,31 @@ void launch_half_step(bool h_half, const HalfStepParams<T>& p, void* stream) {
 // Source term of the cells a LEAN half-step updated as B|D-keeping cells:
 // O = m⁻¹·(T + S), the same arithmetic update_field_generic performs
 // (net = T; net += S; A = m⁻¹·net, Helpers.jl:329-347).
+// Component c of source cell q: O = m⁻¹·(T + S), or through the W stage
+// when the cell lies in the CPML of c's own axis (SourceFixParams).
+template <typename T>
+__device__ __forceinline__ void source_fix_one(const SourceFixParams<T>& p, long long q, int c, T S) {
+  const T m = p.m_inv[c] ? p.m_inv[c][q] : p.m_scalar;
+  T net = p.Ts[c][q];
+  net += S;
+  if (p.W[c]) {
+    const long long rel = q - p.origin;
+    const long long k = rel / p.plane, rem = rel % p.plane;
+    const int idx = c == 0 ? int(rem % p.pitch) : (c == 1 ? int(rem / p.pitch) : int(k));
+    if ((idx < p.pml_lo[c] || idx >= p.n[c] - p.pml_hi[c]) && KH_IN(idx, p.n[c], 3031)) {
+      const AxisCoef<T> ao = p.ax[c][idx];
+      if (ao.s != T(0)) {
+        const T wl = p.W[c][q];
+        const T wn = m * net;
+        p.W[c][q] = wn;
+        p.O[c][q] = p.O[c][q] + ao.op * (wn - wl);
+        return;
+      }
+    }
+  }
+  p.O[c][q] = m * net;
+}
+
 template <typename T>
 __global__ void source_fix_kernel(const SourceFixParams<T> p) {
   const int slot = blockIdx.x * blockDim.x + threadIdx.x;
@@ -342,10 +367,7 @@ __global__ void source_fix_kernel(const SourceFixParams<T> p) {
     const Cplx<T> f = p.f_now[pk.src];
     T S = T(0);
     S += f.re * pk.amp.re - f.im * pk.amp.im;
-    const T m = p.m_inv[c] ? p.m_inv[c][q] : p.m_scalar;
-    T net = p.Ts[c][q];
-    net += S;
-    p.O[c][q] = m * net;
+    source_fix_one(p, q, c, S);
     return;
   }
   T S[3] = {T(0), T(0), T(0)};
@@ -363,13 +385,8 @@ __global__ void source_fix_kernel(const SourceFixParams<T> p) {
     else { S[2] += v; has[2] = true; }
   }
 #pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    if (!has[c]) continue;
-    const T m = p.m_inv[c] ? p.m_inv[c][q] : p.m_scalar;
-    T net = p.Ts[c][q];
-    net += S[c];
-    p.O[c][q] = m * net;
-  }
+  for (int c = 0; c < 3; ++c)
+    if (has[c]) source_fix_one(p, q, c, S[c]);
 }
 
 template <typename T>

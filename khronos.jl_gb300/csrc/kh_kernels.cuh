@@ -300,6 +300,14 @@ struct SourceFixParams {
   const T* m_inv[3];
   T m_scalar;
   int h_half;
+  // CUDA-path CPML: a sourced component whose own axis is PML at the cell
+  // has a W stage (update_field_generic, Helpers.jl:333-339).  The LEAN launch
+  // stored w = m⁻¹·T and O = (O_old + (1+σ)·w) − (1−σ)·w_old; with the source
+  // w becomes m⁻¹·(T + S), so O moves by (1+σ)·Δw.
+  T* W[3];
+  const AxisCoef<T>* ax[3];
+  int n[3], pml_lo[3], pml_hi[3];
+  long long pitch, plane, origin;
 };
 
 // Dispersive and Kerr cells of a LEAN E half-step (the launch kept their D

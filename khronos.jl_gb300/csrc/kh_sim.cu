@@ -523,8 +523,10 @@ class Sim : public SimBase {
       const int half = e.comp >= 3 ? 1 : 0;
       has_src_[half] = true;
       const int own = e.comp % 3;
+      // own-axis CPML: a W stage, which the source kernel applies for the
+      // CUDA-path stages; the CPU-path dispatch keeps such cells FULL
       const bool fown = flag(own, own == 0 ? e.i : (own == 1 ? e.j : e.k));
-      if (fown) src_lean_ok_[half] = false;
+      if (fown && d_.semantics == KH_SEM_REFERENCE_CPU) src_lean_ok_[half] = false;
       if (!half) {
         const size_t ci = center(e.i, e.j, e.k);
         bool dispersive = !chi3_h_.empty() && chi3_h_[ci] != T(0);
@@ -1863,6 +1865,17 @@ class Sim : public SimBase {
     }
     f.m_scalar = h ? T(d_.mu_inv) : T(d_.eps_inv);
     f.h_half = h ? 1 : 0;
+    if (d_.semantics == KH_SEM_CPML)
+      for (int c = 0; c < 3; ++c) f.W[c] = h ? WB_[c] : WD_[c];
+    for (int a = 0; a < 3; ++a) {
+      f.ax[a] = h ? axb_[a] : axd_[a];
+      f.n[a] = n_[a];
+      f.pml_lo[a] = lo_[a];
+      f.pml_hi[a] = hi_[a];
+    }
+    f.pitch = pitch_;
+    f.plane = plane_;
+    f.origin = origin_;
     return f;
   }
 
