@@ -398,17 +398,24 @@ void launch_source_fix(const SourceFixParams<T>& p, void* stream) {
 
 // ---------------------------------------------------------------------------
 // Dispersive and Kerr cells after a LEAN E half-step (DispFixParams).  One
-// thread per cell of planes [k0, k1), x fastest; cells without χ3 or a pole
-// only read their class word.
+// warp per row segment of 32·kVN cells of planes [k0, k1); a segment whose
+// special-cell bit is clear is skipped, the others read their class words.
 template <typename T>
 __global__ void disp_fix_kernel(const DispFixParams<T> p) {
-  const long long nxy = (long long)p.nx * p.ny;
-  const long long total = nxy * (p.k1 - p.k0);
-  for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < total;
-       u += (long long)gridDim.x * blockDim.x) {
-    const int k = p.k0 + int(u / nxy);
-    const long long r = u % nxy;
-    const int j = int(r / p.nx), i = int(r % p.nx);
+  const long long seg = (long long)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  const long long nseg = (long long)(p.k1 - p.k0) * p.ny * p.nxb;
+  if (seg >= nseg) return;  // warp-uniform
+  const int xb = int(seg % p.nxb);
+  const long long r = seg / p.nxb;
+  const int j = int(r % p.ny);
+  const int k = p.k0 + int(r / p.ny);
+  const long long w = ((long long)(k >> 6) * p.ny + j) * p.nxb + xb;
+  if (!KH_IN(w, p.n_tile_words, 3044) || !((p.tile_bits[w] >> (k & 63)) & 1ull)) return;
+  const int lane = threadIdx.x & 31;
+#pragma unroll 1
+  for (int v = 0; v < kVN; ++v) {
+    const int i = xb * 32 * kVN + lane * kVN + v;
+    if (i >= p.nx) continue;
     const long long q = p.origin + (long long)k * p.plane + (long long)j * p.pitch + i;
     if (!KH_IN(q, p.total, 3040)) continue;
     const uint32_t cls = p.cell_class[q];
@@ -488,11 +495,10 @@ __global__ void disp_fix_kernel(const DispFixParams<T> p) {
 
 template <typename T>
 void launch_disp_fix(const DispFixParams<T>& p, void* stream) {
-  const long long total = (long long)p.nx * p.ny * (p.k1 - p.k0);
-  if (total <= 0) return;
-  long long blocks = (total + 255) / 256;
-  if (blocks > 152 * 32) blocks = 152 * 32;
-  disp_fix_kernel<T><<<unsigned(blocks), 256, 0, static_cast<cudaStream_t>(stream)>>>(p);
+  const long long nseg = (long long)(p.k1 - p.k0) * p.ny * p.nxb;
+  if (nseg <= 0) return;
+  const int warps = 8;
+  disp_fix_kernel<T><<<unsigned((nseg + warps - 1) / warps), 32 * warps, 0, static_cast<cudaStream_t>(stream)>>>(p);
 }
 
 // ---------------------------------------------------------------------------

@@ -321,6 +321,9 @@ template <typename T>
 struct DispFixParams {
   int nx, ny, k0, k1;
   long long pitch, plane, origin, total;
+  int nxb;                      // row segments of 32·kVN cells per row
+  const uint64_t* tile_bits;    // the E half's special-cell plane masks
+  long long n_tile_words;
   const uint32_t* cell_class;
   const T* chi3;
   const T* D[3];

@@ -1891,6 +1891,9 @@ class Sim : public SimBase {
     d.origin = origin_;
     d.total = total_;
     d.cell_class = cls_;
+    d.nxb = nxb_;
+    d.tile_bits = tbits_e_;
+    d.n_tile_words = (long long)((n_[2] + 63) / 64) * n_[1] * nxb_;
     d.chi3 = chi3_;
     for (int c = 0; c < 3; ++c) {
       d.D[c] = D_[c];
