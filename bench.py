@@ -645,12 +645,14 @@ def run_serving(args, world=1, rank=0, local_rank=0):
     return 0
 
 
-def adjoint_leg(steps=6000, fd_voxels=0, scale=1.0, fp64=True):
+def adjoint_leg(steps=6000, fd_voxels=0, scale=1.0, fp64=True, mode="time", compare_modes=False):
     """Waveguide-bend inverse design (400×400×128, 120×120×22 design voxels,
     5 frequencies): FP32 objective + adjoint gradient wall time through the
-    public API; optionally the FP64 gradient of the same inputs (error of the
-    FP32 gradient) and central finite differences (δρ = 1e-3, FP64) on
-    `fd_voxels` seeded design voxels."""
+    public API in `mode` ("time": windowed, exact for the finite run; "dft":
+    forward DFT fields kept, one adjoint run per frequency); optionally the
+    other mode's FP32 gradient of the same inputs (`compare_modes`), the FP64
+    gradient (error of the FP32 gradient) and central finite differences
+    (δρ = 1e-3, FP64, forward runs only) on `fd_voxels` seeded design voxels."""
     import numpy as np
     import torch
 
@@ -666,7 +668,7 @@ def adjoint_leg(steps=6000, fd_voxels=0, scale=1.0, fp64=True):
     t0 = time.perf_counter()
     e_ref = reference_fields(w)
     t_ref = time.perf_counter() - t0
-    opt = bend_problem(w, e_ref)
+    opt = bend_problem(w, e_ref, mode=mode)
     opt(w.rho0, need_gradient=False)  # creates both simulations (set-up, uploads)
     t0 = time.perf_counter()
     opt.update_design(w.rho0)
@@ -688,6 +690,19 @@ def adjoint_leg(steps=6000, fd_voxels=0, scale=1.0, fp64=True):
         "gcell_per_s": cells * steps * (1 + n_adj) / (t_fwd + t_adj) / 1e9,
         "gpu_launches_fwd_adj": launches,
     })
+    others = {}
+    if compare_modes:
+        other = "dft" if opt.mode == "time" else "time"
+        o2 = bend_problem(w, e_ref, mode=other)
+        t0 = time.perf_counter()
+        _, g_other = o2(w.rho0)
+        others[other] = g_other.copy()
+        o2.close()
+        out["other_mode"] = {"mode": other, "seconds": time.perf_counter() - t0,
+                             "gradient_rel_l2_vs_this_mode": float(np.linalg.norm(g32 - others[other]) /
+                                                                   np.linalg.norm(others[other]))}
+    rng = np.random.default_rng(99)
+    idx = [tuple(int(rng.integers(0, d)) for d in w.design_dims) for _ in range(16)][:fd_voxels]
     if fp64:
         # the FP64 run of the same inputs (FP32 specs promoted)
         o64 = bend_problem(w, reference_fields(w, promote=True), promote=True)
@@ -698,18 +713,23 @@ def adjoint_leg(steps=6000, fd_voxels=0, scale=1.0, fp64=True):
         out["f0_fp64"] = f64
         out["f0_rel_err_fp32"] = abs(f0 - f64) / abs(f64)
         out["gradient_rel_l2_fp32_vs_fp64"] = float(np.linalg.norm(g32 - g64) / np.linalg.norm(g64))
-        if fd_voxels:
-            rng = np.random.default_rng(99)
-            idx = [tuple(int(rng.integers(0, d)) for d in w.design_dims) for _ in range(fd_voxels)]
-            t0 = time.perf_counter()
-            fd = o64.calculate_fd_gradient(w.rho0, idx, db=1e-3)
-            rel = [abs(g64[i] - f) / abs(f) for i, f in zip(idx, fd)]
-            rel32 = [abs(g32[i] - f) / abs(f) for i, f in zip(idx, fd)]
-            out["fd"] = {"voxels": [list(i) for i in idx], "fd": fd.tolist(),
-                         "adjoint_fp64": [float(g64[i]) for i in idx],
-                         "adjoint_fp32": [float(g32[i]) for i in idx],
-                         "rel_err_fp64_max": max(rel), "rel_err_fp32_max": max(rel32),
-                         "seconds": time.perf_counter() - t0, "db": 1e-3}
+    if fd_voxels:
+        # FP64 forward runs only: a DFT-mode problem keeps no time history
+        ofd = bend_problem(w, reference_fields(w, promote=True), promote=True, mode="dft")
+        t0 = time.perf_counter()
+        fd = ofd.calculate_fd_gradient(w.rho0, idx, db=1e-3)
+        rel = lambda g: max(abs(g[i] - f) / abs(f) for i, f in zip(idx, fd))
+        out["fd"] = {"voxels": [list(i) for i in idx], "fd": fd.tolist(),
+                     "adjoint_fp32": [float(g32[i]) for i in idx], "rel_err_fp32_max": rel(g32),
+                     "seconds": time.perf_counter() - t0, "db": 1e-3, "mode": opt.mode}
+        if fp64:
+            out["fd"]["adjoint_fp64"] = [float(g64[i]) for i in idx]
+            out["fd"]["rel_err_fp64_max"] = rel(g64)
+        for m, g in others.items():
+            out["fd"][f"adjoint_fp32_{m}"] = [float(g[i]) for i in idx]
+            out["fd"][f"rel_err_fp32_{m}_max"] = rel(g)
+        ofd.close()
+    if fp64:
         o64.close()
     return out
 
@@ -719,7 +739,8 @@ def run_adjoint(args):
 
     torch.cuda.set_device(0)
     __graft_entry__.package()
-    res = adjoint_leg(args.adjoint_steps, args.adjoint_fd, args.adjoint_scale, not args.adjoint_no_fp64)
+    res = adjoint_leg(args.adjoint_steps, args.adjoint_fd, args.adjoint_scale, not args.adjoint_no_fp64,
+                      args.adjoint_mode, args.adjoint_compare_modes)
     line = {"metric": "adjoint gradient of the waveguide-bend objective (wall time, s)", "unit": "s",
             "value": res["gradient_s"], "higher_is_better": False, "dtype": "f32", "data": "synthetic",
             "n_gpus": 1, "config": {"workload": "waveguide bend inverse design 400x400x128 (scaled by "
@@ -747,6 +768,9 @@ def main(argv=None):
     ap.add_argument("--adjoint-scale", type=float, default=1.0)
     ap.add_argument("--adjoint-fd", type=int, default=0, help="finite-difference voxels (FP64)")
     ap.add_argument("--adjoint-no-fp64", action="store_true")
+    ap.add_argument("--adjoint-mode", choices=["time", "dft"], default="time")
+    ap.add_argument("--adjoint-compare-modes", action="store_true",
+                    help="also the other mode's FP32 gradient of the same inputs")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="waveguide",
                     help="waveguide: the 320x192x128 heterogeneous grid (default); dispersive: 256^3 ADE + chi3")
     args = ap.parse_args(argv)
