@@ -250,8 +250,14 @@ kh_status kh_sim_get_field(kh_sim* sim, int32_t component, double* out);
  * (i, j, k) of the component's dims (the Center range plus the staggered
  * N+1 layer, as kh_sim_get_field) sits at
  *   data + i·strides[0] + j·strides[1] + k·strides[2]   (strides in elements),
- * of type dtype (KH_F32 / KH_F64).  Neighbours at −1 and dims are the zero
- * ghost ring.  The memory belongs to the simulation: valid until
+ * of type dtype (KH_F32 / KH_F64).  Index −1 of every axis is the zero ghost
+ * layer, so the view shifted by one cell per axis is the reference's raw
+ * layout (ghost at raw index 1, interior at 2:N+1, Fields.jl:130-141); the
+ * block holds at least (dims[2] + 1)·strides[2] elements from the ghost cell
+ * (−1, −1, −1), so a dense wrapper of that extent starting there is in
+ * bounds.  Along an axis without the staggered layer, index dims is the high
+ * ghost layer too; along a staggered axis the N+1 layer sits on it and
+ * nothing lies beyond.  The memory belongs to the simulation: valid until
  * kh_sim_destroy, its values current once the steps queued on it have
  * finished (kh_sim_synchronize, or an event on the stepping stream).
  * Writes through it change the simulation; values at cells that keep B/D

@@ -1309,7 +1309,12 @@ class Sim : public SimBase {
     *out = p;
     return KH_OK;
   }
-  kh_status alloc_field(T** out) { return alloc_raw(size_t(total_) * sizeof(T), (void**)out, true); }
+  // One row of slack past the last plane: a dense wrapper that starts at the
+  // (-1, -1, -1) ghost cell of a component and spans dims[2] + 1 whole planes
+  // (the reference's raw layout, kh_sim_field_view) stays inside the block.
+  kh_status alloc_field(T** out) {
+    return alloc_raw(size_t(total_ + pitch_) * sizeof(T), (void**)out, true);
+  }
 
   kh_status upload_raw(const void* h, size_t bytes, void** out) {
     KH_CUDA(kh_host::dev_alloc(out, bytes, cudaStreamLegacy));

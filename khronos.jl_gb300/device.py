@@ -176,16 +176,25 @@ class GpuSim:
         self._check(self.lib.kh_sim_get_field(self.handle, comp, _dptr(out)))
         return out.reshape(dims, order="F")
 
-    def field_view(self, comp: int):
+    def field_view(self, comp: int, ghosted: bool = False):
         """Component `comp` in place on the device as a torch tensor indexed
         [i, j, k] (no copy; strided over the padded layout).  Its values are
         current after synchronize(); it keeps this simulation from being
-        garbage-collected, and is invalid after close()."""
+        garbage-collected, and is invalid after close().
+
+        ``ghosted=True`` starts the view at the (−1, −1, −1) ghost cell, one
+        more cell per axis: the reference's raw field layout with the ghost at
+        index 0 and the interior at 1..N (Fields.jl:130-141; readers take
+        2:N+1 in Julia's 1-based indexing, Visualization.jl:296-302)."""
         import torch
 
         v = _abi.FieldView()
         self._check(self.lib.kh_sim_field_view(self.handle, comp, C.byref(v)))
         item = 4 if v.dtype == _abi.KH_F32 else 8
+        if ghosted:
+            v.data = int(v.data) - item * int(v.strides[0] + v.strides[1] + v.strides[2])
+            for a in range(3):
+                v.dims[a] += 1
 
         class _Holder:
             pass

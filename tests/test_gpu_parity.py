@@ -403,6 +403,15 @@ def test_field_view_is_the_field_in_place(kh, gpu_lib, dtype):
         assert np.array_equal(views[c].double().cpu().numpy(), g.field(c))
         dev = float(torch.sum(views[c].double() ** 2))
         assert math.isclose(dev, norms[c], rel_tol=1e-12, abs_tol=1e-300)
+    # the reference's raw layout (ghost at 0, interior 1..N): what a Julia
+    # shim puts back into sim.fields
+    for c in range(6):
+        gv = g.field_view(c, ghosted=True)
+        host = g.field(c)
+        assert tuple(gv.shape) == tuple(d + 1 for d in host.shape)
+        assert np.array_equal(gv[1:, 1:, 1:].double().cpu().numpy(), host)
+        for a in range(3):
+            assert not torch.any(gv.select(a, 0) != 0)
     del views
     g.close()
 
