@@ -398,25 +398,57 @@ void launch_source_fix(const SourceFixParams<T>& p, void* stream) {
 
 // ---------------------------------------------------------------------------
 // Dispersive and Kerr cells after a LEAN E half-step (DispFixParams).  One
-// warp per row segment of 32·kVN cells of planes [k0, k1); a segment whose
-// special-cell bit is clear is skipped, the others read their class words.
+// warp per entry of the row-segment list (32·kVN cells).  A segment without
+// pole cells needs no class words: its lanes load the pair of E vectors and
+// χ3 values of their two cells at once and correct the cells with χ3 ≠ 0
+// (the cells the LEAN launch left uncorrected).  Pole segments go cell by
+// cell through the class words.
 template <typename T>
 __global__ void disp_fix_kernel(const DispFixParams<T> p) {
-  const long long seg = (long long)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
-  const long long nseg = (long long)(p.k1 - p.k0) * p.ny * p.nxb;
-  if (seg >= nseg) return;  // warp-uniform
+  static_assert(kVN == 2, "paired loads of the χ3 path");
+  const long long w = (long long)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  if (w >= p.n_list) return;  // warp-uniform
+  const uint32_t ent = p.list[w];
+  const long long seg = ent & 0x7fffffffu;
   const int xb = int(seg % p.nxb);
   const long long r = seg / p.nxb;
   const int j = int(r % p.ny);
-  const int k = p.k0 + int(r / p.ny);
-  const long long w = ((long long)(k >> 6) * p.ny + j) * p.nxb + xb;
-  if (!KH_IN(w, p.n_tile_words, 3044) || !((p.tile_bits[w] >> (k & 63)) & 1ull)) return;
+  const int k = int(r / p.ny);
   const int lane = threadIdx.x & 31;
+  const int i0 = xb * 32 * kVN + lane * kVN;
+  const long long q0 = p.origin + (long long)k * p.plane + (long long)j * p.pitch + i0;
+  if (!(ent >> 31)) {
+    if (!p.chi3 || i0 >= p.nx) return;
+    if (i0 + 1 < p.nx && KH_IN(q0 + 1, p.total, 3045)) {
+      using V2 = typename VT<T, 2>::V;  // q0 is even: 8/16-byte aligned
+      const V2 c3 = *reinterpret_cast<const V2*>(p.chi3 + q0);
+      if (c3.x == T(0) && c3.y == T(0)) return;
+      V2 e[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) e[c] = *reinterpret_cast<const V2*>(p.E[c] + q0);
+      // χ3 Kerr correction (Dispersive.jl:127-147), same operation order as below
+      if (c3.x != T(0)) {
+        const T esq = (e[0].x * e[0].x + e[1].x * e[1].x) + e[2].x * e[2].x;
+        const T corr = T(1) / (T(1) + c3.x * esq);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) e[c].x = e[c].x * corr;
+      }
+      if (c3.y != T(0)) {
+        const T esq = (e[0].y * e[0].y + e[1].y * e[1].y) + e[2].y * e[2].y;
+        const T corr = T(1) / (T(1) + c3.y * esq);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) e[c].y = e[c].y * corr;
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) *reinterpret_cast<V2*>(p.E[c] + q0) = e[c];
+      return;
+    }
+  }
 #pragma unroll 1
   for (int v = 0; v < kVN; ++v) {
-    const int i = xb * 32 * kVN + lane * kVN + v;
+    const int i = i0 + v;
     if (i >= p.nx) continue;
-    const long long q = p.origin + (long long)k * p.plane + (long long)j * p.pitch + i;
+    const long long q = q0 + v;
     if (!KH_IN(q, p.total, 3040)) continue;
     const uint32_t cls = p.cell_class[q];
     if (!(cls & (kHasChi3 | kHasPole))) continue;
@@ -454,6 +486,23 @@ __global__ void disp_fix_kernel(const DispFixParams<T> p) {
         net -= Ptot[c];
         const T m = p.m_inv[c] ? p.m_inv[c][q] : p.m_scalar;
         O[c] = m * net;
+        // in the CPML of its own axis the cell's E comes out of the W stage
+        // (update_field_generic, Helpers.jl:333-339): E = E' + op·(W_new − W')
+        // on top of the W' and E' that the LEAN launch (or the source kernel)
+        // left, W_new = ε⁻¹·net
+        if (p.W[c]) {
+          const int idx = c == 0 ? i : (c == 1 ? j : k);
+          const int nn = c == 0 ? p.nx : (c == 1 ? p.ny : p.nz);
+          if ((idx < p.pml_lo[c] || idx >= nn - p.pml_hi[c]) && KH_IN(idx, nn, 3046)) {
+            const AxisCoef<T> ao = p.ax[c][idx];
+            if (ao.s != T(0)) {
+              const T wl = p.W[c][q];
+              const T wn = m * net;
+              p.W[c][q] = wn;
+              O[c] = p.E[c][q] + ao.op * (wn - wl);
+            }
+          }
+        }
       }
     } else {
 #pragma unroll
@@ -495,19 +544,19 @@ __global__ void disp_fix_kernel(const DispFixParams<T> p) {
 
 template <typename T>
 void launch_disp_fix(const DispFixParams<T>& p, void* stream) {
-  const long long nseg = (long long)(p.k1 - p.k0) * p.ny * p.nxb;
-  if (nseg <= 0) return;
+  if (p.n_list <= 0) return;
   const int warps = 8;
-  disp_fix_kernel<T><<<unsigned((nseg + warps - 1) / warps), 32 * warps, 0, static_cast<cudaStream_t>(stream)>>>(p);
+  disp_fix_kernel<T><<<unsigned((p.n_list + warps - 1) / warps), 32 * warps, 0,
+                       static_cast<cudaStream_t>(stream)>>>(p);
 }
 
 // ---------------------------------------------------------------------------
-// Periodic wrap.  blockIdx.y = 3·axis + component; threads stride over the
-// face's (n_t1 × n_t2) cells; each copies both directions of one cell.
+// Periodic wrap.  One block row per periodic axis and component:
+// blockIdx.y = 3·(index of the axis in p.axes) + component; threads stride
+// over the face's (n_t1 × n_t2) cells; each copies both directions of one cell.
 template <typename T>
 __global__ void wrap_kernel(const WrapParams<T> p) {
-  const int a = blockIdx.y / 3, c = blockIdx.y % 3;
-  if (!((p.periodic >> a) & 1u)) return;
+  const int a = p.axes[blockIdx.y / 3], c = blockIdx.y % 3;
   const int t1 = (a + 1) % 3, t2 = (a + 2) % 3;
   const long long st[3] = {1, p.pitch, p.plane};
   const long long face = (long long)p.n[t1] * p.n[t2];
@@ -525,14 +574,19 @@ __global__ void wrap_kernel(const WrapParams<T> p) {
 }
 
 template <typename T>
-void launch_wrap(const WrapParams<T>& p, void* stream) {
-  if (!p.periodic) return;
+void launch_wrap(const WrapParams<T>& p0, void* stream) {
+  if (!(p0.periodic & 7u)) return;
+  WrapParams<T> p = p0;
+  int na = 0;
   long long face = 0;
   for (int a = 0; a < 3; ++a)
-    if ((p.periodic >> a) & 1u) face = std::max(face, (long long)p.n[(a + 1) % 3] * p.n[(a + 2) % 3]);
+    if ((p.periodic >> a) & 1u) {
+      p.axes[na++] = a;
+      face = std::max(face, (long long)p.n[(a + 1) % 3] * p.n[(a + 2) % 3]);
+    }
   const int threads = 256;
   const long long blocks = std::min<long long>((face + threads - 1) / threads, 1024);
-  wrap_kernel<T><<<dim3(unsigned(std::max<long long>(blocks, 1)), 9), threads, 0,
+  wrap_kernel<T><<<dim3(unsigned(std::max<long long>(blocks, 1)), unsigned(3 * na)), threads, 0,
                    static_cast<cudaStream_t>(stream)>>>(p);
 }
 

@@ -133,6 +133,8 @@ struct HalfStepParams {
   int nxb;  // x tiles of 32*VN cells
   int full; // 1: cells with sources/χ3/poles/conductivity handled in-kernel (FULL variant)
   int zplanes;  // z planes marched by one CTA of the TMA-staged kernel
+  int xprefetch;   // TMA-staged kernel, x-CPML state into L2: 0 tile-wide (H half), 1 per lane (H), 2 per lane (H, E)
+  int xpf_dist;    // planes ahead of the per-lane x-CPML prefetch
   T dt, inv_d[3];
   T cd[3];  // Δt·(1/Δ_a): curl coefficients of the TMA-staged kernel
 
@@ -319,11 +321,13 @@ struct SourceFixParams {
 // (the ADE σ is zeroed there), χ3 cells may lie inside it.
 template <typename T>
 struct DispFixParams {
-  int nx, ny, k0, k1;
+  int nx, ny, nz;
   long long pitch, plane, origin, total;
   int nxb;                      // row segments of 32·kVN cells per row
-  const uint64_t* tile_bits;    // the E half's special-cell plane masks
-  long long n_tile_words;
+  // row segments that hold χ3 or pole cells, in grid order: segment index
+  // ((k·ny + j)·nxb + xb), bit 31 set when the segment holds pole cells
+  const uint32_t* list;
+  int n_list;
   const uint32_t* cell_class;
   const T* chi3;
   const T* D[3];
@@ -332,6 +336,11 @@ struct DispFixParams {
   T m_scalar;
   int npoles;
   PoleParams<T> poles[kMaxPoles];
+  // W stage of pole cells in the CPML of their own axis (the LEAN launch
+  // applied it without the polarisation): W auxiliaries and axis coefficients
+  T* W[3];
+  const AxisCoef<T>* ax[3];
+  int pml_lo[3], pml_hi[3];
   // source terms of pole cells that are also source cells (a χ3-only source
   // cell already holds ε⁻¹·(D + S) from the source kernel, which runs first)
   int sources_active;
@@ -371,6 +380,7 @@ struct WrapParams {
   int n[3];
   long long pitch, plane, origin, total;
   uint32_t periodic;
+  int axes[3];  // the periodic axes in order (filled by launch_wrap)
   T* O[3];
   const T* chi3;  // E group: cells with χ3 ≠ 0 already stored their pre-correction value
 };
@@ -427,6 +437,20 @@ struct TileBitsArgs {
   unsigned int* region_flags;  // bit 0: special E cell in a CPML region; bit 1: special H cell
 };
 void launch_tile_bits(const TileBitsArgs& a, void* stream);
+
+// Row-segment list of the dispersive-cell pass (DispFixParams::list), built
+// in grid order on the device: *count entries written to list (capacity
+// n[2]·n[1]·nxb), flags is scratch of one byte per segment.
+struct DispListArgs {
+  int n[3];
+  long long pitch, plane, origin;
+  int nxb;
+  const uint32_t* cls;
+  unsigned char* flags;
+  uint32_t* list;
+  int* count;
+};
+void launch_disp_list(const DispListArgs& a, void* stream);
 
 // DFT accumulators (with Kahan compensation C, or nullptr) → interleaved
 // (re, im) doubles, value = F − C.

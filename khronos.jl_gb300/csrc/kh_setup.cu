@@ -91,6 +91,57 @@ __global__ void tile_bits_kernel(const TileBitsArgs a) {
   }
 }
 
+// One warp per row segment: flag 2 when it holds a pole cell, 1 when it holds
+// χ3 cells only, 0 otherwise.
+__global__ void disp_flags_kernel(const DispListArgs a) {
+  const long long seg = (long long)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  const long long nseg = (long long)a.n[2] * a.n[1] * a.nxb;
+  if (seg >= nseg) return;  // warp-uniform
+  const int lane = threadIdx.x & 31;
+  const int xb = int(seg % a.nxb);
+  const long long r = seg / a.nxb;
+  const int j = int(r % a.n[1]);
+  const int k = int(r / a.n[1]);
+  bool c3 = false, pl = false;
+#pragma unroll
+  for (int v = 0; v < kVN; ++v) {
+    const int i = xb * 32 * kVN + lane * kVN + v;
+    if (i >= a.n[0]) continue;
+    const uint32_t c = a.cls[a.origin + (long long)k * a.plane + (long long)j * a.pitch + i];
+    c3 |= (c & kHasChi3) != 0;
+    pl |= (c & kHasPole) != 0;
+  }
+  const bool apl = __any_sync(0xffffffffu, pl), ac3 = __any_sync(0xffffffffu, c3);
+  if (lane == 0) a.flags[seg] = apl ? 2 : (ac3 ? 1 : 0);
+}
+
+// Ordered compaction of the flagged segments by one block: thread t scans a
+// contiguous chunk, a shared-memory prefix sum gives its first output slot.
+constexpr int kCompactThreads = 1024;
+__global__ void __launch_bounds__(kCompactThreads) compact_segments_kernel(const DispListArgs a) {
+  __shared__ int part[kCompactThreads];
+  const long long nseg = (long long)a.n[2] * a.n[1] * a.nxb;
+  const long long chunk = (nseg + kCompactThreads - 1) / kCompactThreads;
+  const long long b = (long long)threadIdx.x * chunk;
+  const long long e = b + chunk < nseg ? b + chunk : nseg;
+  int n = 0;
+  for (long long q = b; q < e; ++q) n += a.flags[q] != 0;
+  part[threadIdx.x] = n;
+  __syncthreads();
+  for (int off = 1; off < kCompactThreads; off <<= 1) {
+    const int v = threadIdx.x >= off ? part[threadIdx.x - off] : 0;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  int pos = part[threadIdx.x] - n;
+  for (long long q = b; q < e; ++q) {
+    const unsigned char f = a.flags[q];
+    if (f) a.list[pos++] = uint32_t(q) | (f == 2 ? 0x80000000u : 0u);
+  }
+  if (threadIdx.x == kCompactThreads - 1) *a.count = part[threadIdx.x];
+}
+
 template <typename T>
 __global__ void dft_read_kernel(const Cplx<T>* __restrict__ F, const Cplx<T>* __restrict__ C, double* out,
                                 long long n) {
@@ -136,6 +187,14 @@ void launch_tile_bits(const TileBitsArgs& a, void* stream) {
   if (nseg <= 0) return;
   const int warps = 8;
   tile_bits_kernel<<<unsigned((nseg + warps - 1) / warps), 32 * warps, 0, static_cast<cudaStream_t>(stream)>>>(a);
+}
+
+void launch_disp_list(const DispListArgs& a, void* stream) {
+  const long long nseg = (long long)a.n[2] * a.n[1] * a.nxb;
+  if (nseg <= 0) return;
+  const int warps = 8;
+  disp_flags_kernel<<<unsigned((nseg + warps - 1) / warps), 32 * warps, 0, static_cast<cudaStream_t>(stream)>>>(a);
+  compact_segments_kernel<<<1, kCompactThreads, 0, static_cast<cudaStream_t>(stream)>>>(a);
 }
 
 template <typename T>

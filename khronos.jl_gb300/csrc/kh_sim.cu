@@ -713,6 +713,8 @@ class Sim : public SimBase {
     dft_batch_ = !(bv && std::string(bv) == "0");
     if (use_tma_) KH_TRY(build_tma_maps());
     zplanes_ = choose_zplanes();
+    if (const char* xv = std::getenv("KHRONOS_GB300_XPREFETCH")) xprefetch_ = std::min(2, std::max(0, std::atoi(xv)));
+    if (const char* dv = std::getenv("KHRONOS_GB300_XPF_DIST")) xpf_dist_ = std::min(8, std::max(1, std::atoi(dv)));
     if (const char* sv = std::getenv("KHRONOS_GB300_TEST_STALL")) stall_tx_ = std::string(sv) == "1" ? 16u : 0u;
     // the zeroing and uploads above ran on the legacy default stream; wait for
     // them only (work of other simulations on non-blocking streams goes on)
@@ -735,21 +737,32 @@ class Sim : public SimBase {
       const bool msd_any = msigd_[0] || msigd_[1] || msigd_[2];
       disp_fix_ = dispersive && !(dv && std::string(dv) == "0") && !msd_any && d_.periodic == 0 &&
                   !(d_.semantics == KH_SEM_REFERENCE_CPU && special_in_region_[0]) && cls_ != nullptr;
+      const long long nseg = (long long)n_[2] * n_[1] * nxb_;
+      if (disp_fix_ && nseg >= (1LL << 31)) disp_fix_ = false;  // list entries carry 31-bit indices
       if (disp_fix_) {
-        // planes holding χ3 or pole cells
-        int k0 = n_[2], k1 = 0;
-        auto scan = [&](const std::vector<T>& a) {
-          const size_t per = size_t(n_[0]) * n_[1];
-          for (int k = 0; k < n_[2]; ++k) {
-            const T* pl = a.data() + size_t(k) * per;
-            for (size_t q = 0; q < per; ++q)
-              if (pl[q] != T(0)) { k0 = std::min(k0, k); k1 = std::max(k1, k + 1); break; }
-          }
-        };
-        if (!chi3_h_.empty()) scan(chi3_h_);
-        for (auto& pl : poles_) scan(pl.sigma);
-        disp_k0_ = k0 < k1 ? k0 : 0;
-        disp_k1_ = k0 < k1 ? k1 : 0;
+        // the row segments holding χ3 or pole cells, in grid order
+        unsigned char* flags = nullptr;
+        KH_CUDA(kh_host::dev_alloc((void**)&flags, size_t(nseg), cudaStreamLegacy));
+        int* cnt = nullptr;
+        KH_TRY(alloc_raw(size_t(nseg) * sizeof(uint32_t), (void**)&disp_list_, false));
+        KH_TRY(alloc_raw(sizeof(int), (void**)&cnt, false));
+        kh::DispListArgs la;
+        for (int a = 0; a < 3; ++a) la.n[a] = n_[a];
+        la.pitch = pitch_;
+        la.plane = plane_;
+        la.origin = origin_;
+        la.nxb = nxb_;
+        la.cls = cls_;
+        la.flags = flags;
+        la.list = disp_list_;
+        la.count = cnt;
+        kh::launch_disp_list(la, cudaStreamLegacy);
+        cudaError_t e = cudaGetLastError();
+        int count = 0;
+        if (e == cudaSuccess) e = cudaMemcpy(&count, cnt, sizeof(int), cudaMemcpyDeviceToHost);
+        kh_host::dev_free(flags, cudaStreamLegacy);
+        if (e != cudaSuccess) return fail(KH_ERR_CUDA, std::string("segment list: ") + cudaGetErrorString(e));
+        n_disp_list_ = count;
       }
       // a source on a χ3 or pole cell: LEAN with the dispersive-cell pass,
       // else the FULL launch while sources are active
@@ -1889,16 +1902,15 @@ class Sim : public SimBase {
     std::memset(&d, 0, sizeof(d));
     d.nx = n_[0];
     d.ny = n_[1];
-    d.k0 = disp_k0_;
-    d.k1 = disp_k1_;
+    d.nz = n_[2];
     d.pitch = pitch_;
     d.plane = plane_;
     d.origin = origin_;
     d.total = total_;
     d.cell_class = cls_;
     d.nxb = nxb_;
-    d.tile_bits = tbits_e_;
-    d.n_tile_words = (long long)((n_[2] + 63) / 64) * n_[1] * nxb_;
+    d.list = disp_list_;
+    d.n_list = n_disp_list_;
     d.chi3 = chi3_;
     for (int c = 0; c < 3; ++c) {
       d.D[c] = D_[c];
@@ -1908,6 +1920,12 @@ class Sim : public SimBase {
     d.m_scalar = T(d_.eps_inv);
     d.npoles = pe.npoles;
     for (int q = 0; q < kh::kMaxPoles; ++q) d.poles[q] = pe.poles[q];
+    for (int c = 0; c < 3; ++c) {
+      d.W[c] = pe.cpml ? pe.W[c] : nullptr;  // the CPU-path semantics do not use the pass in a CPML region
+      d.ax[c] = pe.ax[c];
+      d.pml_lo[c] = pe.pml_lo[c];
+      d.pml_hi[c] = pe.pml_hi[c];
+    }
     d.slot_off = slot_off_;
     d.ent_src = ent_src_;
     d.ent_comp = ent_comp_;
@@ -1944,6 +1962,8 @@ class Sim : public SimBase {
     p.total = total_;
     p.nxb = nxb_;
     p.zplanes = zplanes_;
+    p.xprefetch = xprefetch_;
+    p.xpf_dist = xpf_dist_;
     p.dt = dt_;
     for (int a = 0; a < 3; ++a) {
       p.inv_d[a] = T(1) / delta_[a];
@@ -2047,8 +2067,11 @@ class Sim : public SimBase {
   bool use_tma_ = true;
   bool dft_batch_ = true;
   bool disp_fix_ = false;      // χ3 / pole cells by the dispersive-cell pass after a LEAN E launch
-  int disp_k0_ = 0, disp_k1_ = 0;  // planes that hold them
+  uint32_t* disp_list_ = nullptr;  // its row-segment list (DispFixParams::list)
+  int n_disp_list_ = 0;
   int zplanes_ = 10;
+  int xprefetch_ = 2;        // x-CPML state prefetch mode (HalfStepParams::xprefetch)
+  int xpf_dist_ = 3;
   int tma_slots_ = 0;  // SMs × resident TMA-kernel CTAs per SM
   kh::TmaMaps maps_h_, maps_e_;
 

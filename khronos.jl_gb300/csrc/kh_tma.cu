@@ -91,6 +91,10 @@ __device__ __forceinline__ void tma_prefetch_3d(const CUtensorMap* map, int x, i
                : "memory");
 }
 
+__device__ __forceinline__ void l2_prefetch(const void* ptr) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(ptr));
+}
+
 template <typename T>
 struct TmaGeom {
   static constexpr int HX = 16 / int(sizeof(T));  // x halo = XOFF of the layout
@@ -219,7 +223,7 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
       // prefetch pays off on the H half, while the E half, which runs at its
       // DRAM limit, loses more to the unused bytes than it gains.
       const bool tfz = plane < p.pml_lo[2] || plane >= p.nz - p.pml_hi[2];
-      if (!FULL && (tfy || tfz || (H && tfx))) {
+      if (!FULL && (tfy || tfz || (H && tfx && p.xprefetch == 0))) {
         const bool af[3] = {tfx, tfy, tfz};
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
@@ -273,6 +277,22 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
           KH_IN(tb_base + (long long)((k + 1) >> 6) * tb_group, p.n_tile_words, 2009))
         tbits = tb_row[(long long)((k + 1) >> 6) * tb_group];
       load_aux<T, H, FULL>(p, nxt, k + 1, row, lane_ok, fy, anyfx, tbits);
+    }
+    // x-CPML lanes of rows outside the y and z CPML: their own state into L2
+    // xpf_dist planes ahead (the tile-wide prefetch above would also pull the
+    // columns that keep no state)
+    if (!FULL && p.xprefetch > (H ? 0 : 1) && anyfx && !fy && lane_ok) {
+      const int kp = k + p.xpf_dist;
+      if (kp < k1 && !(kp < p.pml_lo[2] || kp >= p.nz - p.pml_hi[2])) {
+        const long long qp = row + (long long)kp * p.plane;
+        if (KH_IN(qp + 1, p.total, 2015)) {
+#pragma unroll
+          for (int cc = 0; cc < 3; ++cc)
+            if (p.Ts[cc]) l2_prefetch(p.Ts[cc] + qp);
+          if (p.U[2]) l2_prefetch(p.U[2] + qp);
+          if (p.W[0]) l2_prefetch(p.W[0] + qp);
+        }
+      }
     }
     const int ncur = H ? c : c + 1;
     const int nnb = H ? c + 1 : c;

@@ -107,6 +107,50 @@ def test_dispersive_cells_pass_matches_full_launch(kh, oracle, gpu_lib, dtype, m
     compare(spec, 150, oracle, gpu_lib, TOL[dtype])
 
 
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_dispersive_cells_pass_on_an_odd_grid(kh, oracle, gpu_lib, dtype, monkeypatch):
+    """The dispersive-cell pass on a grid whose x extent is odd (the last lane
+    of a row has one cell), with χ3-only row segments, pole segments and a
+    12%-filled χ3 mix inside and outside the CPML: same as the FULL launch and
+    the oracle."""
+    from khronos_gb300 import grid as G
+    from khronos_gb300.device import GpuSim
+    from khronos_gb300.simulation import apply_chi1_correction
+    from khronos_gb300.spec import DrudeSusceptibility, LorentzianSusceptibility
+
+    rng = np.random.default_rng(11)
+    n = (37, 22, 18)
+    chi3 = np.where(rng.uniform(size=n) > 0.88, 0.04, 0.0)
+    chi3[:, :, 8:11] = 0.02  # whole χ3 planes: segments without pole cells
+    lor, dru = LorentzianSusceptibility(1.0, 0.05, 1.0), DrudeSusceptibility(0.1, 40.0)
+    sl = np.zeros(n)
+    sl[25:37, 3:9, 4:12] = lor.sigma
+    sd = np.zeros(n)
+    sd[2:7, 12:20, 6:14] = dru.sigma
+    poles = [(lor, sl), (dru, sd)]
+    dt = G.Grid.build((3.7, 2.2, 1.8), (0, 0, 0), 10, dtype).dt
+    eps = apply_chi1_correction([1.0 / rng.uniform(1.0, 3.0, size=n) for _ in range(3)], poles, dt, T=np.float64)
+    src = kh.UniformSource(time_profile=kh.GaussianPulseSource(fcen=0.8, fwidth=0.4), component=kh.EZ,
+                           center=(0.2, 0, 0), size=(0.4, 0.6, 0.5), amplitude=3.0)
+    mon = kh.DFTMonitor(component=kh.EX, center=(0, 0, 0), size=(3.7, 2.2, 0), frequencies=[0.7, 0.9])
+    sim = kh.Simulation(cell_size=(3.7, 2.2, 1.8), resolution=10, sources=[src], monitors=[mon],
+                        boundaries=[[0.3, 0.3]] * 3, dtype=dtype, eps_inv=eps, chi3=chi3, poles=poles)
+    spec = sim.spec()
+    assert tuple(spec.n) == n
+    out = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("KHRONOS_GB300_DISP_FIX", mode)
+        g = GpuSim(spec, lib=gpu_lib)
+        g.step(160)
+        out[mode] = ([g.field(c) for c in range(6)], [g.dft(0)])
+        g.close()
+    tol = 1e-13 if dtype == "f64" else 1e-6
+    assert max(field_errors(out["1"][0], out["0"][0])) <= tol
+    assert max(dft_errors(out["1"][1], out["0"][1])) <= tol
+    monkeypatch.setenv("KHRONOS_GB300_DISP_FIX", "1")
+    compare(spec, 160, oracle, gpu_lib, TOL[dtype])
+
+
 def _odd_sim(kh, semantics="cpml", dtype="f64", boundaries=((0.3, 0.2), (0.2, 0.4), (0.4, 0.3)), **kw):
     srcs = [
         kh.UniformSource(time_profile=kh.GaussianPulseSource(fcen=0.8, fwidth=0.3), component=kh.EZ,
