@@ -421,11 +421,13 @@ __global__ void disp_fix_kernel(const DispFixParams<T> p) {
     if (!p.chi3 || i0 >= p.nx) return;
     if (i0 + 1 < p.nx && KH_IN(q0 + 1, p.total, 3045)) {
       using V2 = typename VT<T, 2>::V;  // q0 is even: 8/16-byte aligned
+      // the E pair is loaded with the χ3 pair (one round trip, not two):
+      // in a Kerr segment nearly every cell has χ3
       const V2 c3 = *reinterpret_cast<const V2*>(p.chi3 + q0);
-      if (c3.x == T(0) && c3.y == T(0)) return;
       V2 e[3];
 #pragma unroll
       for (int c = 0; c < 3; ++c) e[c] = *reinterpret_cast<const V2*>(p.E[c] + q0);
+      if (c3.x == T(0) && c3.y == T(0)) return;
       // χ3 Kerr correction (Dispersive.jl:127-147), same operation order as below
       if (c3.x != T(0)) {
         const T esq = (e[0].x * e[0].x + e[1].x * e[1].x) + e[2].x * e[2].x;
