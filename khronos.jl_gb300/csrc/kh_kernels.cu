@@ -749,12 +749,14 @@ __device__ __forceinline__ void avg_at(const Cplx<T>* F, const Cplx<T>* C, const
   }
 }
 
+constexpr int kFluxCellsPerBlock = 1024;
+
 template <typename T>
-__global__ void flux_kernel(const Cplx<T>* e1, const Cplx<T>* e2, const Cplx<T>* h1,
-                            const Cplx<T>* h2, const Cplx<T>* ce1, const Cplx<T>* ce2,
-                            const Cplx<T>* ch1, const Cplx<T>* ch2, const FluxArgs a,
-                            double* out) {
-  const int f = blockIdx.x;
+__global__ void flux_partial_kernel(const Cplx<T>* e1, const Cplx<T>* e2, const Cplx<T>* h1,
+                                    const Cplx<T>* h2, const Cplx<T>* ce1, const Cplx<T>* ce2,
+                                    const Cplx<T>* ch1, const Cplx<T>* ch2, const FluxArgs a,
+                                    double* partial) {
+  const int f = blockIdx.y;
   const int n = a.normal;
   const int a1 = n == 0 ? 1 : 0;
   const int a2 = n == 2 ? 1 : 2;
@@ -763,8 +765,13 @@ __global__ void flux_kernel(const Cplx<T>* e1, const Cplx<T>* e2, const Cplx<T>*
     n1 = min(n1, a.d[m][a1]);
     n2 = min(n2, a.d[m][a2]);
   }
+  const long long cells = (long long)n1 * n2;
+  // block b takes cells [b·span, (b+1)·span), span a multiple of blockDim
+  const long long span = ((cells + gridDim.x - 1) / gridDim.x + blockDim.x - 1) / blockDim.x * blockDim.x;
+  const long long t0 = (long long)blockIdx.x * span;
+  const long long t1 = t0 + span < cells ? t0 + span : cells;
   double acc = 0.0;
-  for (long long t = threadIdx.x; t < (long long)n1 * n2; t += blockDim.x) {
+  for (long long t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
     const int i1 = int(t % n1), i2 = int(t / n1);
     double E1r, E1i, E2r, E2i, H1r, H1i, H2r, H2i;
     avg_at(e1, ce1, a.d[0], n, a1, a2, i1, i2, f, E1r, E1i);
@@ -781,7 +788,27 @@ __global__ void flux_kernel(const Cplx<T>* e1, const Cplx<T>* e2, const Cplx<T>*
     if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
     __syncthreads();
   }
-  if (threadIdx.x == 0) out[f] = red[0];
+  if (threadIdx.x == 0) partial[(long long)f * gridDim.x + blockIdx.x] = red[0];
+}
+
+// One warp per frequency: lane l adds partials l, l+32, … in order, then a
+// fixed shuffle tree.
+__global__ void flux_final_kernel(const double* partial, int nb, double* out) {
+  const int f = blockIdx.x;
+  const int lane = threadIdx.x;
+  double s = 0.0;
+  for (int b = lane; b < nb; b += 32) s += partial[(long long)f * nb + b];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (lane == 0) out[f] = s;
+}
+
+int flux_blocks(long long cells, int nf, int partial_cap) {
+  long long b = (cells + kFluxCellsPerBlock - 1) / kFluxCellsPerBlock;
+  const long long fill = (4LL * 152 + nf - 1) / (nf > 0 ? nf : 1);  // about four blocks per SM in all
+  if (b > fill) b = fill;
+  if (nf > 0 && b > partial_cap / nf) b = partial_cap / nf;
+  return int(b < 1 ? 1 : b);
 }
 
 template <typename T>
@@ -789,7 +816,7 @@ void launch_flux(const Cplx<T>* e1, const Cplx<T>* e2, const Cplx<T>* h1, const 
                  const Cplx<T>* c_e1, const Cplx<T>* c_e2, const Cplx<T>* c_h1,
                  const Cplx<T>* c_h2, const int dims_e1[3], const int dims_e2[3],
                  const int dims_h1[3], const int dims_h2[3], int normal_axis, int nf, double dA,
-                 double* out, void* stream) {
+                 double* out, double* partial, int partial_cap, void* stream) {
   FluxArgs a;
   for (int q = 0; q < 3; ++q) {
     a.d[0][q] = dims_e1[q];
@@ -800,8 +827,18 @@ void launch_flux(const Cplx<T>* e1, const Cplx<T>* e2, const Cplx<T>* h1, const 
   a.normal = normal_axis;
   a.nf = nf;
   a.dA = dA;
-  flux_kernel<T><<<nf, 256, 0, static_cast<cudaStream_t>(stream)>>>(e1, e2, h1, h2, c_e1, c_e2,
-                                                                      c_h1, c_h2, a, out);
+  if (nf <= 0) return;
+  const int na1 = normal_axis == 0 ? 1 : 0, na2 = normal_axis == 2 ? 1 : 2;
+  long long n1 = dims_e1[na1], n2 = dims_e1[na2];
+  for (const int* d : {dims_e2, dims_h1, dims_h2}) {
+    n1 = std::min<long long>(n1, d[na1]);
+    n2 = std::min<long long>(n2, d[na2]);
+  }
+  const int nb = flux_blocks(n1 * n2, nf, partial_cap);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  flux_partial_kernel<T><<<dim3(unsigned(nb), unsigned(nf)), 256, 0, st>>>(e1, e2, h1, h2, c_e1, c_e2, c_h1,
+                                                                          c_h2, a, partial);
+  flux_final_kernel<<<unsigned(nf), 32, 0, st>>>(partial, nb, out);
 }
 
 template void launch_half_step<float>(bool, const HalfStepParams<float>&, void*);
@@ -821,10 +858,10 @@ template void launch_dft<double>(const DftParams<double>&, void*);
 template void launch_flux<float>(const Cplx<float>*, const Cplx<float>*, const Cplx<float>*,
                                  const Cplx<float>*, const Cplx<float>*, const Cplx<float>*,
                                  const Cplx<float>*, const Cplx<float>*, const int*, const int*,
-                                 const int*, const int*, int, int, double, double*, void*);
+                                 const int*, const int*, int, int, double, double*, double*, int, void*);
 template void launch_flux<double>(const Cplx<double>*, const Cplx<double>*, const Cplx<double>*,
                                   const Cplx<double>*, const Cplx<double>*, const Cplx<double>*,
                                   const Cplx<double>*, const Cplx<double>*, const int*, const int*,
-                                  const int*, const int*, int, int, double, double*, void*);
+                                  const int*, const int*, int, int, double, double*, double*, int, void*);
 
 }  // namespace kh

@@ -457,12 +457,17 @@ void launch_disp_list(const DispListArgs& a, void* stream);
 template <typename T>
 void launch_dft_read(const Cplx<T>* F, const Cplx<T>* C, double* out, long long n, void* stream);
 
-// FP64 flux reduction: one block per frequency.
+// FP64 flux reduction in two passes with a fixed summation order: blocks of
+// 1024 cells per frequency write partial sums into `partial` (room for
+// partial_cap doubles; at most partial_cap / nf blocks per frequency), one
+// warp per frequency adds them in block order into out[f].
 template <typename T>
 void launch_flux(const Cplx<T>* e1, const Cplx<T>* e2, const Cplx<T>* h1, const Cplx<T>* h2,
                  const Cplx<T>* c_e1, const Cplx<T>* c_e2, const Cplx<T>* c_h1,
                  const Cplx<T>* c_h2, const int dims_e1[3], const int dims_e2[3],
                  const int dims_h1[3], const int dims_h2[3], int normal_axis, int nf, double dA,
-                 double* out, void* stream);
+                 double* out, double* partial, int partial_cap, void* stream);
+// Blocks per frequency launch_flux uses for a plane of `cells` cells.
+int flux_blocks(long long cells, int nf, int partial_cap);
 
 }  // namespace kh

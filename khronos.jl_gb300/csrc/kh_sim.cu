@@ -35,12 +35,16 @@ const char* kVersion = "khronos_gb300 1.0 (sm_103a)";
 constexpr int kMaxDevices = 64;
 
 // Device scratch of kh_sim_flux_static: the per-frequency flux sums of one
-// call.  Fixed size (kFluxStaticMaxFreqs doubles = 32 KB per device), shared
-// by every simulation in the process on that device; it keeps the last
-// call's values.  The flux kernel writes every entry 0..nf-1 before the copy
-// reads them, so nothing has to start at zero.
+// call followed by the per-block partial sums of the reduction.  Fixed size
+// (kFluxStaticMaxFreqs + kFluxStaticPartials doubles = 288 KB per device),
+// shared by every simulation in the process on that device; it keeps the
+// last call's values.  The flux kernels write every entry they read, so
+// nothing has to start at zero.
 constexpr int kFluxStaticMaxFreqs = 4096;
-static __device__ __align__(256) double g_flux_static_scratch[kFluxStaticMaxFreqs];
+constexpr int kFluxStaticPartials = 8 * kFluxStaticMaxFreqs;
+static __device__ __align__(256) double g_flux_static_scratch[kFluxStaticMaxFreqs + kFluxStaticPartials];
+// Partial sums of kh_sim_flux per frequency (blocks per frequency at most).
+constexpr int kFluxMaxBlocks = 64;
 
 // Device address of g_flux_static_scratch, resolved once per device with that
 // device current (the first kh_sim_flux_static call on the device).
@@ -910,10 +914,12 @@ class Sim : public SimBase {
     // into a recycled pinned buffer, and only that stream is waited for.
     cudaStream_t st = last_stream_;
     const size_t bytes = sizeof(double) * m[0]->nf;
+    const int cap = kFluxMaxBlocks * m[0]->nf;
     double* dout = nullptr;
-    KH_CUDA(kh_host::dev_alloc((void**)&dout, bytes, st));
+    KH_CUDA(kh_host::dev_alloc((void**)&dout, bytes + sizeof(double) * size_t(cap), st));
     kh::launch_flux<T>(m[0]->F, m[1]->F, m[2]->F, m[3]->F, m[0]->C, m[1]->C, m[2]->C, m[3]->C,
-                       m[0]->dims, m[1]->dims, m[2]->dims, m[3]->dims, normal, m[0]->nf, dA, dout, st);
+                       m[0]->dims, m[1]->dims, m[2]->dims, m[3]->dims, normal, m[0]->nf, dA, dout,
+                       dout + m[0]->nf, cap, st);
     ++launches;
     double* host = static_cast<double*>(kh_host::pinned_get(bytes));
     cudaError_t e = cudaGetLastError();
@@ -949,6 +955,7 @@ class Sim : public SimBase {
     if (st != KH_OK) return st;
     kh::launch_flux<T>(m[0]->F, m[1]->F, m[2]->F, m[3]->F, m[0]->C, m[1]->C, m[2]->C, m[3]->C,
                        m[0]->dims, m[1]->dims, m[2]->dims, m[3]->dims, normal, nf, dA, scratch,
+                       scratch + kFluxStaticMaxFreqs, std::min(kFluxStaticPartials, kFluxMaxBlocks * nf),
                        nullptr);
     ++launches;
     cudaError_t e = cudaGetLastError();
