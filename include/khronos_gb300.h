@@ -285,7 +285,8 @@ kh_status kh_sim_flux(kh_sim* sim, const int32_t ids[4], int32_t normal_axis, do
  * pool, and a process whose device memory is fully committed to its
  * simulations may have nothing left for even that small allocation (nor may
  * code that forbids allocations inside its own critical sections).  The
- * per-frequency sums go to a fixed device array inside the library instead:
+ * per-frequency sums and the reduction's partial sums go to a fixed device
+ * array inside the library instead:
  * at most 4096 frequencies (more returns KH_ERR_INVALID; use kh_sim_flux).
  * The first call on each device does a one-time set-up (it resolves that
  * array's device address with the device current); make it before any

@@ -464,12 +464,36 @@ class Sim : public SimBase {
       KH_TRY(alloc_field(&E_[c]));
       KH_TRY(alloc_field(&H_[c]));
     }
+    // materials: compact uploads scattered into the padded layout on the device,
+    // queued before the host builds the source table so the copies overlap it
+    if (geo_set_) KH_TRY(build_geometry());
+    const int tdt = sizeof(T) == 4 ? KH_F32 : KH_F64;
+    for (int c = 0; c < 3; ++c) {
+      if (att_eps_[c].ptr) KH_TRY(upload_center(att_eps_[c].ptr, att_eps_[c].dtype, &eps_[c]));
+      else if (!eps_h_[c].empty()) KH_TRY(upload_center(eps_h_[c].data(), tdt, &eps_[c]));
+      if (att_mu_[c].ptr) KH_TRY(upload_center(att_mu_[c].ptr, att_mu_[c].dtype, &mu_[c]));
+      else if (!mu_h_[c].empty()) KH_TRY(upload_center(mu_h_[c].data(), tdt, &mu_[c]));
+      if (!msigd_h_[c].empty()) KH_TRY(upload_center(msigd_h_[c].data(), tdt, &msigd_[c]));
+      if (!msigb_h_[c].empty()) KH_TRY(upload_center(msigb_h_[c].data(), tdt, &msigb_[c]));
+    }
+    if ((eps_[0] != nullptr) != (eps_[2] != nullptr) || (eps_[0] != nullptr) != (eps_[1] != nullptr))
+      return fail(KH_ERR_INVALID, "per-voxel ε⁻¹ must be given for all three components");
+    if ((mu_[0] != nullptr) != (mu_[2] != nullptr) || (mu_[0] != nullptr) != (mu_[1] != nullptr))
+      return fail(KH_ERR_INVALID, "per-voxel μ⁻¹ must be given for all three components");
+    if (!chi3_h_.empty()) KH_TRY(upload_center(chi3_h_.data(), tdt, &chi3_));
+    std::vector<T*> pole_sigma(poles_.size(), nullptr);
+    for (size_t q = 0; q < poles_.size(); ++q) KH_TRY(upload_center(poles_[q].sigma.data(), tdt, &pole_sigma[q]));
     auto cidx = [&](int i, int j, int k) { return origin_ + (long long)k * plane_ + (long long)j * pitch_ + i; };
     auto center = [&](int i, int j, int k) { return (size_t(k) * n_[1] + j) * n_[0] + i; };
     // Sparse source table: entries per cell in injection order
     // (components Ex..Hz, then sources in order; Kernels.jl:455-463, Sources.jl:330-340).
     struct Ent { long long cell; int src, comp; std::complex<double> amp; int i, j, k; long long q; };
     std::vector<Ent> ents;
+    {
+      size_t cap = 0;
+      for (const SrcH& s : srcs_) cap += size_t(s.d.dims[0]) * s.d.dims[1] * s.d.dims[2];
+      ents.reserve(cap);
+    }
     for (int comp = 0; comp < 6; ++comp)
       for (size_t si = 0; si < srcs_.size(); ++si) {
         const SrcH& s = srcs_[si];
@@ -487,7 +511,9 @@ class Sim : public SimBase {
               ents.push_back({cidx(gi, gj, gk), int(si), comp, std::complex<double>(aT.real(), aT.imag()), gi, gj, gk, q});
             }
       }
-    std::stable_sort(ents.begin(), ents.end(), [](const Ent& a, const Ent& b) { return a.cell < b.cell; });
+    // one source, or sources on disjoint increasing boxes, come out sorted already
+    auto by_cell = [](const Ent& a, const Ent& b) { return a.cell < b.cell; };
+    if (!std::is_sorted(ents.begin(), ents.end(), by_cell)) std::stable_sort(ents.begin(), ents.end(), by_cell);
     // Special cells keep their B|D state: E sources, χ3 and poles (E half), H
     // sources (H half).  An all-zero χ3 or pole array counts as present.
     bool anySpecialE = !chi3_h_.empty() || !poles_.empty(), anySpecialH = false;
@@ -496,6 +522,12 @@ class Sim : public SimBase {
     std::vector<long long> slot_cell;
     std::vector<uint32_t> slot_bits;
     std::vector<Cplx<T>> ent_amp;
+    slot_off.reserve(ents.size() + 1);
+    ent_src.reserve(ents.size());
+    ent_comp.reserve(ents.size());
+    ent_amp.reserve(ents.size());
+    slot_cell.reserve(ents.size());
+    slot_bits.reserve(ents.size());
     for (size_t e = 0; e < ents.size();) {
       size_t e2 = e;
       const int slot = int(slot_off.size() - 1);
@@ -551,30 +583,14 @@ class Sim : public SimBase {
       if (msb && sigmask_b_ && (pml_axis_[nx] || pml_axis_[pv])) KH_TRY(alloc_field(&CB_[c]));
       if (msd && sigmask_d_ && (pml_axis_[nx] || pml_axis_[pv])) KH_TRY(alloc_field(&CD_[c]));
     }
-    // materials: compact uploads scattered into the padded layout on the device
-    if (geo_set_) KH_TRY(build_geometry());
-    const int tdt = sizeof(T) == 4 ? KH_F32 : KH_F64;
-    for (int c = 0; c < 3; ++c) {
-      if (att_eps_[c].ptr) KH_TRY(upload_center(att_eps_[c].ptr, att_eps_[c].dtype, &eps_[c]));
-      else if (!eps_h_[c].empty()) KH_TRY(upload_center(eps_h_[c].data(), tdt, &eps_[c]));
-      if (att_mu_[c].ptr) KH_TRY(upload_center(att_mu_[c].ptr, att_mu_[c].dtype, &mu_[c]));
-      else if (!mu_h_[c].empty()) KH_TRY(upload_center(mu_h_[c].data(), tdt, &mu_[c]));
-      if (!msigd_h_[c].empty()) KH_TRY(upload_center(msigd_h_[c].data(), tdt, &msigd_[c]));
-      if (!msigb_h_[c].empty()) KH_TRY(upload_center(msigb_h_[c].data(), tdt, &msigb_[c]));
-    }
-    if ((eps_[0] != nullptr) != (eps_[2] != nullptr) || (eps_[0] != nullptr) != (eps_[1] != nullptr))
-      return fail(KH_ERR_INVALID, "per-voxel ε⁻¹ must be given for all three components");
-    if ((mu_[0] != nullptr) != (mu_[2] != nullptr) || (mu_[0] != nullptr) != (mu_[1] != nullptr))
-      return fail(KH_ERR_INVALID, "per-voxel μ⁻¹ must be given for all three components");
-    if (!chi3_h_.empty()) KH_TRY(upload_center(chi3_h_.data(), tdt, &chi3_));
-    for (auto& p : poles_) {
+    for (size_t q = 0; q < poles_.size(); ++q) {
       PoleD pd;
-      KH_TRY(upload_center(p.sigma.data(), tdt, &pd.sigma));
+      pd.sigma = pole_sigma[q];
       for (int c = 0; c < 3; ++c) {
         KH_TRY(alloc_field(&pd.P[c]));
         KH_TRY(alloc_field(&pd.Pp[c]));
       }
-      pd.c = p.c;
+      pd.c = poles_[q].c;
       poles_d_.push_back(pd);
     }
     for (int a = 0; a < 3; ++a) {
