@@ -197,13 +197,14 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel: str):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+def ncu_traffic(kernel: str, workload: str = "waveguide"):
+    """DRAM bytes per launch of `kernel` on `workload` from the committed ncu
+    summary, if any (keys "<workload>:<kernel>", the waveguide's without prefix)."""
     p = ROOT / "profiles" / "dram_traffic.json"
     if not p.exists():
         return None
     d = json.loads(p.read_text())
-    v = d.get(kernel)
+    v = d.get(kernel if workload == "waveguide" else f"{workload}:{kernel}")
     return None if v is None else float(v)
 
 
@@ -366,7 +367,7 @@ def run_ours(args, world, rank, local_rank):
         "roofline": {"bound": "hbm", "kernel": e_kernel, "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "algorithmic_bytes_per_launch": e_bytes,
-                     "traffic": ncu_traffic(e_kernel) if _workload_name == "waveguide" else None,
+                     "traffic": ncu_traffic(e_kernel, _workload_name),
                      "h_kernel": {"achieved": h_bytes / (h_ms / rsteps / 1e3) / 1e9,
                                   "algorithmic_bytes_per_launch": h_bytes, "ms_per_launch": h_ms / rsteps,
                                   "frac": h_bytes / (h_ms / rsteps / 1e3) / 1e9 / peak},
