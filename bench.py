@@ -213,6 +213,9 @@ WORKLOADS = {
     "dispersive": ("dispersive 256^3 FP32, 12-cell CPML (CUDA-path semantics), eps 2.25 slab with chi3=1e-3, "
                    "4 Lorentz (eps_inf 2, sigma 1, f0 1, gamma 0.05) + 4 Drude (eps_inf 1, wp 5, gamma 0.1) "
                    "spheres (seed 42), Ez Gaussian plane source, 6-face box flux x 11 freqs, Kahan FP32 DFT"),
+    "periodic": ("photonic-crystal slab 256x256x128 FP32, periodic x and y (halo wrap after every half-step), "
+                 "12-cell CPML in z (CUDA-path semantics), Si slab 0.22 um with a 0.4 um square lattice of "
+                 "0.12 um air holes, Ex plane-wave current plane, two 21-frequency flux planes, Kahan FP32 DFT"),
 }
 _workload_name = "waveguide"
 
@@ -773,7 +776,8 @@ def main(argv=None):
     ap.add_argument("--adjoint-compare-modes", action="store_true",
                     help="also the other mode's FP32 gradient of the same inputs")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="waveguide",
-                    help="waveguide: the 320x192x128 heterogeneous grid (default); dispersive: 256^3 ADE + chi3")
+                    help="waveguide: the 320x192x128 heterogeneous grid (default); dispersive: 256^3 ADE + chi3; "
+                         "periodic: 256x256x128 photonic-crystal slab, periodic x/y")
     args = ap.parse_args(argv)
     global _workload_name
     _workload_name = args.workload

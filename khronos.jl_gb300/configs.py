@@ -185,6 +185,45 @@ def dispersive(dtype="f32", steps=3000, scale=1.0, seed=42) -> Workload:
                     f"{sim.n[0]}^3, chi3 slab, 4 Lorentz + 4 Drude spheres, PML 12 cells")
 
 
+def photonic_slab(dtype="f32", steps=3000, scale=1.0) -> Workload:
+    """Periodic along x and y (no PML there), 12-cell CPML along z: a silicon
+    slab (ε 12.25, 0.22 µm thick) with a square lattice of air holes (period
+    0.4 µm, radius 0.12 µm) in a 6.4 × 6.4 µm supercell, an Ex current plane
+    1 µm below it spanning the cell (a normal-incidence plane wave), flux
+    planes below and above at 21 frequencies.  256×256×128 at 40 cells/µm;
+    the periodic set-up of the reference's slab examples at benchmark size,
+    with the wrap of both periodic axes after every half-step."""
+    from .boundaries import Periodic
+
+    res = 40 * scale
+    size = (6.4, 6.4, 3.2)
+    pml = 12 / 40
+    g = G.Grid.build(size, (0, 0, 0), res, dtype)
+    a, r = 0.4, 0.12
+    eps = []
+    for comp in (G.EX, G.EY, G.EZ):
+        xs, ys, zs = yee_coords(g, comp)
+        dx = np.mod(xs + a / 2, a) - a / 2
+        dy = np.mod(ys + a / 2, a) - a / 2
+        hole = (dx[:, None] ** 2 + dy[None, :] ** 2 < r * r)[:, :, None]
+        slab = (np.abs(zs) <= 0.11)[None, None, :]
+        e = np.where(slab & ~hole, 12.25, 1.0)
+        eps.append(1.0 / e)
+    src = UniformSource(time_profile=GaussianPulseSource(fcen=FCEN, fwidth=0.25 * FCEN), component=G.EX,
+                        center=(0.0, 0.0, -1.0), size=(math.inf, math.inf, 0.0))
+    fw = 0.25 * FCEN
+    freqs = _freqs(21, FCEN - 0.5 * fw, FCEN + 0.5 * fw)
+    # flux planes just inside the periodic span (a full-span plane would read
+    # the staggered layer on the wrap faces)
+    fms = [FluxMonitor(center=(0.0, 0.0, zp), size=(0.98 * size[0], 0.98 * size[1], 0.0), frequencies=freqs)
+           for zp in (-1.2, 1.0)]
+    sim = Simulation(cell_size=size, resolution=res, sources=[src], boundaries=[[0.0, 0.0], [0.0, 0.0], [pml, pml]],
+                     boundary_conditions=[[Periodic(), Periodic()], [Periodic(), Periodic()], [None, None]],
+                     monitors=fms, dtype=dtype, eps_inv=eps)
+    return Workload("periodic", sim, steps, fms,
+                    f"{sim.n[0]}x{sim.n[1]}x{sim.n[2]} photonic-crystal slab, periodic x/y, PML 12 cells in z")
+
+
 @dataclass
 class BendWorkload:
     """Inverse-design workload: forward and straight-reference simulations,
@@ -330,4 +369,4 @@ def serving_stream(n_requests: int = 512, seed: int = 2024, dtype="f32") -> List
     return out
 
 
-BUILDERS = {"dipole": dipole, "waveguide": waveguide, "dispersive": dispersive}
+BUILDERS = {"dipole": dipole, "waveguide": waveguide, "dispersive": dispersive, "periodic": photonic_slab}

@@ -135,7 +135,6 @@ struct HalfStepParams {
   int zplanes;  // z planes marched by one CTA of the TMA-staged kernel
   int xprefetch;   // TMA-staged kernel, x-CPML state into L2: 0 tile-wide (H half), 1 per lane (H), 2 per lane (H, E)
   int xpf_dist;    // planes ahead of the per-lane x-CPML prefetch
-  int ring_release;  // TMA-staged kernel: 1 = the last warp done with a stage re-issues it (no CTA barrier per plane)
   T dt, inv_d[3];
   T cd[3];  // Δt·(1/Δ_a): curl coefficients of the TMA-staged kernel
 

@@ -735,7 +735,6 @@ class Sim : public SimBase {
     zplanes_ = choose_zplanes();
     if (const char* xv = std::getenv("KHRONOS_GB300_XPREFETCH")) xprefetch_ = std::min(2, std::max(0, std::atoi(xv)));
     if (const char* dv = std::getenv("KHRONOS_GB300_XPF_DIST")) xpf_dist_ = std::min(8, std::max(1, std::atoi(dv)));
-    if (const char* rv = std::getenv("KHRONOS_GB300_RING_RELEASE")) ring_release_ = std::atoi(rv) != 0;
     if (const char* sv = std::getenv("KHRONOS_GB300_TEST_STALL")) stall_tx_ = std::string(sv) == "1" ? 16u : 0u;
     // the zeroing and uploads above ran on the legacy default stream; wait for
     // them only (work of other simulations on non-blocking streams goes on)
@@ -1988,7 +1987,6 @@ class Sim : public SimBase {
     p.zplanes = zplanes_;
     p.xprefetch = xprefetch_;
     p.xpf_dist = xpf_dist_;
-    p.ring_release = ring_release_ ? 1 : 0;
     p.dt = dt_;
     for (int a = 0; a < 3; ++a) {
       p.inv_d[a] = T(1) / delta_[a];
@@ -2097,7 +2095,6 @@ class Sim : public SimBase {
   int zplanes_ = 10;
   int xprefetch_ = 2;        // x-CPML state prefetch mode (HalfStepParams::xprefetch)
   int xpf_dist_ = 3;
-  bool ring_release_ = false;  // TMA-staged kernel stage-release protocol
   int tma_slots_ = 0;  // SMs × resident TMA-kernel CTAs per SM
   kh::TmaMaps maps_h_, maps_e_;
 

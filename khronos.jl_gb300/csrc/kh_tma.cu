@@ -171,19 +171,8 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
   // the failure-detection test instantiation waits briefly for bytes that never come
   constexpr long long kLimit = STALL ? kStallWaitLimit : kWaitLimit;
 
-  // ring_release protocol: per stage, the number of warps done with its load
-  // (the last one re-issues the stage), a stop flag, and how many loads were
-  // issued (for the drain before the CTA leaves)
-  __shared__ int s_done[kTmaStages];
-  __shared__ int s_stop;
-  __shared__ int s_issued;
   if (tid == 0) {
-    for (int st = 0; st < kTmaStages; ++st) {
-      mbar_init(&bars[st], 1);
-      s_done[st] = 0;
-    }
-    s_stop = 0;
-    s_issued = 0;
+    for (int st = 0; st < kTmaStages; ++st) mbar_init(&bars[st], 1);
     mbar_fence_init();
   }
   __syncthreads();
@@ -248,7 +237,6 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
   if (tid == 0) {
     const int first = min(kTmaStages, N + 1);
     for (int n = 0; n < first; ++n) issue(n);
-    s_issued = first;
   }
 
   // static per-thread data along the march
@@ -471,52 +459,19 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
     }
     // every thread is done with load c (H: current, E: z neighbour); its
     // stage takes load c + kTmaStages
-    if (p.ring_release) {
-      // the last warp done with the stage re-issues it; the others go on
-      // (up to kTmaStages − 1 planes ahead, held back by the full barriers)
-      __syncwarp();
-      const bool wbad = __any_sync(0xffffffffu, bad);
-      if (lane == 0) {
-        if (wbad) atomicExch(&s_stop, 1);
-        __threadfence_block();
-        const int st = c % kTmaStages;
-        if (atomicAdd(&s_done[st], 1) == kTmaY - 1) {
-          s_done[st] = 0;
-          __threadfence_block();
-          if (!*(volatile int*)&s_stop && c + kTmaStages <= N) {
-            fence_proxy_async();
-            issue(c + kTmaStages);
-            atomicMax(&s_issued, c + kTmaStages + 1);
-          }
-        }
+    if (__syncthreads_or(bad)) {
+      // stop: wait (bounded) for the copies this CTA issued, then leave
+      if (tid == 0) {
+        const int issued = min(c + kTmaStages, N + 1);
+        for (int n = c; n < issued; ++n) mbar_wait(&bars[n % kTmaStages], uint32_t((n / kTmaStages) & 1), kLimit);
       }
-      __syncwarp();
-      if (*(volatile int*)&s_stop) break;
-    } else {
-      if (__syncthreads_or(bad)) {
-        // stop: wait (bounded) for the copies this CTA issued, then leave
-        if (tid == 0) {
-          const int issued = min(c + kTmaStages, N + 1);
-          for (int n = c; n < issued; ++n) mbar_wait(&bars[n % kTmaStages], uint32_t((n / kTmaStages) & 1), kLimit);
-        }
-        return;
-      }
-      if (tid == 0 && c + kTmaStages <= N) {
-        fence_proxy_async();
-        issue(c + kTmaStages);
-      }
+      return;
+    }
+    if (tid == 0 && c + kTmaStages <= N) {
+      fence_proxy_async();
+      issue(c + kTmaStages);
     }
     cur = nxt;
-  }
-  if (p.ring_release) {
-    // drain: every load issued has landed (bounded waits) before the CTA's
-    // shared memory is handed on
-    __syncthreads();
-    if (tid == 0) {
-      const int issued = s_issued;
-      for (int n = max(0, issued - kTmaStages); n < issued; ++n)
-        mbar_wait(&bars[n % kTmaStages], uint32_t((n / kTmaStages) & 1), kLimit);
-    }
   }
 }
 

@@ -83,6 +83,17 @@ def test_dispersive_scaled(kh, oracle, gpu_lib, dtype):
 
 
 @pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_photonic_slab_scaled(kh, oracle, gpu_lib, dtype):
+    """The periodic benchmark workload (x and y wrapped, CPML along z) at a
+    quarter of its resolution: 64×64×32."""
+    from khronos_gb300 import configs
+
+    w = configs.photonic_slab(dtype=dtype, scale=0.25)
+    assert tuple(w.sim.spec().n) == (64, 64, 32) and w.sim.spec().periodic == 3
+    compare(w.sim.spec(), 150, oracle, gpu_lib, TOL[dtype])
+
+
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
 def test_dispersive_cells_pass_matches_full_launch(kh, oracle, gpu_lib, dtype, monkeypatch):
     """χ3 and pole cells updated by the LEAN E launch plus the dispersive-cell
     pass agree with the FULL launch (KHRONOS_GB300_DISP_FIX=0), which does
