@@ -555,11 +555,14 @@ void launch_disp_fix(const DispFixParams<T>& p, void* stream) {
 // ---------------------------------------------------------------------------
 // Periodic wrap.  One block row per periodic axis and component:
 // blockIdx.y = 3·(index of the axis in p.axes) + component; threads stride
-// over the face's (n_t1 × n_t2) cells; each copies both directions of one cell.
+// over the face's (n_t1 × n_t2) cells, t1 the lower of the face's two axes;
+// each copies both directions of one cell.
 template <typename T>
 __global__ void wrap_kernel(const WrapParams<T> p) {
   const int a = p.axes[blockIdx.y / 3], c = blockIdx.y % 3;
-  const int t1 = (a + 1) % 3, t2 = (a + 2) % 3;
+  // the face's lower axis runs fastest across threads: x on the y and z
+  // faces (coalesced rows), y on the x face (one element per row there)
+  const int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
   const long long st[3] = {1, p.pitch, p.plane};
   const long long face = (long long)p.n[t1] * p.n[t2];
   T* f = p.O[c];
