@@ -4,9 +4,10 @@
 // Device layout of every full-domain array (fields, materials, auxiliaries):
 //   element (i, j, k), -1 <= i,j,k <= n, lives at
 //     origin + (k * (ny + 2) + j) * pitch + i
-//   with origin = ((ny + 2) + 1) * pitch + XOFF and XOFF = VEC elements
-//   (16 bytes), so x = 0 of every row is 16-byte aligned and the row pitch is
-//   a multiple of 128 bytes.  The ring i,j,k in {-1, n} (and the row padding)
+//   with origin = ((ny + 2) + 1) * pitch + XOFF and XOFF = 32 bytes of
+//   elements (xoff<T>()), so x = 0 of every row starts a 32-byte sector (a
+//   row segment of 64 cells covers whole sectors) and the row pitch is a
+//   multiple of 128 bytes.  The ring i,j,k in {-1, n} (and the row padding)
 //   is never written: it is the reference's zero ghost layer / staggered wall.
 #pragma once
 
@@ -15,6 +16,15 @@
 #include <cstdint>
 
 namespace kh {
+
+#ifndef KH_XOFF_BYTES
+#define KH_XOFF_BYTES 32
+#endif
+// Elements before x = 0 in every padded row (see the layout above).
+template <typename T>
+constexpr int xoff() {
+  return KH_XOFF_BYTES / int(sizeof(T));
+}
 
 constexpr int kMaxPoles = 4;
 constexpr int kBlockY = 4;      // rows per CTA

@@ -164,11 +164,13 @@ class Sim : public SimBase {
     for (int a = 0; a < 3; ++a) n_[a] = desc.n[a];
     dt_ = T(desc.dt);
     for (int a = 0; a < 3; ++a) delta_[a] = T(desc.delta[a]);
+    static_assert(kh::xoff<T>() >= VN && kh::xoff<T>() % VN == 0, "row offset keeps the vector alignment");
     const long long nxp = (n_[0] + VN - 1) / VN * VN;
     const long long align = 128 / sizeof(T);
-    pitch_ = (VN + nxp + VN + align - 1) / align * align;
+    const long long xo = kh::xoff<T>();
+    pitch_ = (xo + nxp + VN + align - 1) / align * align;
     plane_ = pitch_ * (n_[1] + 2);
-    origin_ = plane_ + pitch_ + VN;
+    origin_ = plane_ + pitch_ + xo;
     total_ = plane_ * (n_[2] + 2);
     nxb_ = int((n_[0] + 32 * kh::kVN - 1) / (32 * kh::kVN));
     for (int a = 0; a < 3; ++a) {
@@ -593,6 +595,17 @@ class Sim : public SimBase {
       pd.c = poles_[q].c;
       poles_d_.push_back(pd);
     }
+    // The small tables (CPML coefficients, the source table) go up in one
+    // asynchronous copy from a pinned staging buffer into one device block,
+    // released after the synchronisation at the end of prepare.
+    std::vector<char> stg;
+    std::vector<std::pair<void**, size_t>> stg_out;
+    auto stage = [&](const void* h, size_t bytes, void** out) {
+      const size_t off = (stg.size() + 255) & ~size_t(255);
+      stg.resize(off + bytes);
+      std::memcpy(stg.data() + off, h, bytes);
+      stg_out.push_back({out, off});
+    };
     for (int a = 0; a < 3; ++a) {
       // CPML coefficient tables (σ, 1-σ, 1/(1+σ), 1+σ) in the run's precision
       for (int h = 0; h < 2; ++h) {
@@ -602,24 +615,57 @@ class Sim : public SimBase {
           const T sv = sg[i];
           tab[i] = {sv, T(1) - sv, T(1) / (T(1) + sv), T(1) + sv};
         }
-        KH_TRY(upload_raw(tab.data(), tab.size() * sizeof(kh::AxisCoef<T>), (void**)(h ? &axb_[a] : &axd_[a])));
+        stage(tab.data(), tab.size() * sizeof(kh::AxisCoef<T>), (void**)(h ? &axb_[a] : &axd_[a]));
       }
     }
     nsrc_ = int(srcs_.size());
     if (!ent_src.empty()) {
-      KH_TRY(upload_raw(slot_off.data(), slot_off.size() * sizeof(int), (void**)&slot_off_));
-      KH_TRY(upload_raw(ent_src.data(), ent_src.size() * sizeof(int), (void**)&ent_src_));
-      KH_TRY(upload_raw(ent_comp.data(), ent_comp.size() * sizeof(int), (void**)&ent_comp_));
-      KH_TRY(upload_raw(ent_amp.data(), ent_amp.size() * sizeof(Cplx<T>), (void**)&ent_amp_));
+      stage(slot_off.data(), slot_off.size() * sizeof(int), (void**)&slot_off_);
+      stage(ent_src.data(), ent_src.size() * sizeof(int), (void**)&ent_src_);
+      stage(ent_comp.data(), ent_comp.size() * sizeof(int), (void**)&ent_comp_);
+      stage(ent_amp.data(), ent_amp.size() * sizeof(Cplx<T>), (void**)&ent_amp_);
       ent_amp_h_ = ent_amp;
-      KH_TRY(upload_raw(slot_cell.data(), slot_cell.size() * sizeof(long long), (void**)&slot_cell_));
+      stage(slot_cell.data(), slot_cell.size() * sizeof(long long), (void**)&slot_cell_);
       nslots_ = int(slot_cell.size());
       slot_off_h_ = slot_off;
       ent_src_h_ = ent_src;
       ent_comp_h_ = ent_comp;
       std::vector<kh::SlotPack<T>> pack = pack_slots();
-      KH_TRY(upload_raw(pack.data(), pack.size() * sizeof(kh::SlotPack<T>), (void**)&slot_pack_));
+      stage(pack.data(), pack.size() * sizeof(kh::SlotPack<T>), (void**)&slot_pack_);
     }
+    void* stg_pinned = nullptr;
+    if (!stg.empty()) {
+      void* dev = nullptr;
+      KH_CUDA(kh_host::dev_alloc(&dev, stg.size(), cudaStreamLegacy));
+      allocs_.push_back(dev);
+      device_bytes_ += int64_t(stg.size());
+      stg_pinned = kh_host::pinned_get(stg.size());
+      cudaError_t e = stg_pinned ? cudaSuccess : cudaErrorMemoryAllocation;
+      if (e == cudaSuccess) {
+        std::memcpy(stg_pinned, stg.data(), stg.size());
+        e = cudaMemcpyAsync(dev, stg_pinned, stg.size(), cudaMemcpyHostToDevice, cudaStreamLegacy);
+      }
+      if (e != cudaSuccess) {
+        if (stg_pinned) {
+          cudaStreamSynchronize(cudaStreamLegacy);
+          kh_host::pinned_put(stg_pinned, stg.size());
+        }
+        return fail(KH_ERR_CUDA, std::string("table upload: ") + cudaGetErrorString(e));
+      }
+      for (auto& o : stg_out) *o.first = static_cast<char*>(dev) + o.second;
+    }
+    // the staging buffer goes back to the pool once the copies queued so far
+    // have run (every exit from here on synchronises the legacy stream first)
+    struct StgRelease {
+      void* p;
+      size_t n;
+      ~StgRelease() {
+        if (p) {
+          cudaStreamSynchronize(cudaStreamLegacy);
+          kh_host::pinned_put(p, n);
+        }
+      }
+    } stg_release{stg_pinned, stg.size()};
     // Cell classes and the per-row-segment plane bitmasks (word (k/64, j, xb),
     // bit k%64), computed on the device from the material arrays and the
     // source table.

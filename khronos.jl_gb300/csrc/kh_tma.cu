@@ -97,7 +97,8 @@ __device__ __forceinline__ void l2_prefetch(const void* ptr) {
 
 template <typename T>
 struct TmaGeom {
-  static constexpr int HX = 16 / int(sizeof(T));  // x halo = XOFF of the layout
+  static constexpr int HX = 16 / int(sizeof(T));  // x halo of the curl-source box (16 bytes)
+  static constexpr int XO = xoff<T>();             // padded x of cell x = 0
   static constexpr int AX = kTmaX + HX;          // A box row length
   static constexpr int A_BYTES = AX * (kTmaY + 1) * int(sizeof(T));
   static constexpr int A_ELEMS = ((A_BYTES + 127) / 128 * 128) / int(sizeof(T));
@@ -198,19 +199,19 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
     }
     mbar_arrive_expect_tx(&bars[st], a_bytes + (comp ? o_bytes : 0u));
     const int zc = plane + 1;                      // padded plane index
-    const int ax = H ? G::HX + x_tile : x_tile;    // padded x of the A box
+    const int ax = H ? G::XO + x_tile : G::XO - G::HX + x_tile;  // padded x of the A box
     const int ay = H ? 1 + y_tile : y_tile;        // padded y of the A box
 #pragma unroll
     for (int c = 0; c < 3; ++c) tma_load_3d(dst + c * G::A_ELEMS, &maps.a[c], ax, ay, zc, &bars[st]);
     if (comp) {
 #pragma unroll
       for (int c = 0; c < 3; ++c)
-        tma_load_3d(dst + 3 * G::A_ELEMS + c * G::O_ELEMS, &maps.o[c], G::HX + x_tile, 1 + y_tile, zc,
+        tma_load_3d(dst + 3 * G::A_ELEMS + c * G::O_ELEMS, &maps.o[c], G::XO + x_tile, 1 + y_tile, zc,
                     &bars[st]);
       if (pervox) {
 #pragma unroll
         for (int c = 0; c < 3; ++c)
-          tma_load_3d(dst + 3 * G::A_ELEMS + (3 + c) * G::O_ELEMS, &maps.m[c], G::HX + x_tile, 1 + y_tile,
+          tma_load_3d(dst + 3 * G::A_ELEMS + (3 + c) * G::O_ELEMS, &maps.m[c], G::XO + x_tile, 1 + y_tile,
                       zc, &bars[st]);
       }
       // LEAN variants: the CPML state of the plane (B|D, U, W where the tile
@@ -227,9 +228,9 @@ __global__ void __launch_bounds__(32 * kTmaY, (tma_min_blocks<T, FULL>()))
         const bool af[3] = {tfx, tfy, tfz};
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          if (p.Ts[c]) tma_prefetch_3d(&maps.t[c], G::HX + x_tile, 1 + y_tile, zc);
-          if (p.U[c] && af[(c + 1) % 3]) tma_prefetch_3d(&maps.u[c], G::HX + x_tile, 1 + y_tile, zc);
-          if (p.W[c] && af[c]) tma_prefetch_3d(&maps.w[c], G::HX + x_tile, 1 + y_tile, zc);
+          if (p.Ts[c]) tma_prefetch_3d(&maps.t[c], G::XO + x_tile, 1 + y_tile, zc);
+          if (p.U[c] && af[(c + 1) % 3]) tma_prefetch_3d(&maps.u[c], G::XO + x_tile, 1 + y_tile, zc);
+          if (p.W[c] && af[c]) tma_prefetch_3d(&maps.w[c], G::XO + x_tile, 1 + y_tile, zc);
         }
       }
     }
