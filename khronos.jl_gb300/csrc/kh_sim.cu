@@ -1875,18 +1875,11 @@ class Sim : public SimBase {
     const cuuint32_t box_o[3] = {cuuint32_t(kh::kTmaX), cuuint32_t(kh::kTmaY), 1};
     const cuuint32_t estr[3] = {1, 1, 1};
     const CUtensorMapDataType dt = sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
-    CUtensorMapL2promotion promo = CU_TENSOR_MAP_L2_PROMOTION_L2_256B;
-    if (const char* pv = std::getenv("KHRONOS_GB300_L2PROMO")) {
-      const int v = std::atoi(pv);
-      promo = v == 0 ? CU_TENSOR_MAP_L2_PROMOTION_NONE
-                     : v == 64 ? CU_TENSOR_MAP_L2_PROMOTION_L2_64B
-                               : v == 128 ? CU_TENSOR_MAP_L2_PROMOTION_L2_128B : CU_TENSOR_MAP_L2_PROMOTION_L2_256B;
-    }
     auto mk = [&](CUtensorMap* m, T* base, const cuuint32_t* box) -> kh_status {
       // base points at element (-1,-1,-1) - XOFF + ... : the allocation start
       CUresult r = encode(m, dt, 3, static_cast<void*>(base), dims, strides, box, estr,
                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                          promo, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
       if (r != CUDA_SUCCESS) return fail(KH_ERR_CUDA, "cuTensorMapEncodeTiled failed");
       return KH_OK;
     };
