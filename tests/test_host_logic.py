@@ -58,6 +58,26 @@ def test_waveguide_spec_shapes(kh):
     assert np.isclose(1 / np.min(eps[0]), 12.25) and np.isclose(1 / np.max(eps[0]), 2.085)
 
 
+def test_photonic_slab_spec(kh):
+    """The periodic benchmark workload: x and y wrapped without PML, 12-cell
+    CPML along z, flux planes inside the periodic span, a hole lattice in the
+    slab (air at the lattice points, silicon between them)."""
+    from khronos_gb300 import configs
+
+    sp = configs.photonic_slab(dtype="f32").sim.spec()
+    assert tuple(sp.n) == (256, 256, 128) and sp.periodic == 3
+    assert tuple(sp.pml_lo) == (0, 0, 12) and tuple(sp.pml_hi) == (0, 0, 12)
+    assert len(sp.monitors) == 8
+    for m in sp.monitors:
+        assert m.dims[0] < sp.n[0] and m.dims[1] < sp.n[1]
+    eps_x = [arr for kind, c, arr in sp.materials if kind == 0 and c == 0][0]
+    mid = sp.n[2] // 2
+    slab = 1.0 / eps_x[:, :, mid]
+    assert np.isclose(slab.max(), 12.25) and np.isclose(slab.min(), 1.0)
+    assert 0.2 < np.mean(slab == 1.0) < 0.4  # π·0.12²/0.4² ≈ 0.28 of the area is hole
+    assert np.all(1.0 / eps_x[:, :, 0] == 1.0)
+
+
 def test_flux_formula_matches_reference_loop(kh):
     from khronos_gb300.monitors import flux_from_dft
 
