@@ -147,8 +147,6 @@ def flat_f(a: np.ndarray) -> np.ndarray:
 
 def flat_complex(a: np.ndarray) -> np.ndarray:
     """Interleaved (re, im) float64, x fastest."""
-    z = np.asarray(a, dtype=np.complex128).ravel(order="F")
-    out = np.empty(2 * z.size, dtype=np.float64)
-    out[0::2] = z.real
-    out[1::2] = z.imag
-    return out
+    # a contiguous complex128 array is already (re, im) pairs in memory
+    z = np.ascontiguousarray(np.asarray(a, dtype=np.complex128).ravel(order="F"))
+    return z.view(np.float64)
