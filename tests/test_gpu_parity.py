@@ -143,8 +143,14 @@ def test_dispersive_cells_pass_on_an_odd_grid(kh, oracle, gpu_lib, dtype, monkey
     eps = apply_chi1_correction([1.0 / rng.uniform(1.0, 3.0, size=n) for _ in range(3)], poles, dt, T=np.float64)
     src = kh.UniformSource(time_profile=kh.GaussianPulseSource(fcen=0.8, fwidth=0.4), component=kh.EZ,
                            center=(0.2, 0, 0), size=(0.4, 0.6, 0.5), amplitude=3.0)
+    # sources on Lorentz cells: their term enters the pass's E = ε⁻¹(D + S − ΣP),
+    # the second (Ex) on cells in the x-CPML, where E also goes through the W stage
+    src2 = kh.UniformSource(time_profile=kh.GaussianPulseSource(fcen=0.8, fwidth=0.4), component=kh.EY,
+                            center=(1.2, -0.55, -0.1), size=(0.4, 0.2, 0.2), amplitude=2.0)
+    src3 = kh.UniformSource(time_profile=kh.GaussianPulseSource(fcen=0.8, fwidth=0.4), component=kh.EX,
+                            center=(1.7, -0.55, -0.1), size=(0.2, 0.2, 0.2), amplitude=2.0)
     mon = kh.DFTMonitor(component=kh.EX, center=(0, 0, 0), size=(3.7, 2.2, 0), frequencies=[0.7, 0.9])
-    sim = kh.Simulation(cell_size=(3.7, 2.2, 1.8), resolution=10, sources=[src], monitors=[mon],
+    sim = kh.Simulation(cell_size=(3.7, 2.2, 1.8), resolution=10, sources=[src, src2, src3], monitors=[mon],
                         boundaries=[[0.3, 0.3]] * 3, dtype=dtype, eps_inv=eps, chi3=chi3, poles=poles)
     spec = sim.spec()
     assert tuple(spec.n) == n
@@ -155,7 +161,10 @@ def test_dispersive_cells_pass_on_an_odd_grid(kh, oracle, gpu_lib, dtype, monkey
         g.step(160)
         out[mode] = ([g.field(c) for c in range(6)], [g.dft(0)])
         g.close()
-    tol = 1e-13 if dtype == "f64" else 1e-6
+    # FP32: the pass applies the W stage of x-CPML pole cells as a correction
+    # of the LEAN launch's result (E' + op·ΔW), the FULL launch in one
+    # expression, so the two round differently
+    tol = 1e-13 if dtype == "f64" else 1e-5
     assert max(field_errors(out["1"][0], out["0"][0])) <= tol
     assert max(dft_errors(out["1"][1], out["0"][1])) <= tol
     monkeypatch.setenv("KHRONOS_GB300_DISP_FIX", "1")
