@@ -74,6 +74,10 @@ class SourceSpec:
     cutoff: float = 0.0
     table: Optional[np.ndarray] = None  # complex128, shape (steps, 2)
 
+    def __post_init__(self):
+        # x fastest in memory, as the library reads it: handing it over is a view
+        self.amp = np.asfortranarray(np.asarray(self.amp, dtype=np.complex128))
+
 
 @dataclass
 class MonitorSpec:
