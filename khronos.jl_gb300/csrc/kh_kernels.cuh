@@ -472,8 +472,8 @@ void launch_dft_read(const Cplx<T>* F, const Cplx<T>* C, double* out, long long 
 
 // FP64 flux reduction in two passes with a fixed summation order: blocks of
 // 1024 cells per frequency write partial sums into `partial` (room for
-// partial_cap doubles; at most partial_cap / nf blocks per frequency), one
-// warp per frequency adds them in block order into out[f].
+// partial_cap doubles, partial_cap >= nf; at most partial_cap / nf blocks per
+// frequency), one warp per frequency adds them in block order into out[f].
 template <typename T>
 void launch_flux(const Cplx<T>* e1, const Cplx<T>* e2, const Cplx<T>* h1, const Cplx<T>* h2,
                  const Cplx<T>* c_e1, const Cplx<T>* c_e2, const Cplx<T>* c_h1,
